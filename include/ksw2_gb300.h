@@ -1,0 +1,115 @@
+/*
+ * ksw2_gb300.h -- batched and served entry points of the GB300 ksw2 library
+ * (libksw2gpu.so).  These have no one-to-one counterpart in the reference:
+ * they let a caller that has many independent DP jobs (the gap fills and end
+ * extensions of align.c:mb_align1, the rescue jobs of pe.c:mb_matesw_core)
+ * hand them over in one call instead of one synchronous call per job.
+ * Every job's result is bit-identical to the per-call ksw_extz2_sse /
+ * ksw_extd2_sse / ksw_ll_* result on the same inputs.
+ *
+ * Conventions: plain pointers and sizes; host buffers unless a name says
+ * "dev"; return value 0 on success or a negative KSW2G_E* code, with a
+ * thread-local message from ksw2g_last_error().
+ */
+#ifndef KSW2_GB300_H_
+#define KSW2_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KSW2G_OK           0
+#define KSW2G_E_CUDA      -1  /* a CUDA call failed */
+#define KSW2G_E_ARG       -2  /* invalid argument */
+#define KSW2G_E_BAND      -3  /* band too wide for the instantiated kernels */
+#define KSW2G_E_NOMEM     -4  /* device or pinned allocation failed */
+#define KSW2G_E_CAPACITY  -5  /* caller's output buffer too small */
+#define KSW2G_E_UNSUPPORTED -6 /* e.g. GENERIC_SC with m > 16 */
+
+typedef struct ksw2g_ctx ksw2g_ctx_t;
+typedef struct ksw2g_batch ksw2g_batch_t;
+
+/* One extension job.  qoff/toff index qbuf/tbuf (codes 0..m-1, one byte per
+ * base); w, zdrop, end_bonus and flag mean what they mean for ksw_extz2_sse. */
+typedef struct {
+	int64_t qoff, toff;
+	int32_t qlen, tlen;
+	int32_t w, zdrop, end_bonus, flag;
+} ksw2g_job_t;
+
+/* Result of one extension job: the ksw_extz_t fields plus counters.
+ * The CIGAR (n_cigar words, len<<4|op) is at cigar[cigar_off].
+ * n_diag: anti-diagonals computed; cells: nominal band cells computed. */
+typedef struct {
+	int32_t score, max, max_q, max_t, mqe, mqe_t, mte, mte_q;
+	int32_t zdropped, reach_end, n_cigar, n_diag;
+	int64_t cigar_off;
+	int64_t cells;
+} ksw2g_ext_result_t;
+
+/* One local-alignment (ksw_ll) job; xtra as for ksw_ll_u8_core. */
+typedef struct {
+	int64_t qoff, toff;
+	int32_t qlen, tlen;
+	int32_t xtra, pad;
+} ksw2g_ll_job_t;
+
+/* ksw_llrst_t plus the number of target rows processed. */
+typedef struct {
+	int32_t score, te, qe, score2, te2, rows;
+} ksw2g_ll_result_t;
+
+/* ---- context: one CUDA stream and its memory pools on one device ---- */
+int ksw2g_ctx_create(int device, ksw2g_ctx_t **ctx);
+void ksw2g_ctx_destroy(ksw2g_ctx_t *ctx);
+void *ksw2g_ctx_stream(ksw2g_ctx_t *ctx);          /* the cudaStream_t all work of ctx runs on */
+int ksw2g_ctx_sync(ksw2g_ctx_t *ctx);
+/* Device bytes a batch may hold for traceback at once (jobs run in waves
+ * under this budget).  Default 8 GiB. */
+int ksw2g_ctx_set_tb_budget(ksw2g_ctx_t *ctx, int64_t bytes);
+const char *ksw2g_last_error(void);
+
+/* ---- one-shot batch: host buffers in, host results out ---- */
+int ksw2g_ext_batch(ksw2g_ctx_t *ctx, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e, int8_t q2, int8_t e2,
+					int n_jobs, const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+					const uint8_t *tbuf, int64_t tbuf_len,
+					ksw2g_ext_result_t *res, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used);
+
+int ksw2g_ll_batch(ksw2g_ctx_t *ctx, int size, int m, const int8_t *mat, int gapo, int gape,
+				   int n_jobs, const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+				   const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ll_result_t *res);
+
+/* ---- resident batch: upload once, run many times (async), fetch ---- */
+int ksw2g_ext_prepare(ksw2g_ctx_t *ctx, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e, int8_t q2, int8_t e2,
+					  int n_jobs, const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+					  const uint8_t *tbuf, int64_t tbuf_len, ksw2g_batch_t **batch);
+int ksw2g_ll_prepare(ksw2g_ctx_t *ctx, int size, int m, const int8_t *mat, int gapo, int gape,
+					 int n_jobs, const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+					 const uint8_t *tbuf, int64_t tbuf_len, ksw2g_batch_t **batch);
+/* Enqueue DP (+ backtrack) of every job on the context stream; returns at once. */
+int ksw2g_batch_run(ksw2g_ctx_t *ctx, ksw2g_batch_t *batch);
+/* Wait for the batch and copy results (and for extension batches the CIGARs). */
+int ksw2g_ext_fetch(ksw2g_ctx_t *ctx, ksw2g_batch_t *batch, ksw2g_ext_result_t *res, uint32_t *cigar,
+					int64_t cigar_cap, int64_t *cigar_used);
+int ksw2g_ll_fetch(ksw2g_ctx_t *ctx, ksw2g_batch_t *batch, ksw2g_ll_result_t *res);
+/* Kernel launches the last run of this batch enqueued. */
+int ksw2g_batch_launches(const ksw2g_batch_t *batch);
+void ksw2g_batch_free(ksw2g_batch_t *batch);
+
+/* Select the thread-group shape used for extension jobs whose reference
+ * n_col_ (16-byte blocks per anti-diagonal) lies in [ncol_lo, ncol_hi];
+ * shape indexes ksw2g_ext_shapes().  Used by the autotuner. */
+int ksw2g_ext_num_shapes(void);
+int ksw2g_ext_shape_info(int shape, int *group_threads, int *words_per_thread);
+int ksw2g_ext_set_shape(int dual, int mode, int ncol_lo, int ncol_hi, int shape);
+
+/* Measured 32-bit integer instruction throughput of the device (lane-ops per
+ * second), the denominator of the DP kernels' integer-pipe roofline. */
+int ksw2g_probe_int32_peak(int device, double *ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,756 @@
+// capi.cu -- C ABI of libksw2gpu.so: contexts, batches, and the per-call
+// drop-in replacements of the reference's ksw2 entry points.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ksw2.h"
+#include "../../include/ksw2_gb300.h"
+#include "ksw2g.h"
+#include "launch.h"
+#include "host_common.h"
+
+static_assert(sizeof(ksw2g_job_t) == sizeof(ksw2g_job), "job layout");
+static_assert(sizeof(ksw2g_ext_result_t) == sizeof(ksw2g_ext_result), "result layout");
+static_assert(sizeof(ksw2g_ll_job_t) == sizeof(ksw2g_ll_job), "ll job layout");
+static_assert(sizeof(ksw2g_ll_result_t) == sizeof(ksw2g_ll_result), "ll result layout");
+
+namespace ksw2g {
+cudaError_t launch_ext_dp_z2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                             cudaStream_t st);
+cudaError_t launch_ext_dp_d2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                             cudaStream_t st);
+cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,
+                          int max_blocks, cudaStream_t st) {
+  return dual ? launch_ext_dp_d2(mode, shape, P, L, max_blocks, st)
+              : launch_ext_dp_z2(mode, shape, P, L, max_blocks, st);
+}
+
+// shape preference per (dual, mode, n_col); 0 = use the smallest shape that fits
+static const int kMaxPrefCol = 512;
+static int g_pref[2][3][kMaxPrefCol + 1];
+static std::mutex g_pref_mu;
+
+int ext_shape_pick(int dual, int mode, int n_col) {
+  const int fit = ext_shape_for(n_col);
+  if (fit < 0) return -1;
+  if (n_col >= 0 && n_col <= kMaxPrefCol) {
+    const int p = g_pref[dual & 1][mode][n_col] - 1;
+    if (p >= fit && p < kNumExtShapes) return p;
+  }
+  return fit;
+}
+void ext_shape_set_pref(int dual, int mode, int lo, int hi, int shape) {
+  std::lock_guard<std::mutex> g(g_pref_mu);
+  for (int c = lo < 0 ? 0 : lo; c <= hi && c <= kMaxPrefCol; ++c) g_pref[dual & 1][mode][c] = shape + 1;
+}
+}  // namespace ksw2g
+
+using namespace ksw2g;
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string tl_err;
+static int set_err(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+static int set_err(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  tl_err = buf;
+  return code;
+}
+#define CK(x)                                                                                          \
+  do {                                                                                                 \
+    cudaError_t e_ = (x);                                                                              \
+    if (e_ != cudaSuccess) return set_err(KSW2G_E_CUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), \
+                                          __FILE__, __LINE__);                                         \
+  } while (0)
+
+extern "C" const char *ksw2g_last_error(void) { return tl_err.c_str(); }
+
+// ---------------------------------------------------------------- buffers
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t n) {
+    if (n <= cap) return 0;
+    if (p) cudaFree(p);
+    p = nullptr, cap = 0;
+    size_t c = n < 4096 ? 4096 : n + n / 8;
+    if (cudaMalloc(&p, c) != cudaSuccess) {
+      cudaGetLastError();
+      if (cudaMalloc(&p, n) != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        return set_err(KSW2G_E_NOMEM, "cudaMalloc(%zu) failed", n);
+      }
+      c = n;
+    }
+    cap = c;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr, cap = 0;
+  }
+  template <typename T>
+  T *as() const { return (T *)p; }
+};
+struct PinBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t n) {
+    if (n <= cap) return 0;
+    if (p) cudaFreeHost(p);
+    p = nullptr, cap = 0;
+    size_t c = n < 4096 ? 4096 : n + n / 8;
+    if (cudaMallocHost(&p, c) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return set_err(KSW2G_E_NOMEM, "cudaMallocHost(%zu) failed", c);
+    }
+    cap = c;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr, cap = 0;
+  }
+};
+
+// ---------------------------------------------------------------- context
+struct ksw2g_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int nsm = 0;
+  int64_t tb_budget = (int64_t)8 << 30;
+  DevBuf tb_pool;       // traceback rows of the running wave
+  DevBuf one;           // per-call drop-in scratch (device)
+  PinBuf one_h;         // per-call drop-in staging (pinned)
+  ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
+};
+
+extern "C" int ksw2g_ctx_create(int device, ksw2g_ctx_t **out) {
+  if (!out) return set_err(KSW2G_E_ARG, "null output");
+  int ndev = 0;
+  CK(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return set_err(KSW2G_E_ARG, "device %d not present (%d devices)", device, ndev);
+  CK(cudaSetDevice(device));
+  ksw2g_ctx *c = new ksw2g_ctx;
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return set_err(KSW2G_E_CUDA, "cudaStreamCreate failed");
+  }
+  c->nsm = num_sms(device);
+  *out = c;
+  return 0;
+}
+
+extern "C" void ksw2g_batch_free(ksw2g_batch_t *b);
+
+extern "C" void ksw2g_ctx_destroy(ksw2g_ctx_t *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->st);
+  if (c->scratch) ksw2g_batch_free(c->scratch);
+  c->tb_pool.release();
+  c->one.release();
+  c->one_h.release();
+  cudaStreamDestroy(c->st);
+  delete c;
+}
+extern "C" void *ksw2g_ctx_stream(ksw2g_ctx_t *c) { return c ? (void *)c->st : nullptr; }
+extern "C" int ksw2g_ctx_sync(ksw2g_ctx_t *c) {
+  if (!c) return set_err(KSW2G_E_ARG, "null ctx");
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+extern "C" int ksw2g_ctx_set_tb_budget(ksw2g_ctx_t *c, int64_t bytes) {
+  if (!c || bytes < (1 << 20)) return set_err(KSW2G_E_ARG, "budget must be >= 1 MiB");
+  c->tb_budget = bytes;
+  return 0;
+}
+
+// ---------------------------------------------------------------- batches
+struct Bin {
+  int mode, shape;
+  int64_t order_off;
+  int count;
+};
+struct Wave {
+  int j0, j1;            // contiguous job range
+  int64_t tb_bytes;
+  std::vector<Bin> bins;
+};
+
+struct ksw2g_batch {
+  int kind = 0;          // 0 extz2, 1 extd2, 2 ll u8, 3 ll i16
+  int n = 0;
+  ksw2g_ext_params P;
+  int ll_m = 0, ll_gapo = 0, ll_gape = 0, ll_size = 1, ll_slen = 0;
+  DevBuf raw, rawmeta, arena, jobs, order, tb_off, res, bts, cigar, counters, llmat, blist, blist_off;
+  int64_t cigar_cap = 0;
+  int n_counters = 0;
+  std::vector<Wave> waves;
+  int launches = 0;
+  int64_t total_cells_hint = 0;
+};
+
+extern "C" void ksw2g_batch_free(ksw2g_batch_t *b) {
+  if (!b) return;
+  for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->tb_off, &b->res, &b->bts, &b->cigar,
+                    &b->counters, &b->llmat, &b->blist, &b->blist_off})
+    d->release();
+  delete b;
+}
+extern "C" int ksw2g_batch_launches(const ksw2g_batch_t *b) { return b ? b->launches : 0; }
+
+// Upload raw sequences and pack them into the padded arena.  Writes the padded
+// offsets of query s and target s to qpad[s], tpad[s].
+static int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, const int32_t *qlen,
+                           const int64_t *toff, const int32_t *tlen, const uint8_t *qbuf, int64_t qbuf_len,
+                           const uint8_t *tbuf, int64_t tbuf_len, std::vector<int64_t> &qpad,
+                           std::vector<int64_t> &tpad) {
+  qpad.resize(n), tpad.resize(n);
+  int64_t a = 0;
+  for (int i = 0; i < n; ++i) {
+    qpad[i] = a + 32, a += slot_bytes(qlen[i]);
+    tpad[i] = a + 32, a += slot_bytes(tlen[i]);
+  }
+  const int64_t arena_bytes = a + 64;
+  int rc;
+  if ((rc = b->arena.ensure(arena_bytes))) return rc;
+  if ((rc = b->raw.ensure(qbuf_len + tbuf_len + 16))) return rc;
+  // metadata: raw offsets (2n int64), lengths (2n int32), dst offsets (2n int64)
+  const size_t meta = (size_t)2 * n * (8 + 4 + 8);
+  if ((rc = b->rawmeta.ensure(meta))) return rc;
+  std::vector<uint8_t> hm(meta);
+  int64_t *ro = (int64_t *)hm.data();
+  int32_t *ln = (int32_t *)(ro + 2 * n);
+  int64_t *dof = (int64_t *)(ln + 2 * n);
+  for (int i = 0; i < n; ++i) {
+    ro[i] = qoff[i], ln[i] = qlen[i], dof[i] = qpad[i];
+    ro[n + i] = qbuf_len + toff[i], ln[n + i] = tlen[i], dof[n + i] = tpad[i];
+  }
+  uint8_t *raw = b->raw.as<uint8_t>();
+  if (qbuf_len) CK(cudaMemcpyAsync(raw, qbuf, qbuf_len, cudaMemcpyHostToDevice, c->st));
+  if (tbuf_len) CK(cudaMemcpyAsync(raw + qbuf_len, tbuf, tbuf_len, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(b->rawmeta.p, hm.data(), meta, cudaMemcpyHostToDevice, c->st));
+  const int64_t *dro = b->rawmeta.as<int64_t>();
+  const int32_t *dln = (const int32_t *)(dro + 2 * n);
+  const int64_t *ddof = (const int64_t *)(dln + 2 * n);
+  CK(launch_pack(2 * n, raw, dro, dln, b->arena.as<uint8_t>(), ddof, c->st));
+  // the H2D source buffers may be reused by the caller after return
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+static int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+                            int8_t q2, int8_t e2, int n, const ksw2g_job_t *jobs, const uint8_t *qbuf,
+                            int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len) {
+  if (n < 0 || (n > 0 && !jobs) || !mat) return set_err(KSW2G_E_ARG, "bad batch arguments");
+  CK(cudaSetDevice(c->device));
+  b->kind = dual ? 1 : 0;
+  b->n = n;
+  b->launches = 0;
+  derive_ext_params(dual, m, mat, q, e, q2, e2, b->P);
+  std::vector<int64_t> qo(n), to(n);
+  std::vector<int32_t> ql(n), tl(n);
+  std::vector<int> shape(n), mode(n);
+  std::vector<int64_t> foot(n);
+  int64_t cig = 0;
+  for (int i = 0; i < n; ++i) {
+    const ksw2g_job_t &J = jobs[i];
+    if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
+        J.toff + J.tlen > tbuf_len)
+      return set_err(KSW2G_E_ARG, "job %d: sequence out of buffer bounds", i);
+    if ((J.flag & KSW_EZ_GENERIC_SC) && m > 16)
+      return set_err(KSW2G_E_UNSUPPORTED, "job %d: GENERIC_SC needs m <= 16 on the device (m=%d)", i, m);
+    qo[i] = J.qoff, to[i] = J.toff, ql[i] = J.qlen, tl[i] = J.tlen;
+    mode[i] = ext_mode(J.flag);
+    const bool live = J.qlen > 0 && J.tlen > 0 && !b->P.skip_all;
+    const int nc = live ? ext_ncol(J.qlen, J.tlen, J.w) : 1;
+    shape[i] = ext_shape_pick(dual, mode[i], nc);
+    if (shape[i] < 0)
+      return set_err(KSW2G_E_BAND, "job %d: band of %d 16-byte blocks exceeds the widest kernel shape", i, nc);
+    foot[i] = (live && mode[i] != 0) ? (((int64_t)(J.qlen + J.tlen - 1) * nc * 16 + 15) & ~(int64_t)15) : 0;
+    if (foot[i] > c->tb_budget)
+      return set_err(KSW2G_E_CAPACITY, "job %d: traceback needs %lld bytes, budget %lld", i, (long long)foot[i],
+                     (long long)c->tb_budget);
+    if (mode[i] != 0) cig += J.qlen + J.tlen + 1;
+  }
+  std::vector<int64_t> qpad, tpad;
+  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), qbuf, qbuf_len, tbuf, tbuf_len,
+                           qpad, tpad);
+  if (rc) return rc;
+  // device job table
+  std::vector<ksw2g_job> dj(n);
+  for (int i = 0; i < n; ++i) {
+    dj[i] = ksw2g_job{qpad[i], tpad[i], jobs[i].qlen, jobs[i].tlen, jobs[i].w, jobs[i].zdrop, jobs[i].end_bonus,
+                      jobs[i].flag};
+  }
+  // waves under the traceback budget; bins by (mode, shape) inside each wave
+  b->waves.clear();
+  std::vector<int64_t> tbo(n);
+  std::vector<int32_t> ord(n);
+  int64_t ordp = 0;
+  for (int i = 0; i < n;) {
+    Wave wv;
+    wv.j0 = i;
+    int64_t acc = 0;
+    while (i < n && (acc + foot[i] <= c->tb_budget || i == wv.j0)) tbo[i] = acc, acc += foot[i], ++i;
+    wv.j1 = i;
+    wv.tb_bytes = acc;
+    for (int md = 0; md < 3; ++md)
+      for (int s = 0; s < kNumExtShapes; ++s) {
+        Bin bn{md, s, ordp, 0};
+        for (int j = wv.j0; j < wv.j1; ++j)
+          if (mode[j] == md && shape[j] == s) ord[ordp++] = j - wv.j0, bn.count++;
+        if (bn.count) wv.bins.push_back(bn);
+      }
+    b->waves.push_back(wv);
+  }
+  b->n_counters = 0;
+  for (auto &wv : b->waves) b->n_counters += (int)wv.bins.size();
+  if ((rc = b->jobs.ensure(sizeof(ksw2g_job) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->order.ensure(sizeof(int32_t) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->tb_off.ensure(sizeof(int64_t) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->res.ensure(sizeof(ksw2g_ext_result) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->bts.ensure(sizeof(ksw2g_bt) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->counters.ensure(16 + sizeof(int) * (size_t)std::max(b->n_counters, 1)))) return rc;
+  b->cigar_cap = std::max<int64_t>(cig, 16);
+  if ((rc = b->cigar.ensure(sizeof(uint32_t) * (size_t)b->cigar_cap))) return rc;
+  if (n) {
+    CK(cudaMemcpyAsync(b->jobs.p, dj.data(), sizeof(ksw2g_job) * n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(b->order.p, ord.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(b->tb_off.p, tbo.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+extern "C" int ksw2g_ext_prepare(ksw2g_ctx_t *c, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+                                 int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs, const uint8_t *qbuf,
+                                 int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len, ksw2g_batch_t **out) {
+  if (!c || !out) return set_err(KSW2G_E_ARG, "null ctx/out");
+  ksw2g_batch *b = new ksw2g_batch;
+  int rc = ext_prepare_into(c, b, dual, m, mat, q, e, q2, e2, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len);
+  if (rc) {
+    ksw2g_batch_free(b);
+    return rc;
+  }
+  *out = b;
+  return 0;
+}
+
+static int ext_run(ksw2g_ctx *c, ksw2g_batch *b) {
+  CK(cudaSetDevice(c->device));
+  b->launches = 0;
+  if (b->n == 0) return 0;
+  int64_t maxtb = 0;
+  for (auto &wv : b->waves) maxtb = std::max(maxtb, wv.tb_bytes);
+  int rc;
+  if ((rc = c->tb_pool.ensure((size_t)std::max<int64_t>(maxtb, 16)))) return rc;
+  int *cnt = b->counters.as<int>();
+  unsigned long long *cursor = (unsigned long long *)cnt;  // bytes 0..7
+  int *err = cnt + 2;                                      // bytes 8..11
+  int *jc = cnt + 4;                                       // per-bin job counters
+  CK(cudaMemsetAsync(b->counters.p, 0, 16 + sizeof(int) * (size_t)b->n_counters, c->st));
+  const ksw2g_job *dj = b->jobs.as<ksw2g_job>();
+  ksw2g_ext_result *dr = b->res.as<ksw2g_ext_result>();
+  ksw2g_bt *db = b->bts.as<ksw2g_bt>();
+  const int64_t *dto = b->tb_off.as<int64_t>();
+  const int32_t *dord = b->order.as<int32_t>();
+  int ci = 0;
+  for (auto &wv : b->waves) {
+    for (auto &bn : wv.bins) {
+      ExtLaunch L{dj + wv.j0, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr + wv.j0, db + wv.j0,
+                  c->tb_pool.as<uint8_t>(), dto + wv.j0, jc + ci++};
+      CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, c->st));
+      ++b->launches;
+    }
+    bool any_cig = false;
+    for (auto &bn : wv.bins) any_cig |= bn.mode != 0;
+    if (any_cig) {
+      CK(launch_ext_bt(dj + wv.j0, wv.j1 - wv.j0, db + wv.j0, c->tb_pool.as<uint8_t>(), dto + wv.j0, dr + wv.j0,
+                       b->cigar.as<uint32_t>(), cursor, (long long)b->cigar_cap, err, c->st));
+      ++b->launches;
+    }
+  }
+  return 0;
+}
+
+extern "C" int ksw2g_batch_run(ksw2g_ctx_t *c, ksw2g_batch_t *b) {
+  if (!c || !b) return set_err(KSW2G_E_ARG, "null ctx/batch");
+  if (b->kind <= 1) return ext_run(c, b);
+  extern int ll_run(ksw2g_ctx * c, ksw2g_batch * b);
+  return ll_run(c, b);
+}
+
+extern "C" int ksw2g_ext_fetch(ksw2g_ctx_t *c, ksw2g_batch_t *b, ksw2g_ext_result_t *res, uint32_t *cigar,
+                               int64_t cigar_cap, int64_t *cigar_used) {
+  if (!c || !b || b->kind > 1) return set_err(KSW2G_E_ARG, "not an extension batch");
+  CK(cudaSetDevice(c->device));
+  struct {
+    unsigned long long cursor;
+    int err, pad;
+  } hdr = {0, 0, 0};
+  if (b->n) {
+    if (res) CK(cudaMemcpyAsync(res, b->res.p, sizeof(ksw2g_ext_result) * b->n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&hdr, b->counters.p, sizeof hdr, cudaMemcpyDeviceToHost, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  if (hdr.err) return set_err(KSW2G_E_CAPACITY, "device CIGAR arena overflow");
+  if (cigar_used) *cigar_used = (int64_t)hdr.cursor;
+  if (hdr.cursor > 0 && cigar) {
+    if ((int64_t)hdr.cursor > cigar_cap)
+      return set_err(KSW2G_E_CAPACITY, "CIGAR buffer holds %lld words, %llu needed", (long long)cigar_cap,
+                     hdr.cursor);
+    CK(cudaMemcpyAsync(cigar, b->cigar.p, sizeof(uint32_t) * hdr.cursor, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  return 0;
+}
+
+extern "C" int ksw2g_ext_batch(ksw2g_ctx_t *c, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+                               int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs, const uint8_t *qbuf,
+                               int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ext_result_t *res,
+                               uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used) {
+  if (!c) return set_err(KSW2G_E_ARG, "null ctx");
+  if (!c->scratch) c->scratch = new ksw2g_batch;
+  int rc = ext_prepare_into(c, c->scratch, dual, m, mat, q, e, q2, e2, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len);
+  if (rc) return rc;
+  if ((rc = ext_run(c, c->scratch))) return rc;
+  return ksw2g_ext_fetch(c, c->scratch, res, cigar, cigar_cap, cigar_used);
+}
+
+extern "C" int ksw2g_ext_num_shapes(void) { return kNumExtShapes; }
+extern "C" int ksw2g_ext_shape_info(int shape, int *g, int *k) {
+  if (shape < 0 || shape >= kNumExtShapes) return set_err(KSW2G_E_ARG, "bad shape");
+  if (g) *g = kExtShapes[shape].G;
+  if (k) *k = kExtShapes[shape].K;
+  return 0;
+}
+extern "C" int ksw2g_ext_set_shape(int dual, int mode, int lo, int hi, int shape) {
+  if (shape < 0 || shape >= kNumExtShapes || mode < 0 || mode > 2) return set_err(KSW2G_E_ARG, "bad shape/mode");
+  ext_shape_set_pref(dual, mode, lo, hi, shape);
+  return 0;
+}
+
+// ---------------------------------------------------------------- per-call drop-in
+// Allocation of ez->cigar and of the ksw_ll_qinit block follows the caller's
+// allocator: when the process exports kalloc's krealloc/kmalloc (minibwa built
+// with mimalloc=0, i.e. HAVE_KALLOC, and linked with -rdynamic), they are used
+// with the caller's km exactly as ksw2.h:114-122 does; kalloc itself falls back
+// to libc for km == NULL (kalloc.c:128-185).  Otherwise libc realloc/malloc.
+extern "C" void *krealloc(void *km, void *ptr, size_t size) __attribute__((weak));
+extern "C" void *kmalloc(void *km, size_t size) __attribute__((weak));
+static void *caller_realloc(void *km, void *p, size_t n) { return krealloc ? krealloc(km, p, n) : realloc(p, n); }
+static void *caller_malloc(void *km, size_t n) { return kmalloc ? kmalloc(km, n) : malloc(n); }
+
+// Each host thread gets its own context (stream + scratch) on the current
+// device, so concurrent kt_for workers never share a stream.
+static void die(const char *what, cudaError_t e) {
+  fprintf(stderr, "[ksw2gpu] fatal: %s: %s\n", what, cudaGetErrorString(e));
+  abort();
+}
+#define DIE_ON(x)                          \
+  do {                                     \
+    cudaError_t e_ = (x);                  \
+    if (e_ != cudaSuccess) die(#x, e_);    \
+  } while (0)
+
+struct TlsCtx {
+  ksw2g_ctx *c = nullptr;
+  ~TlsCtx() {
+    if (c) ksw2g_ctx_destroy(c);
+  }
+};
+static thread_local TlsCtx tls;
+
+static ksw2g_ctx *thread_ctx() {
+  int dev = 0;
+  DIE_ON(cudaGetDevice(&dev));
+  if (tls.c && tls.c->device != dev) {
+    ksw2g_ctx_destroy(tls.c);
+    tls.c = nullptr;
+  }
+  if (!tls.c) {
+    if (ksw2g_ctx_create(dev, &tls.c) != 0) {
+      fprintf(stderr, "[ksw2gpu] fatal: %s\n", tl_err.c_str());
+      abort();
+    }
+  }
+  return tls.c;
+}
+
+// Device scratch layout of one call (all 16-byte aligned):
+//   [0,16) cursor/err | [16,32) job counter | job | tb_off | bt | res | cigar | arena | traceback
+static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen, const uint8_t *target, int8_t m,
+                    const int8_t *mat, int8_t q, int8_t e, int8_t q2, int8_t e2, int w, int zdrop, int end_bonus,
+                    int flag, ksw_extz_t *ez) {
+  // ksw_reset_extz (ksw2.h:174-179): cigar and m_cigar are left alone
+  ez->max_q = ez->max_t = ez->mqe_t = ez->mte_q = -1;
+  ez->max = 0, ez->score = ez->mqe = ez->mte = KSW_NEG_INF;
+  ez->n_cigar = 0, ez->zdropped = 0, ez->reach_end = 0;
+  if (m <= dual || qlen <= 0 || tlen <= 0) return;
+  ksw2g_ext_params P;
+  derive_ext_params(dual, m, mat, q, e, q2, e2, P);
+  if (P.skip_all) return;
+  if ((flag & KSW_EZ_GENERIC_SC) && m > 16) {
+    fprintf(stderr, "[ksw2gpu] fatal: GENERIC_SC with m=%d > 16 is not supported on the device\n", m);
+    abort();
+  }
+  ksw2g_ctx *c = thread_ctx();
+  const int mode = ext_mode(flag);
+  const int nc = ext_ncol(qlen, tlen, w);
+  const int shape = ext_shape_pick(dual, mode, nc);
+  if (shape < 0) {
+    fprintf(stderr, "[ksw2gpu] fatal: band of %d blocks exceeds the widest kernel shape\n", nc);
+    abort();
+  }
+  const int64_t ncig = mode ? (int64_t)qlen + tlen + 1 : 0;
+  const int64_t foot = mode ? (int64_t)(qlen + tlen - 1) * nc * 16 : 0;
+  const size_t o_job = 32, o_tbo = o_job + 48, o_bt = o_tbo + 16, o_res = o_bt + 16;
+  const size_t o_cig = o_res + 64;
+  const size_t o_arena = (o_cig + ncig * 4 + 15) & ~(size_t)15;
+  const size_t arena_bytes = slot_bytes(qlen) + slot_bytes(tlen);
+  const size_t o_tb = (o_arena + arena_bytes + 255) & ~(size_t)255;
+  const size_t total = o_tb + foot + 16;
+  if (c->one.ensure(total) || c->one_h.ensure(o_tb)) {
+    fprintf(stderr, "[ksw2gpu] fatal: %s\n", tl_err.c_str());
+    abort();
+  }
+  uint8_t *h = (uint8_t *)c->one_h.p;
+  uint8_t *d = (uint8_t *)c->one.p;
+  memset(h, 0, o_job);
+  const int64_t qpad = (int64_t)(o_arena - o_arena) + 32, tpad = slot_bytes(qlen) + 32;
+  ksw2g_job J{qpad, tpad, qlen, tlen, w, zdrop, end_bonus, flag};
+  memcpy(h + o_job, &J, sizeof J);
+  memset(h + o_tbo, 0, 16);
+  memset(h + o_arena, 0, arena_bytes);
+  memcpy(h + o_arena + qpad, query, qlen);
+  memcpy(h + o_arena + tpad, target, tlen);
+  // upload counters + job + tb offset, and the arena, in two copies from one pinned block
+  DIE_ON(cudaMemcpyAsync(d, h, o_bt, cudaMemcpyHostToDevice, c->st));
+  DIE_ON(cudaMemcpyAsync(d + o_arena, h + o_arena, arena_bytes, cudaMemcpyHostToDevice, c->st));
+  ExtLaunch L{(const ksw2g_job *)(d + o_job), nullptr, 1, d + o_arena, (ksw2g_ext_result *)(d + o_res),
+              (ksw2g_bt *)(d + o_bt), d + o_tb, (const int64_t *)(d + o_tbo), (int *)(d + 16)};
+  DIE_ON(launch_ext_dp(dual, mode, shape, P, L, 1, c->st));
+  if (mode)
+    DIE_ON(launch_ext_bt((const ksw2g_job *)(d + o_job), 1, (const ksw2g_bt *)(d + o_bt), d + o_tb,
+                         (const int64_t *)(d + o_tbo), (ksw2g_ext_result *)(d + o_res), (uint32_t *)(d + o_cig),
+                         (unsigned long long *)d, (long long)ncig, (int *)(d + 8), c->st));
+  DIE_ON(cudaMemcpyAsync(h + o_res, d + o_res, 64 + ncig * 4, cudaMemcpyDeviceToHost, c->st));
+  DIE_ON(cudaStreamSynchronize(c->st));
+  ksw2g_ext_result R;
+  memcpy(&R, h + o_res, sizeof R);
+  ez->max = (uint32_t)R.max, ez->zdropped = R.zdropped ? 1 : 0;
+  ez->max_q = R.max_q, ez->max_t = R.max_t, ez->mqe = R.mqe, ez->mqe_t = R.mqe_t;
+  ez->mte = R.mte, ez->mte_q = R.mte_q, ez->score = R.score, ez->reach_end = R.reach_end;
+  if (R.n_cigar > 0) {
+    // grow like ksw_push_cigar (ksw2.h:127-129): doubling from 4
+    int mc = ez->m_cigar;
+    while (mc < R.n_cigar) mc = mc ? mc << 1 : 4;
+    if (mc != ez->m_cigar || !ez->cigar) {
+      ez->cigar = (uint32_t *)caller_realloc(km, ez->cigar, (size_t)mc * 4);
+      ez->m_cigar = mc;
+    }
+    memcpy(ez->cigar, h + o_cig, (size_t)R.n_cigar * 4);
+    ez->n_cigar = R.n_cigar;
+  }
+}
+
+extern "C" void ksw_extz2_sse(void *km, int qlen, const uint8_t *query, int tlen, const uint8_t *target, int8_t m,
+                              const int8_t *mat, int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag,
+                              ksw_extz_t *ez) {
+  ext_one(km, 0, qlen, query, tlen, target, m, mat, q, e, q, e, w, zdrop, end_bonus, flag, ez);
+}
+
+extern "C" void ksw_extd2_sse(void *km, int qlen, const uint8_t *query, int tlen, const uint8_t *target, int8_t m,
+                              const int8_t *mat, int8_t gapo, int8_t gape, int8_t gapo2, int8_t gape2, int w,
+                              int zdrop, int end_bonus, int flag, ksw_extz_t *ez) {
+  ext_one(km, 1, qlen, query, tlen, target, m, mat, gapo, gape, gapo2, gape2, w, zdrop, end_bonus, flag, ez);
+}
+
+// ================================================================ ksw_ll
+static int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape,
+                           int n, const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+                           const uint8_t *tbuf, int64_t tbuf_len) {
+  if (n < 0 || (n > 0 && !jobs) || !mat || m <= 0 || m > 64) return set_err(KSW2G_E_ARG, "bad ll batch arguments");
+  CK(cudaSetDevice(c->device));
+  size = size > 1 ? 2 : 1;
+  b->kind = size == 1 ? 2 : 3;
+  b->ll_size = size, b->ll_m = m, b->ll_gapo = gapo, b->ll_gape = gape;
+  b->n = n;
+  b->launches = 0;
+  const int lanes = size == 1 ? 16 : 8;
+  std::vector<int64_t> qo(n), to(n), blo(n);
+  std::vector<int32_t> ql(n), tl(n);
+  int slen = 1;
+  int64_t nbl = 0;
+  for (int i = 0; i < n; ++i) {
+    const ksw2g_ll_job_t &J = jobs[i];
+    if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
+        J.toff + J.tlen > tbuf_len)
+      return set_err(KSW2G_E_ARG, "ll job %d: sequence out of buffer bounds", i);
+    qo[i] = J.qoff, to[i] = J.toff, ql[i] = J.qlen, tl[i] = J.tlen;
+    slen = std::max(slen, (J.qlen + lanes - 1) / lanes);
+    blo[i] = nbl;
+    if (J.xtra & KSW_LL_SUBO) nbl += J.tlen;
+  }
+  if (slen > ll_slen_cap(size))
+    return set_err(KSW2G_E_BAND, "ll query of %d segments exceeds the kernel's %d", slen, ll_slen_cap(size));
+  b->ll_slen = slen;
+  std::vector<int64_t> qpad, tpad;
+  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), qbuf, qbuf_len, tbuf, tbuf_len, qpad,
+                           tpad);
+  if (rc) return rc;
+  std::vector<ksw2g_ll_job> dj(n);
+  for (int i = 0; i < n; ++i) dj[i] = ksw2g_ll_job{qpad[i], tpad[i], jobs[i].qlen, jobs[i].tlen, jobs[i].xtra, 0};
+  if ((rc = b->jobs.ensure(sizeof(ksw2g_ll_job) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->res.ensure(sizeof(ksw2g_ll_result) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->counters.ensure(16))) return rc;
+  if ((rc = b->llmat.ensure((size_t)m * m + 16))) return rc;
+  if ((rc = b->blist.ensure(sizeof(uint64_t) * (size_t)std::max<int64_t>(nbl, 1)))) return rc;
+  if ((rc = b->blist_off.ensure(sizeof(int64_t) * (size_t)std::max(n, 1)))) return rc;
+  if (n) {
+    CK(cudaMemcpyAsync(b->jobs.p, dj.data(), sizeof(ksw2g_ll_job) * n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(b->blist_off.p, blo.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->st));
+  }
+  CK(cudaMemcpyAsync(b->llmat.p, mat, (size_t)m * m, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+int ll_run(ksw2g_ctx *c, ksw2g_batch *b) {
+  CK(cudaSetDevice(c->device));
+  b->launches = 0;
+  if (b->n == 0) return 0;
+  CK(cudaMemsetAsync(b->counters.p, 0, 16, c->st));
+  LLLaunch L{b->jobs.as<ksw2g_ll_job>(), b->n, b->arena.as<uint8_t>(), b->llmat.as<int8_t>(), b->ll_m, b->ll_gapo,
+             b->ll_gape, b->res.as<ksw2g_ll_result>(), b->blist.as<uint64_t>(), b->blist_off.as<int64_t>(),
+             b->counters.as<int>()};
+  CK(launch_ll(b->ll_size, b->ll_slen, L, 0, c->st));
+  ++b->launches;
+  return 0;
+}
+
+extern "C" int ksw2g_ll_prepare(ksw2g_ctx_t *c, int size, int m, const int8_t *mat, int gapo, int gape, int n_jobs,
+                                const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+                                const uint8_t *tbuf, int64_t tbuf_len, ksw2g_batch_t **out) {
+  if (!c || !out) return set_err(KSW2G_E_ARG, "null ctx/out");
+  ksw2g_batch *b = new ksw2g_batch;
+  int rc = ll_prepare_into(c, b, size, m, mat, gapo, gape, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len);
+  if (rc) {
+    ksw2g_batch_free(b);
+    return rc;
+  }
+  *out = b;
+  return 0;
+}
+
+extern "C" int ksw2g_ll_fetch(ksw2g_ctx_t *c, ksw2g_batch_t *b, ksw2g_ll_result_t *res) {
+  if (!c || !b || b->kind < 2) return set_err(KSW2G_E_ARG, "not an ll batch");
+  CK(cudaSetDevice(c->device));
+  if (b->n && res) CK(cudaMemcpyAsync(res, b->res.p, sizeof(ksw2g_ll_result) * b->n, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+extern "C" int ksw2g_ll_batch(ksw2g_ctx_t *c, int size, int m, const int8_t *mat, int gapo, int gape, int n_jobs,
+                              const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+                              int64_t tbuf_len, ksw2g_ll_result_t *res) {
+  if (!c) return set_err(KSW2G_E_ARG, "null ctx");
+  if (!c->scratch) c->scratch = new ksw2g_batch;
+  int rc = ll_prepare_into(c, c->scratch, size, m, mat, gapo, gape, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len);
+  if (rc) return rc;
+  if ((rc = ll_run(c, c->scratch))) return rc;
+  return ksw2g_ll_fetch(c, c->scratch, res);
+}
+
+// ---- per-call drop-ins of ksw_ll_qinit / ksw_ll_u8_core / ksw_ll_i16_core / ksw_ll_i16
+// The "profile" returned by ksw_ll_qinit is one malloc() block holding the
+// query and the matrix; the striped profile itself is built on the device
+// by every core call.  Callers only pass the block back and free() it.
+struct LLQ {
+  uint32_t magic;
+  int32_t size, qlen, m;
+};
+static const uint32_t kLLQMagic = 0x6b73776cu;
+
+extern "C" void *ksw_ll_qinit(void *km, int size, int qlen, const uint8_t *query, int m, const int8_t *mat) {
+  if (qlen < 0) qlen = 0;
+  LLQ *h = (LLQ *)caller_malloc(km, sizeof(LLQ) + (size_t)m * m + qlen + 16);
+  h->magic = kLLQMagic, h->size = size > 1 ? 2 : 1, h->qlen = qlen, h->m = m;
+  memcpy((uint8_t *)(h + 1), mat, (size_t)m * m);
+  if (qlen) memcpy((uint8_t *)(h + 1) + m * m, query, qlen);
+  return h;
+}
+
+static ksw_llrst_t ll_one(void *q_, int tlen, const uint8_t *target, int gapo, int gape, int xtra, int want_size) {
+  LLQ *h = (LLQ *)q_;
+  if (!h || h->magic != kLLQMagic) {
+    fprintf(stderr, "[ksw2gpu] fatal: ksw_ll core called with a block not made by ksw_ll_qinit\n");
+    abort();
+  }
+  (void)want_size;  // the reference runs the core it is asked for, whatever size qinit used
+  const int m = h->m, qlen = h->qlen, size = want_size;
+  const int lanes = size == 1 ? 16 : 8;
+  const int slen = (qlen + lanes - 1) / lanes;
+  if (slen > ll_slen_cap(size)) {
+    fprintf(stderr, "[ksw2gpu] fatal: ksw_ll query of %d nt exceeds the kernel limit\n", qlen);
+    abort();
+  }
+  if (tlen < 0) tlen = 0;
+  ksw2g_ctx *c = thread_ctx();
+  const int64_t nbl = (xtra & KSW_LL_SUBO) ? tlen : 0;
+  const size_t o_job = 16, o_blo = o_job + 32, o_res = o_blo + 16, o_mat = o_res + 32;
+  const size_t o_arena = (o_mat + (size_t)m * m + 15) & ~(size_t)15;
+  const size_t arena_bytes = slot_bytes(qlen) + slot_bytes(tlen);
+  const size_t o_bl = (o_arena + arena_bytes + 15) & ~(size_t)15;
+  const size_t total = o_bl + nbl * 8 + 16;
+  if (c->one.ensure(total) || c->one_h.ensure(o_bl)) {
+    fprintf(stderr, "[ksw2gpu] fatal: %s\n", tl_err.c_str());
+    abort();
+  }
+  uint8_t *hb = (uint8_t *)c->one_h.p, *d = (uint8_t *)c->one.p;
+  memset(hb, 0, o_arena);
+  ksw2g_ll_job J{32, slot_bytes(qlen) + 32, qlen, tlen, xtra, 0};
+  memcpy(hb + o_job, &J, sizeof J);
+  memcpy(hb + o_mat, (uint8_t *)(h + 1), (size_t)m * m);
+  memset(hb + o_arena, 0, arena_bytes);
+  if (qlen) memcpy(hb + o_arena + J.qoff, (uint8_t *)(h + 1) + m * m, qlen);
+  if (tlen) memcpy(hb + o_arena + J.toff, target, tlen);
+  DIE_ON(cudaMemcpyAsync(d, hb, o_arena + arena_bytes, cudaMemcpyHostToDevice, c->st));
+  LLLaunch L{(const ksw2g_ll_job *)(d + o_job), 1, d + o_arena, (const int8_t *)(d + o_mat), m, gapo, gape,
+             (ksw2g_ll_result *)(d + o_res), (uint64_t *)(d + o_bl), (const int64_t *)(d + o_blo), (int *)d};
+  DIE_ON(launch_ll(size, slen < 1 ? 1 : slen, L, 1, c->st));
+  DIE_ON(cudaMemcpyAsync(hb + o_res, d + o_res, sizeof(ksw2g_ll_result), cudaMemcpyDeviceToHost, c->st));
+  DIE_ON(cudaStreamSynchronize(c->st));
+  ksw2g_ll_result R;
+  memcpy(&R, hb + o_res, sizeof R);
+  ksw_llrst_t r;
+  r.score = R.score, r.te = R.te, r.qe = R.qe, r.score2 = R.score2, r.te2 = R.te2;
+  return r;
+}
+
+extern "C" ksw_llrst_t ksw_ll_u8_core(void *q, int tlen, const uint8_t *target, int gapo, int gape, int xtra) {
+  return ll_one(q, tlen, target, gapo, gape, xtra, 1);
+}
+extern "C" ksw_llrst_t ksw_ll_i16_core(void *q, int tlen, const uint8_t *target, int gapo, int gape, int xtra) {
+  return ll_one(q, tlen, target, gapo, gape, xtra, 2);
+}
+extern "C" int ksw_ll_i16(void *q, int tlen, const uint8_t *target, int gapo, int gape, int *qe, int *te) {
+  ksw_llrst_t r = ll_one(q, tlen, target, gapo, gape, 0, 2);
+  *qe = r.qe, *te = r.te;
+  return r.score;
+}

@@ -1,0 +1,104 @@
+// ext_bt.cuh -- traceback walk (ksw_backtrack, ksw2.h:140-172, rotated layout)
+// and the packing of raw sequences into the padded device arena.
+#pragma once
+#include "ksw2g.h"
+
+namespace ksw2g {
+
+// padded first/last target position of anti-diagonal r (ksw2_extz2_sse.c:99-108)
+__device__ __forceinline__ void band_pad(int r, int qlen, int tlen, int w, int &off, int &off_end) {
+  int st = r - qlen + 1 > 0 ? r - qlen + 1 : 0;
+  int en = r < tlen - 1 ? r : tlen - 1;
+  const int a = (r - w + 1) >> 1, b = (r + w) >> 1;
+  if (st < a) st = a;
+  if (en > b) en = b;
+  off = st & ~15;
+  off_end = (en & ~15) + 15;
+}
+
+// One walk over the traceback.  WRITE == false counts CIGAR operations;
+// WRITE == true stores them in final order at out[0..n).
+template <bool WRITE>
+__device__ int bt_walk(const uint8_t *__restrict__ tb, int ncol16, int qlen, int tlen, int w, int i0, int j0,
+                       int rev, int n_total, uint32_t *__restrict__ out) {
+  int i = i0, j = j0, state = 0, n = 0, last_op = -1;
+  uint32_t run = 0;
+  auto push = [&](int op, int len) {
+    if (n == 0 || op != last_op) {
+      if (WRITE && n > 0) out[rev ? n - 1 : n_total - n] = run << 4 | (uint32_t)last_op;
+      ++n, last_op = op, run = (uint32_t)len;
+    } else run += (uint32_t)len;
+  };
+  while (i >= 0 && j >= 0) {
+    const int r = i + j;
+    int off, off_end, force = -1;
+    band_pad(r, qlen, tlen, w, off, off_end);
+    if (i < off) force = 2;
+    if (i > off_end) force = 1;
+    const unsigned t = force < 0 ? __ldg(tb + (size_t)r * ncol16 + (i - off)) : 0u;
+    if (state == 0) state = t & 7;
+    else if (!(t >> (state + 2) & 1)) state = 0;
+    if (state == 0) state = t & 7;
+    if (force >= 0) state = force;
+    if (state == 0) push(0, 1), --i, --j;
+    else if (state == 1 || state == 3) push(2, 1), --i;
+    else push(1, 1), --j;
+  }
+  if (i >= 0) push(2, i + 1);
+  if (j >= 0) push(1, j + 1);
+  if (WRITE && n > 0) out[rev ? n - 1 : n_total - n] = run << 4 | (uint32_t)last_op;
+  return n;
+}
+
+__global__ void ext_bt_kernel(const ksw2g_job *__restrict__ jobs, int n_jobs, const ksw2g_bt *__restrict__ bts,
+                              const uint8_t *__restrict__ tb_pool, const int64_t *__restrict__ tb_off,
+                              ksw2g_ext_result *__restrict__ res, uint32_t *__restrict__ cigar_out,
+                              unsigned long long *__restrict__ cursor, long long cigar_cap, int *__restrict__ err) {
+  const int jid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jid >= n_jobs) return;
+  const ksw2g_bt b = bts[jid];
+  if (b.i0 < 0) {
+    res[jid].n_cigar = 0;
+    return;
+  }
+  const ksw2g_job J = jobs[jid];
+  int w = J.w;
+  if (w < 0) w = J.tlen > J.qlen ? J.tlen : J.qlen;
+  int nc = J.qlen < J.tlen ? J.qlen : J.tlen;
+  nc = ((nc < w + 1 ? nc : w + 1) + 15) / 16 + 1;
+  const int rev = (J.flag & KSW2G_REV_CIGAR) ? 1 : 0;
+  const uint8_t *tb = tb_pool + tb_off[jid];
+  const int n = bt_walk<false>(tb, nc * 16, J.qlen, J.tlen, w, b.i0, b.j0, rev, 0, nullptr);
+  const unsigned long long o = atomicAdd(cursor, (unsigned long long)n);
+  if ((long long)(o + n) > cigar_cap) {  // arena too small: report, write nothing
+    atomicOr(err, 1);
+    res[jid].n_cigar = -n;
+    res[jid].cigar_off = -1;
+    return;
+  }
+  bt_walk<true>(tb, nc * 16, J.qlen, J.tlen, w, b.i0, b.j0, rev, n, cigar_out + o);
+  res[jid].n_cigar = n;
+  res[jid].cigar_off = (int64_t)o;
+}
+
+// Copy raw (unpadded, back-to-back) sequences into the padded arena:
+// dst[off-32 .. off+len+32) receives 32 zero bytes, the sequence, then zeros up
+// to the next 16-byte boundary plus 32.  One warp per sequence.
+__global__ void pack_seqs_kernel(int n, const uint8_t *__restrict__ raw, const int64_t *__restrict__ raw_off,
+                                 const int32_t *__restrict__ len, uint8_t *__restrict__ arena,
+                                 const int64_t *__restrict__ dst_off) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = warp; s < n; s += nw) {
+    const int L = len[s];
+    const int64_t so = raw_off[s];
+    uint8_t *d = arena + dst_off[s] - 32;
+    const int tot = 32 + ((L + 15) & ~15) + 32;
+    for (int i = lane; i < tot; i += 32) {
+      const int p = i - 32;
+      d[i] = (p >= 0 && p < L) ? raw[so + p] : (uint8_t)0;
+    }
+  }
+}
+
+}  // namespace ksw2g

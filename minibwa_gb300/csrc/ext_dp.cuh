@@ -1,0 +1,548 @@
+// ext_dp.cuh -- banded anti-diagonal DP for ksw_extz2_sse / ksw_extd2_sse on sm_103a.
+//
+// Mapping.  A group of G threads (4 <= G <= 32, inside one warp) owns one
+// pair at a time.  The group keeps a window of W = G*K 32-bit words of every
+// per-position state array of the reference (u, v, x, y[, x2, y2], s and the
+// 32-bit H of the exact max) in registers: word i of the window covers
+// absolute target positions 16*wb + 4*i .. +3, and thread k owns words
+// k, k+G, k+2G, ... so that one store instruction of the group writes G
+// consecutive traceback words.  The window base wb always equals the
+// reference's first padded 16-byte block of the current anti-diagonal
+// (st_ in ksw2_extz2_sse.c:140), which moves right by at most one block per
+// anti-diagonal; when it moves, all state shifts down by four words.  W is at
+// least 4*(n_col_+1) words: the n_col_ blocks the reference computes per
+// anti-diagonal (ksw2_extz2_sse.c:68,141) plus one block that receives the
+// 16-byte score stores running past en0 (ksw2_extz2_sse.c:118-132).
+//
+// Every cell operation reproduces the reference's byte-lane semantics
+// (swar.cuh), including the cells of the 16-byte padding outside the nominal
+// band, because those are read back as neighbours.  The groups of a warp
+// step their anti-diagonals in lockstep; a group whose pair ends (last
+// anti-diagonal, z-drop, or the extd2 early stop) takes the next job from a
+// device work counter at once.
+#pragma once
+#include "ksw2g.h"
+#include "swar.cuh"
+
+#ifndef KSW2G_TRACE
+#define KSW2G_TRACE(...)
+#endif
+
+namespace ksw2g {
+
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+  if (G == 32) return 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  return ((1u << G) - 1u) << (lane & ~(G - 1));
+}
+
+template <int K>
+__device__ __forceinline__ uint32_t pick(const uint32_t (&a)[K], int j) {  // a[j], j uniform
+  uint32_t v = a[0];
+#pragma unroll
+  for (int i = 1; i < K; ++i) v = (j == i) ? a[i] : v;
+  return v;
+}
+template <int K>
+__device__ __forceinline__ int32_t pickH(const int32_t (&h0)[K], const int32_t (&h1)[K], const int32_t (&h2)[K],
+                                         const int32_t (&h3)[K], int j, int b) {
+  int32_t v = 0;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    int32_t c = b == 0 ? h0[i] : b == 1 ? h1[i] : b == 2 ? h2[i] : h3[i];
+    v = (j == i) ? c : v;
+  }
+  return v;
+}
+
+// shift a per-slot array down by four words (word i <- word i+4)
+template <int G, int K, typename T>
+__device__ __forceinline__ void shift4(T (&a)[K], T fill, int k, unsigned gm) {
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    T send = (k < 4) ? (j + 1 < K ? a[j + 1] : fill) : a[j];
+    a[j] = __shfl_sync(gm, send, (k + 4) & (G - 1), G);
+  }
+}
+
+__device__ __forceinline__ uint32_t ld_tw(const uint8_t *tp, int p, int tlen) {
+  return p < tlen ? __ldg((const uint32_t *)(tp + p)) : 0u;
+}
+
+// VAR: 0 = extz2 (affine), 1 = extd2 (dual affine)
+// MODE: 0 = score only, 1 = left-aligned gaps with traceback, 2 = right-aligned gaps with traceback
+template <int VAR, int MODE, int G, int K>
+__global__ void __launch_bounds__(128)
+ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ order, int n_jobs,
+              const uint8_t *__restrict__ arena, const ksw2g_ext_params P, ksw2g_ext_result *__restrict__ res,
+              ksw2g_bt *__restrict__ bts, uint8_t *__restrict__ tb_pool, const int64_t *__restrict__ tb_off,
+              int *__restrict__ job_counter) {
+  constexpr bool D2 = VAR == 1;
+  constexpr bool CIG = MODE != 0;
+  const int lane = threadIdx.x & 31;
+  const int k = lane & (G - 1);
+  const unsigned gm = group_mask<G>();
+
+  // batch constants (byte lanes)
+  const uint32_t q4 = splat8(P.c_q), q24 = splat8(P.c_q2), qe4 = splat8(P.c_qe), qe24 = splat8(P.c_qe2);
+  const uint32_t mch4 = splat8(D2 ? P.c_mch : P.c_mch + P.c_qe2);  // extz2 stores s + 2(q+e)
+  const uint32_t mis4 = splat8(D2 ? P.c_mis : P.c_mis + P.c_qe2);
+  const uint32_t N4 = splat8(D2 ? P.c_N : P.c_N + P.c_qe2);
+  const uint32_t m14 = splat8(P.c_m1), maxsc4 = splat8(P.c_maxsc), mchraw4 = splat8(P.c_mch);
+  const uint32_t initb = D2 ? (uint32_t)(uint8_t)(-P.q - P.e) : 0u;
+  const uint32_t init2b = D2 ? (uint32_t)(uint8_t)(-P.q2 - P.e2) : 0u;
+  const uint32_t init4 = splat8(initb), init24 = splat8(init2b);
+  const uint32_t s_init4 = D2 ? 0u : splat8(P.c_qe2);
+  // extz2: q+e; extd2: q+e as declared before the swap (ksw2_extd2_sse.c:60,70), used only at r == 0
+  const int qe = P.qe_scalar;
+  const int ez_e = D2 ? P.e2 : P.e;
+
+  // per-slot state
+  uint32_t U[K], V[K], X[K], Y[K], X2[K], Y2[K], S[K], TW[K];
+  int32_t H0[K], H1[K], H2[K], H3[K];
+
+  // per-group state (identical in every thread of the group)
+  int jid = -1, qlen = 0, tlen = 0, w = 0, zdrop = 0, end_bonus = 0, flag = 0;
+  int r = 0, wb = 0, ncol16 = 0, n_diag = 0;
+  int64_t cells = 0;
+  const uint8_t *qp = nullptr, *tp = nullptr;
+  uint8_t *tb = nullptr;
+  int32_t ez_max = 0, max_q = -1, max_t = -1, mqe = KSW2G_NEG_INF, mqe_t = -1, mte = KSW2G_NEG_INF, mte_q = -1;
+  int32_t score = KSW2G_NEG_INF, zdropped = 0, H_left = KSW2G_NEG_INF, last_max_H = 0, Hz = 0, last_H0_t = 0;
+  bool active = false, need = true;
+
+  auto vv = [&](uint32_t byte) -> int32_t { return D2 ? (int32_t)(int8_t)(uint8_t)byte : (int32_t)(byte & 0xffu) - qe; };
+
+  for (;;) {
+    // ---------------- take the next job ----------------
+    if (need) {
+      int j = 0;
+      if (k == 0) j = atomicAdd(job_counter, 1);
+      j = __shfl_sync(gm, j, 0, G);
+      need = false;
+      active = j < n_jobs;
+      if (active) {
+        jid = order ? order[j] : j;
+        const ksw2g_job J = jobs[jid];
+        qlen = J.qlen, tlen = J.tlen, w = J.w, zdrop = J.zdrop, end_bonus = J.end_bonus, flag = J.flag;
+        ez_max = 0, max_q = max_t = mqe_t = mte_q = -1;
+        score = mqe = mte = KSW2G_NEG_INF;
+        zdropped = 0, n_diag = 0, cells = 0;
+        if (P.skip_all || qlen <= 0 || tlen <= 0 || P.m <= VAR) {
+          // degenerate input: the reference returns right after ksw_reset_extz
+          if (k == 0) {
+            ksw2g_ext_result o;
+            o.score = score, o.max = 0, o.max_q = -1, o.max_t = -1, o.mqe = mqe, o.mqe_t = -1, o.mte = mte, o.mte_q = -1;
+            o.zdropped = 0, o.reach_end = 0, o.n_cigar = 0, o.n_diag = 0, o.cigar_off = 0, o.cells = 0;
+            res[jid] = o;
+            if (CIG) bts[jid] = ksw2g_bt{-1, -1, 0, 0};
+          }
+          need = true;
+          continue;
+        }
+        if (w < 0) w = tlen > qlen ? tlen : qlen;
+        {
+          int nc = qlen < tlen ? qlen : tlen;
+          nc = ((nc < w + 1 ? nc : w + 1) + 15) / 16 + 1;
+          ncol16 = nc * 16;
+        }
+        qp = arena + J.qoff, tp = arena + J.toff;
+        if (CIG) tb = tb_pool + tb_off[jid];
+        r = 0, wb = 0, H_left = KSW2G_NEG_INF, last_max_H = 0, Hz = 0, last_H0_t = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+          U[i] = V[i] = X[i] = Y[i] = init4;
+          X2[i] = Y2[i] = init24;
+          S[i] = s_init4;
+          H0[i] = H1[i] = H2[i] = H3[i] = KSW2G_NEG_INF;
+          TW[i] = ld_tw(tp, 4 * (k + G * i), tlen);
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, !active)) break;
+    if (!active) continue;
+
+    // ---------------- one anti-diagonal ----------------
+    bool done = false;
+    {
+      int st0 = r - qlen + 1 > 0 ? r - qlen + 1 : 0;
+      int en0 = r < tlen - 1 ? r : tlen - 1;
+      {
+        const int a = (r - w + 1) >> 1, b = (r + w) >> 1;
+        if (st0 < a) st0 = a;
+        if (en0 > b) en0 = b;
+      }
+      KSW2G_TRACE("lane %d job %d r %d st0 %d en0 %d wb %d\n", lane, jid, r, st0, en0, wb);
+      if (st0 > en0) {  // ksw2_extz2_sse.c:103-106
+        zdropped = 1;
+        done = true;
+      } else {
+        const int stb = st0 >> 4, enb = en0 >> 4;
+        uint32_t x1, v1, x21 = 0;
+        if (stb != wb) {  // the first padded block moved right by one: slide the window
+          const uint32_t xr = __shfl_sync(gm, X[0], 3, G) >> 24;
+          const uint32_t vr = __shfl_sync(gm, V[0], 3, G) >> 24;
+          uint32_t x2r = 0;
+          if (D2) x2r = __shfl_sync(gm, X2[0], 3, G) >> 24;
+          H_left = __shfl_sync(gm, H3[0], 3, G);
+          shift4<G, K>(U, init4, k, gm);
+          shift4<G, K>(V, init4, k, gm);
+          shift4<G, K>(X, init4, k, gm);
+          shift4<G, K>(Y, init4, k, gm);
+          if (D2) {
+            shift4<G, K>(X2, init24, k, gm);
+            shift4<G, K>(Y2, init24, k, gm);
+          }
+          shift4<G, K>(S, s_init4, k, gm);
+          shift4<G, K>(TW, 0u, k, gm);
+          shift4<G, K>(H0, (int32_t)KSW2G_NEG_INF, k, gm);
+          shift4<G, K>(H1, (int32_t)KSW2G_NEG_INF, k, gm);
+          shift4<G, K>(H2, (int32_t)KSW2G_NEG_INF, k, gm);
+          shift4<G, K>(H3, (int32_t)KSW2G_NEG_INF, k, gm);
+          wb = stb;
+          if (k >= G - 4) TW[K - 1] = ld_tw(tp, (wb << 4) + 4 * (k + G * (K - 1)), tlen);
+          x1 = xr, v1 = vr, x21 = x2r;  // (r-1, st-1) was computed on the last anti-diagonal
+        } else {
+          x1 = initb, v1 = initb, x21 = init2b;
+        }
+        const uint32_t vb = D2 ? (r == 0 ? (uint32_t)(uint8_t)(-P.q - P.e)
+                                  : r < P.long_thres ? (uint32_t)(uint8_t)(-P.e)
+                                  : r == P.long_thres ? (uint32_t)(uint8_t)P.long_diff
+                                                      : (uint32_t)(uint8_t)(-P.e2))
+                               : (r ? P.c_q : 0u);
+        if (stb == 0) x1 = initb, x21 = init2b, v1 = vb;  // ksw2_extz2_sse.c:114, ksw2_extd2_sse.c:148-151
+        const int base = wb << 4;
+        const int en = (enb << 4) + 15;
+        if (en >= r) {  // top row boundary (ksw2_extz2_sse.c:115, ksw2_extd2_sse.c:152-155)
+          const int pr = r - base, wr = pr >> 2, sh = (pr & 3) * 8;
+          const uint32_t keep = ~(0xffu << sh);
+#pragma unroll
+          for (int i = 0; i < K; ++i)
+            if (k + G * i == wr) {
+              Y[i] = (Y[i] & keep) | (initb << sh);
+              U[i] = (U[i] & keep) | (vb << sh);
+              if (D2) Y2[i] = (Y2[i] & keep) | (init2b << sh);
+            }
+        }
+        // ---- substitution scores written by the 16-byte stores from st0 (ksw2_extz2_sse.c:117-136) ----
+        {
+          const bool generic = flag & KSW2G_GENERIC_SC;
+          const int fend = generic ? en0 : st0 + (((en0 - st0) >> 4) << 4) + 15;
+          const int o = (r + 1) & 3;
+          const uint32_t qsel = (uint32_t)((o + 3) | ((o + 2) << 4) | ((o + 1) << 8) | (o << 12));
+#pragma unroll
+          for (int i = 0; i < K; ++i) {
+            const int p0 = base + 4 * (k + G * i);
+            if (p0 + 3 >= st0 && p0 <= fend) {
+              const int idx0 = r - p0 - 3;
+              const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
+              const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
+              const uint32_t Tw = TW[i];
+              uint32_t sn;
+              if (!generic) {
+                const uint32_t eq = eqz8(Tw ^ Qw);
+                const uint32_t nn = eqz8(Tw ^ m14) | eqz8(Qw ^ m14);
+                sn = sel(bmask(eq), mch4, mis4);
+                sn = sel(bmask(nn), N4, sn);
+              } else {
+                sn = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                  const int tc = (Tw >> (8 * b)) & 0xff, qc = (Qw >> (8 * b)) & 0xff;
+                  uint32_t v = (uint32_t)(uint8_t)P.mat[(tc * P.m + qc) & 255];
+                  if (!D2) v = (v + P.c_qe2) & 0xffu;
+                  sn |= v << (8 * b);
+                }
+              }
+              const int lo = st0 - p0, hi = fend - p0;
+              uint32_t wm = 0xffffffffu;
+              if (lo > 0) wm <<= 8 * lo;
+              if (hi < 3) wm &= 0xffffffffu >> (8 * (3 - hi));
+              S[i] = (S[i] & ~wm) | (sn & wm);
+            }
+          }
+        }
+        // ---- cells st..en of the anti-diagonal (ksw2_extz2_sse.c:142-215, ksw2_extd2_sse.c:183-314) ----
+        const int nlive = (enb - wb + 1) << 2;
+        const uint32_t extx = (!D2 && (x1 & 0x80)) ? 0xffffff00u : 0u;  // sign-extended _mm_cvtsi32_si128
+        const uint32_t extv = (!D2 && (v1 & 0x80)) ? 0xffffff00u : 0u;
+        uint32_t *row = CIG ? (uint32_t *)(tb + (size_t)r * ncol16) : nullptr;
+#pragma unroll
+        for (int i = K - 1; i >= 0; --i) {
+          const int wi = k + G * i;
+          const uint32_t sx = (k == G - 1) ? (i > 0 ? X[i > 0 ? i - 1 : 0] : 0u) : X[i];
+          const uint32_t sv = (k == G - 1) ? (i > 0 ? V[i > 0 ? i - 1 : 0] : 0u) : V[i];
+          uint32_t px = __shfl_sync(gm, sx, (k - 1) & (G - 1), G);
+          uint32_t pv = __shfl_sync(gm, sv, (k - 1) & (G - 1), G);
+          uint32_t px2 = 0;
+          if (D2) {
+            const uint32_t sx2 = (k == G - 1) ? (i > 0 ? X2[i > 0 ? i - 1 : 0] : 0u) : X2[i];
+            px2 = __shfl_sync(gm, sx2, (k - 1) & (G - 1), G);
+          }
+          if (i == 0 && k == 0) px = x1 << 24, pv = v1 << 24, px2 = x21 << 24;
+          if (wi < nlive) {
+            uint32_t xt1 = __funnelshift_l(px, X[i], 8);  // x[r-1][t-1 .. t+2]
+            uint32_t vt1 = __funnelshift_l(pv, V[i], 8);
+            if (!D2 && i == 0 && k == 0) xt1 |= extx, vt1 |= extv;
+            const uint32_t ut = U[i];
+            uint32_t z = S[i], a = add8(xt1, vt1), b = add8(Y[i], ut), d = 0;
+            if (!D2) {
+              if (MODE == 0) {
+                z = maxs8(z, a);
+              } else if (MODE == 1) {
+                const uint32_t M = bmask(gts8(a, z));
+                d = M & 0x01010101u;
+                z = sel(M, a, z);
+                d = sel(bmask(gts8(b, z)), 0x02020202u, d);
+              } else {
+                const uint32_t M = bmask(gts8(z, a));
+                d = ~M & 0x01010101u;
+                z = sel(M, z, a);
+                d = sel(bmask(gts8(z, b)), d, 0x02020202u);
+              }
+              z = maxu8(z, b);
+              z = minu8(z, maxsc4);
+              U[i] = sub8(z, vt1);
+              V[i] = sub8(z, ut);
+              z = sub8(z, q4);
+              a = sub8(a, z);
+              b = sub8(b, z);
+              if (MODE == 0) {
+                X[i] = relu8(a);
+                Y[i] = relu8(b);
+              } else if (MODE == 1) {
+                const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi;
+                X[i] = a & bmask(ga);
+                Y[i] = b & bmask(gb);
+                d |= (ga >> 4) | (gb >> 3);
+              } else {
+                X[i] = relu8(a);
+                Y[i] = relu8(b);
+                d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3);
+              }
+            } else {
+              const uint32_t x2t1 = __funnelshift_l(px2, X2[i], 8);
+              uint32_t a2 = add8(x2t1, vt1), b2 = add8(Y2[i], ut);
+              if (MODE == 0) {
+                z = maxs8(z, a);
+                z = maxs8(z, b);
+                z = maxs8(z, a2);
+                z = maxs8(z, b2);
+              } else if (MODE == 1) {
+                uint32_t M = bmask(gts8(a, z));
+                d = M & 0x01010101u;
+                z = sel(M, a, z);
+                M = bmask(gts8(b, z));
+                d = sel(M, 0x02020202u, d);
+                z = sel(M, b, z);
+                M = bmask(gts8(a2, z));
+                d = sel(M, 0x03030303u, d);
+                z = sel(M, a2, z);
+                M = bmask(gts8(b2, z));
+                d = sel(M, 0x04040404u, d);
+                z = sel(M, b2, z);
+              } else {
+                uint32_t M = bmask(gts8(z, a));
+                d = ~M & 0x01010101u;
+                z = sel(M, z, a);
+                M = bmask(gts8(z, b));
+                d = sel(M, d, 0x02020202u);
+                z = sel(M, z, b);
+                M = bmask(gts8(z, a2));
+                d = sel(M, d, 0x03030303u);
+                z = sel(M, z, a2);
+                M = bmask(gts8(z, b2));
+                d = sel(M, d, 0x04040404u);
+                z = sel(M, z, b2);
+              }
+              z = mins8(z, mchraw4);
+              U[i] = sub8(z, vt1);
+              V[i] = sub8(z, ut);
+              uint32_t tq = sub8(z, q4);
+              a = sub8(a, tq);
+              b = sub8(b, tq);
+              tq = sub8(z, q24);
+              a2 = sub8(a2, tq);
+              b2 = sub8(b2, tq);
+              if (MODE == 1) {
+                const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi, ga2 = gt0s8(a2) & kHi, gb2 = gt0s8(b2) & kHi;
+                X[i] = sub8(a & bmask(ga), qe4);
+                Y[i] = sub8(b & bmask(gb), qe4);
+                X2[i] = sub8(a2 & bmask(ga2), qe24);
+                Y2[i] = sub8(b2 & bmask(gb2), qe24);
+                d |= (ga >> 4) | (gb >> 3) | (ga2 >> 2) | (gb2 >> 1);
+              } else {
+                X[i] = sub8(relu8(a), qe4);
+                Y[i] = sub8(relu8(b), qe4);
+                X2[i] = sub8(relu8(a2), qe24);
+                Y2[i] = sub8(relu8(b2), qe24);
+                if (MODE == 2)
+                  d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3) | ((~a2 & kHi) >> 2) | ((~b2 & kHi) >> 1);
+              }
+            }
+            if (CIG) row[wi] = d;
+          }
+        }
+        ++n_diag;
+        cells += en0 - st0 + 1;
+        // ---- exact or approximate max, z-drop (ksw2_extz2_sse.c:216-278, ksw2_extd2_sse.c:315-385) ----
+        if (!(flag & KSW2G_APPROX_MAX)) {
+          const int pe = en0 - base;
+          int32_t Hen0;
+          if (r == 0) {
+            Hen0 = vv(__shfl_sync(gm, V[0], 0, G) & 0xff) - qe;
+          } else {
+            const int ws = pe >> 2, bs = pe & 3;
+            if (en0 > 0) {
+              const int pm = pe - 1;
+              int32_t hm1 = pm >= 0 ? __shfl_sync(gm, pickH<K>(H0, H1, H2, H3, (pm >> 2) / G, pm & 3), (pm >> 2) & (G - 1), G)
+                                    : H_left;
+              const uint32_t uw = __shfl_sync(gm, pick<K>(U, ws / G), ws & (G - 1), G);
+              Hen0 = hm1 + vv(uw >> (8 * bs));
+            } else {
+              const int32_t h = __shfl_sync(gm, pickH<K>(H0, H1, H2, H3, ws / G, bs), ws & (G - 1), G);
+              const uint32_t vw = __shfl_sync(gm, pick<K>(V, ws / G), ws & (G - 1), G);
+              Hen0 = h + vv(vw >> (8 * bs));
+            }
+          }
+          // update H over [st0, en0] and find the local maximum
+          int32_t lmax = INT32_MIN;
+#pragma unroll
+          for (int i = 0; i < K; ++i) {
+            const int p0 = base + 4 * (k + G * i);
+            if (p0 + 3 >= st0 && p0 <= en0) {
+              const uint32_t vw = V[i];
+              if (p0 >= st0 && p0 + 3 < en0) {
+                H0[i] += vv(vw), H1[i] += vv(vw >> 8), H2[i] += vv(vw >> 16), H3[i] += vv(vw >> 24);
+                lmax = max(lmax, max(max(H0[i], H1[i]), max(H2[i], H3[i])));
+              } else {
+                auto upd = [&](int32_t &h, int b) {
+                  const int p = p0 + b;
+                  if (p == en0) h = Hen0;
+                  else if (p >= st0 && p < en0) h += vv(vw >> (8 * b));
+                  if (p >= st0 && p <= en0) lmax = max(lmax, h);
+                };
+                upd(H0[i], 0);
+                upd(H1[i], 1);
+                upd(H2[i], 2);
+                upd(H3[i], 3);
+              }
+            }
+          }
+          int32_t gmax = lmax;
+#pragma unroll
+          for (int off = G / 2; off > 0; off >>= 1) gmax = max(gmax, __shfl_xor_sync(gm, gmax, off, G));
+          // tie-break of the reference: en0 first, then four int32 lanes over
+          // [st0, en1) (lowest lane, then lowest t), then the scalar tail [en1, en0)
+          uint32_t key = 0xffffffffu;
+          if (lmax == gmax) {
+            const int en1 = st0 + (((en0 - st0) >> 2) << 2);
+#pragma unroll
+            for (int i = 0; i < K; ++i) {
+              const int p0 = base + 4 * (k + G * i);
+              if (p0 + 3 >= st0 && p0 <= en0) {
+                const int32_t hv[4] = {H0[i], H1[i], H2[i], H3[i]};
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                  const int p = p0 + b;
+                  if (p >= st0 && p <= en0 && hv[b] == gmax) {
+                    const uint32_t c = p == en0 ? 0u : p < en1 ? (uint32_t)(1 + ((p - st0) & 3)) : 5u;
+                    const uint32_t kk = p == en0 ? 0u : (c << 24) | (uint32_t)(p - st0);
+                    key = min(key, kk);
+                  }
+                }
+              }
+            }
+          }
+#pragma unroll
+          for (int off = G / 2; off > 0; off >>= 1) key = min(key, __shfl_xor_sync(gm, key, off, G));
+          const int32_t max_H = gmax;
+          const int mt = key == 0 ? en0 : st0 + (int)(key & 0xffffffu);
+          if (en0 == tlen - 1 && Hen0 > mte) mte = Hen0, mte_q = r - en0;
+          if (r - st0 == qlen - 1) {
+            const int ps = st0 - base;
+            const int32_t hs = __shfl_sync(gm, pickH<K>(H0, H1, H2, H3, (ps >> 2) / G, ps & 3), (ps >> 2) & (G - 1), G);
+            if (hs > mqe) mqe = hs, mqe_t = st0;
+          }
+          // ksw_apply_zdrop (ksw2.h:181-197)
+          if (max_H > ez_max) {
+            ez_max = max_H, max_t = mt, max_q = r - mt;
+          } else if (mt >= max_t && r - mt >= max_q) {
+            const int tl = mt - max_t, ql = (r - mt) - max_q, l = tl > ql ? tl - ql : ql - tl;
+            if (zdrop >= 0 && ez_max - max_H > zdrop + l * ez_e) zdropped = 1, done = true;
+          }
+          if (!done) {
+            if (r == qlen + tlen - 2 && en0 == tlen - 1) score = Hen0;
+            if (D2) {
+              if (flag & KSW2G_EXTZ_ONLY) {  // early stop, ksw2_extd2_sse.c:361-367
+                const int32_t rH = last_max_H > max_H ? last_max_H : max_H;
+                const int32_t rq = qlen - (r - st0), rt = tlen - en0;
+                const int32_t rm = rq >= tlen - st0 ? tlen - st0
+                                   : rt >= qlen - (r - en0) ? qlen - (r - en0)
+                                                            : tlen + qlen - 1 - r;
+                if (rH + rm * P.max_sc + end_bonus < ez_max) done = true;
+              }
+              last_max_H = max_H;
+            }
+          }
+        } else {
+          // approximate max: follow one cell per anti-diagonal
+          auto bytev = [&](const uint32_t(&A)[K], int p) -> uint32_t {
+            const int pp = p - base, ws = pp >> 2;
+            return (__shfl_sync(gm, pick<K>(A, ws / G), ws & (G - 1), G) >> (8 * (pp & 3))) & 0xffu;
+          };
+          bool zd = false;
+          if (r > 0) {
+            const bool in1 = last_H0_t >= st0 && last_H0_t <= en0, in2 = last_H0_t + 1 >= st0 && last_H0_t + 1 <= en0;
+            if (in1 && in2) {
+              const int32_t d0 = vv(bytev(V, last_H0_t)), d1 = vv(bytev(U, last_H0_t + 1));
+              if (d0 > d1) Hz += d0;
+              else Hz += d1, ++last_H0_t;
+            } else if (in1) {
+              Hz += vv(bytev(V, last_H0_t));
+            } else {
+              ++last_H0_t;
+              Hz += vv(bytev(U, last_H0_t));
+            }
+            if (!D2) zd = true;
+          } else {
+            Hz = vv(bytev(V, 0)) - qe, last_H0_t = 0;
+          }
+          if (D2) zd = true;
+          if (zd && (flag & KSW2G_APPROX_DROP)) {
+            if (Hz > ez_max) {
+              ez_max = Hz, max_t = last_H0_t, max_q = r - last_H0_t;
+            } else if (last_H0_t >= max_t && r - last_H0_t >= max_q) {
+              const int tl = last_H0_t - max_t, ql = (r - last_H0_t) - max_q, l = tl > ql ? tl - ql : ql - tl;
+              if (zdrop >= 0 && ez_max - Hz > zdrop + l * ez_e) zdropped = 1, done = true;
+            }
+          }
+          if (!done && r == qlen + tlen - 2 && en0 == tlen - 1) score = Hz;
+        }
+        ++r;
+        if (r == qlen + tlen - 1) done = true;
+      }
+    }
+    if (done) {
+      // ---------------- finish the pair: choose the backtrack start (ksw2_extz2_sse.c:284-295) ----------------
+      int reach_end = 0, i0 = -1, j0 = -1;
+      if (CIG) {
+        if (!zdropped && !(flag & KSW2G_EXTZ_ONLY)) i0 = tlen - 1, j0 = qlen - 1;
+        else if ((flag & KSW2G_EXTZ_ONLY) && mqe + end_bonus > ez_max) reach_end = 1, i0 = mqe_t, j0 = qlen - 1;
+        else if (max_t >= 0 && max_q >= 0) i0 = max_t, j0 = max_q;
+      }
+      if (k == 0) {
+        ksw2g_ext_result o;
+        o.score = score, o.max = ez_max, o.max_q = max_q, o.max_t = max_t, o.mqe = mqe, o.mqe_t = mqe_t;
+        o.mte = mte, o.mte_q = mte_q, o.zdropped = zdropped, o.reach_end = reach_end, o.n_cigar = 0;
+        o.n_diag = n_diag, o.cigar_off = 0, o.cells = cells;
+        res[jid] = o;
+        if (CIG) bts[jid] = ksw2g_bt{i0, j0, n_diag, 0};
+      }
+      need = true;
+    }
+  }
+}
+
+}  // namespace ksw2g

@@ -1,0 +1,63 @@
+// launch.h -- host-side entry points of the kernels (C++; used by the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "ksw2g.h"
+#include "shapes.h"
+
+namespace ksw2g {
+
+// Thread-group shapes instantiated for the extension DP kernel.  A pair with
+// n_col_ 16-byte blocks per anti-diagonal needs G*K >= 4*(n_col_+1) words.
+struct ExtShape {
+  int G, K;
+};
+constexpr int kNumExtShapes = KSW2G_NUM_SHAPES;
+extern const ExtShape kExtShapes[kNumExtShapes];
+
+// Smallest instantiated shape index able to hold n_col_ blocks, or -1.
+int ext_shape_for(int n_col);
+// Shape index preferred for n_col_ by the autotuner table (falls back to ext_shape_for).
+int ext_shape_pick(int dual, int mode, int n_col);
+void ext_shape_set_pref(int dual, int mode, int n_col_lo, int n_col_hi, int shape);
+
+struct ExtLaunch {
+  const ksw2g_job *jobs;
+  const int32_t *order;
+  int n_jobs;
+  const uint8_t *arena;
+  ksw2g_ext_result *res;
+  ksw2g_bt *bts;
+  uint8_t *tb_pool;
+  const int64_t *tb_off;
+  int *job_counter;
+};
+
+// Launch the DP kernel of (dual, mode, shape) as a persistent grid.
+cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,
+                          int max_blocks, cudaStream_t st);
+cudaError_t launch_ext_bt(const ksw2g_job *jobs, int n_jobs, const ksw2g_bt *bts, const uint8_t *tb_pool,
+                          const int64_t *tb_off, ksw2g_ext_result *res, uint32_t *cigar_out,
+                          unsigned long long *cursor, long long cigar_cap, int *err, cudaStream_t st);
+cudaError_t launch_pack(int n, const uint8_t *raw, const int64_t *raw_off, const int32_t *len, uint8_t *arena,
+                        const int64_t *dst_off, cudaStream_t st);
+
+// ksw_ll (striped local SW)
+struct LLLaunch {
+  const ksw2g_ll_job *jobs;
+  int n_jobs;
+  const uint8_t *arena;
+  const int8_t *mat;
+  int m;
+  int gapo, gape;
+  ksw2g_ll_result *res;
+  uint64_t *blist;          // per-job second-best scratch (KSW_LL_SUBO), may be null
+  const int64_t *blist_off;
+  int *job_counter;
+};
+cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st);
+int ll_slen_cap(int size);
+
+int num_sms(int device);
+
+}  // namespace ksw2g

@@ -1,0 +1,55 @@
+// ll_kernels.cu -- instantiations and launcher of the striped local-alignment kernel.
+#include <cuda_runtime.h>
+#include "launch.h"
+#include "ll.cuh"
+
+namespace ksw2g {
+
+typedef void (*ll_fn)(const ksw2g_ll_job *, int, const uint8_t *, const int8_t *, int, int, int, ksw2g_ll_result *,
+                      uint64_t *, const int64_t *, int *);
+
+static const int kSlen[] = {8, 16, 32, 64};
+static const ll_fn kLL[2][4] = {{ll_kernel<1, 8>, ll_kernel<1, 16>, ll_kernel<1, 32>, ll_kernel<1, 64>},
+                                {ll_kernel<2, 8>, ll_kernel<2, 16>, ll_kernel<2, 32>, ll_kernel<2, 64>}};
+
+int ll_slen_cap(int size) { (void)size; return 64; }
+
+cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st) {
+  if (L.n_jobs <= 0) return cudaSuccess;
+  int si = -1;
+  for (int i = 0; i < 4; ++i)
+    if (slen_max <= kSlen[i]) {
+      si = i;
+      break;
+    }
+  if (si < 0 || (size != 1 && size != 2)) return cudaErrorInvalidValue;
+  const ll_fn fn = kLL[size - 1][si];
+  const int lanes = size == 1 ? 16 : 8, groups = 128 / lanes;
+  const size_t smem = (size_t)groups * (L.m * kSlen[si] * lanes + 8) * sizeof(int16_t);
+  static int occ[2][4][17] = {};
+  static int sms = 0;
+  const int mi = L.m < 16 ? L.m : 16;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  if (!occ[size - 1][si][mi]) {
+    int o = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, 128, smem);
+    occ[size - 1][si][mi] = o > 0 ? o : 1;
+  }
+  if (!sms) {
+    int d = 0;
+    cudaGetDevice(&d);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+  }
+  int blocks = (L.n_jobs + groups - 1) / groups;
+  const int cap = sms * occ[size - 1][si][mi];
+  if (blocks > cap) blocks = cap;
+  if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
+  fn<<<blocks, 128, smem, st>>>(L.jobs, L.n_jobs, L.arena, L.mat, L.m, L.gapo, L.gape, L.res, L.blist, L.blist_off,
+                                L.job_counter);
+  return cudaGetLastError();
+}
+
+}  // namespace ksw2g

@@ -1,0 +1,322 @@
+"""ctypes binding of libksw2gpu.so.
+
+Two surfaces:
+  * the reference-shaped per-call functions (ksw_extz2_sse, ksw_extd2_sse, ksw_ll_*),
+    with the same argument meaning and results as ksw2.h of the reference;
+  * the batched API (Context, ExtBatch, LLBatch) over include/ksw2_gb300.h.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+
+KSW_NEG_INF = -0x40000000
+KSW_EZ_SCORE_ONLY = 0x01
+KSW_EZ_RIGHT = 0x02
+KSW_EZ_GENERIC_SC = 0x04
+KSW_EZ_APPROX_MAX = 0x08
+KSW_EZ_APPROX_DROP = 0x10
+KSW_EZ_EXTZ_ONLY = 0x40
+KSW_EZ_REV_CIGAR = 0x80
+KSW_LL_STOP = 0x20000
+KSW_LL_SUBO = 0x40000
+
+# include/ksw2_gb300.h layouts
+EXT_JOB = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"),
+                    ("w", "<i4"), ("zdrop", "<i4"), ("end_bonus", "<i4"), ("flag", "<i4")])
+EXT_RESULT = np.dtype([("score", "<i4"), ("max", "<i4"), ("max_q", "<i4"), ("max_t", "<i4"),
+                       ("mqe", "<i4"), ("mqe_t", "<i4"), ("mte", "<i4"), ("mte_q", "<i4"),
+                       ("zdropped", "<i4"), ("reach_end", "<i4"), ("n_cigar", "<i4"), ("n_diag", "<i4"),
+                       ("cigar_off", "<i8"), ("cells", "<i8")])
+LL_JOB = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"),
+                   ("xtra", "<i4"), ("pad", "<i4")])
+LL_RESULT = np.dtype([("score", "<i4"), ("te", "<i4"), ("qe", "<i4"), ("score2", "<i4"),
+                      ("te2", "<i4"), ("rows", "<i4")])
+assert EXT_JOB.itemsize == 40 and EXT_RESULT.itemsize == 64 and LL_JOB.itemsize == 32 and LL_RESULT.itemsize == 24
+
+
+class KswExtz(C.Structure):
+    """ksw_extz_t (ksw2.h:36-45)."""
+    _fields_ = [("max", C.c_uint32, 31), ("zdropped", C.c_uint32, 1),
+                ("max_q", C.c_int), ("max_t", C.c_int), ("mqe", C.c_int), ("mqe_t", C.c_int),
+                ("mte", C.c_int), ("mte_q", C.c_int), ("score", C.c_int),
+                ("m_cigar", C.c_int), ("n_cigar", C.c_int), ("reach_end", C.c_int),
+                ("cigar", C.POINTER(C.c_uint32))]
+
+    def cigar_list(self):
+        return [self.cigar[i] for i in range(self.n_cigar)]
+
+    def fields(self):
+        return dict(max=self.max, zdropped=self.zdropped, max_q=self.max_q, max_t=self.max_t, mqe=self.mqe,
+                    mqe_t=self.mqe_t, mte=self.mte, mte_q=self.mte_q, score=self.score,
+                    reach_end=self.reach_end, n_cigar=self.n_cigar, cigar=self.cigar_list())
+
+
+class KswLLRst(C.Structure):
+    """ksw_llrst_t (ksw2.h:47-51)."""
+    _fields_ = [("score", C.c_int), ("te", C.c_int), ("qe", C.c_int), ("score2", C.c_int), ("te2", C.c_int)]
+
+
+def lib_path():
+    return os.environ.get("KSW2GPU_LIB", os.path.join(_PKG, "libksw2gpu.so"))
+
+
+_lib = None
+
+
+def load_library():
+    """Load libksw2gpu.so; raises if it is missing (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = lib_path()
+    if not os.path.exists(p):
+        raise RuntimeError(f"libksw2gpu.so not found at {p}: build it with `python -m minibwa_gb300.build`")
+    L = C.CDLL(p)
+    vp, i32, i64, u8p, i8 = C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_int8
+    sig = {
+        "ksw2g_ctx_create": (i32, [i32, C.POINTER(vp)]),
+        "ksw2g_ctx_destroy": (None, [vp]),
+        "ksw2g_ctx_stream": (vp, [vp]),
+        "ksw2g_ctx_sync": (i32, [vp]),
+        "ksw2g_ctx_set_tb_budget": (i32, [vp, i64]),
+        "ksw2g_last_error": (C.c_char_p, []),
+        "ksw2g_ext_batch": (i32, [vp, i32, i8, vp, i8, i8, i8, i8, i32, vp, u8p, i64, u8p, i64, vp, vp, i64,
+                                  C.POINTER(i64)]),
+        "ksw2g_ll_batch": (i32, [vp, i32, i32, vp, i32, i32, i32, vp, u8p, i64, u8p, i64, vp]),
+        "ksw2g_ext_prepare": (i32, [vp, i32, i8, vp, i8, i8, i8, i8, i32, vp, u8p, i64, u8p, i64, C.POINTER(vp)]),
+        "ksw2g_ll_prepare": (i32, [vp, i32, i32, vp, i32, i32, i32, vp, u8p, i64, u8p, i64, C.POINTER(vp)]),
+        "ksw2g_batch_run": (i32, [vp, vp]),
+        "ksw2g_ext_fetch": (i32, [vp, vp, vp, vp, i64, C.POINTER(i64)]),
+        "ksw2g_ll_fetch": (i32, [vp, vp, vp]),
+        "ksw2g_batch_launches": (i32, [vp]),
+        "ksw2g_batch_free": (None, [vp]),
+        "ksw2g_ext_num_shapes": (i32, []),
+        "ksw2g_ext_shape_info": (i32, [i32, C.POINTER(i32), C.POINTER(i32)]),
+        "ksw2g_ext_set_shape": (i32, [i32, i32, i32, i32, i32]),
+        "ksw2g_probe_int32_peak": (i32, [i32, C.POINTER(C.c_double)]),
+        "ksw_extz2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i32, i32, i32, i32, C.POINTER(KswExtz)]),
+        "ksw_extd2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i8, i8, i32, i32, i32, i32,
+                                 C.POINTER(KswExtz)]),
+        "ksw_ll_qinit": (vp, [vp, i32, i32, u8p, i32, vp]),
+        "ksw_ll_u8_core": (KswLLRst, [vp, i32, u8p, i32, i32, i32]),
+        "ksw_ll_i16_core": (KswLLRst, [vp, i32, u8p, i32, i32, i32]),
+        "ksw_ll_i16": (i32, [vp, i32, u8p, i32, i32, C.POINTER(i32), C.POINTER(i32)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError(f"ksw2gpu error {rc}: {_lib.ksw2g_last_error().decode()}")
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+_libc = C.CDLL(None)
+_libc.free.argtypes = [C.c_void_p]
+
+
+def gen_nt4_mat(a=2, b=8, b_ts=0, b_ambi=1, mt=0):
+    """ksw_gen_nt4_mat (ksw2.h:199-219) as an int8 numpy array of 25."""
+    m = 5
+    a = abs(a)
+    b = -abs(b)
+    b_ambi = -abs(b_ambi)
+    mat = np.zeros(25, np.int8)
+    for i in range(m - 1):
+        for j in range(m - 1):
+            mat[i * m + j] = a if i == j else b
+        mat[i * m + m - 1] = b_ambi
+    for j in range(m):
+        mat[(m - 1) * m + j] = b_ambi
+    if b_ts != 0 and -abs(b_ts) != b:
+        bt = -abs(b_ts)
+        mat[0 * m + 2] = mat[1 * m + 3] = mat[2 * m + 0] = mat[3 * m + 1] = bt
+    if mt == 1:
+        mat[1 * m + 3] = a
+    elif mt == 2:
+        mat[2 * m + 0] = a
+    return mat
+
+
+# ------------------------------------------------------------------ per-call (reference-shaped)
+def _u8(a):
+    return np.ascontiguousarray(a, dtype=np.uint8)
+
+
+def ksw_extz2_sse(query, target, m, mat, q, e, w, zdrop, end_bonus, flag, ez=None):
+    L = load_library()
+    q_, t_, mat_ = _u8(query), _u8(target), np.ascontiguousarray(mat, np.int8)
+    ez = ez if ez is not None else KswExtz()
+    L.ksw_extz2_sse(None, len(q_), _ptr(q_), len(t_), _ptr(t_), m, _ptr(mat_), q, e, w, zdrop, end_bonus, flag,
+                    C.byref(ez))
+    return ez
+
+
+def ksw_extd2_sse(query, target, m, mat, q, e, q2, e2, w, zdrop, end_bonus, flag, ez=None):
+    L = load_library()
+    q_, t_, mat_ = _u8(query), _u8(target), np.ascontiguousarray(mat, np.int8)
+    ez = ez if ez is not None else KswExtz()
+    L.ksw_extd2_sse(None, len(q_), _ptr(q_), len(t_), _ptr(t_), m, _ptr(mat_), q, e, q2, e2, w, zdrop, end_bonus,
+                    flag, C.byref(ez))
+    return ez
+
+
+def free_extz(ez):
+    if ez.cigar:
+        _libc.free(C.cast(ez.cigar, C.c_void_p))
+        ez.cigar = None
+        ez.m_cigar = 0
+
+
+def ksw_ll_qinit(size, query, m, mat):
+    L = load_library()
+    q_, mat_ = _u8(query), np.ascontiguousarray(mat, np.int8)
+    return L.ksw_ll_qinit(None, size, len(q_), _ptr(q_), m, _ptr(mat_))
+
+
+def ll_free(qp):
+    _libc.free(qp)
+
+
+def ksw_ll_u8_core(qp, target, gapo, gape, xtra):
+    t_ = _u8(target)
+    return load_library().ksw_ll_u8_core(qp, len(t_), _ptr(t_), gapo, gape, xtra)
+
+
+def ksw_ll_i16_core(qp, target, gapo, gape, xtra):
+    t_ = _u8(target)
+    return load_library().ksw_ll_i16_core(qp, len(t_), _ptr(t_), gapo, gape, xtra)
+
+
+def ksw_ll_i16(qp, target, gapo, gape):
+    t_ = _u8(target)
+    qe, te = C.c_int(), C.c_int()
+    s = load_library().ksw_ll_i16(qp, len(t_), _ptr(t_), gapo, gape, C.byref(qe), C.byref(te))
+    return s, qe.value, te.value
+
+
+# ------------------------------------------------------------------ batched API
+class Context:
+    """One CUDA stream and its device pools (ksw2g_ctx_t)."""
+
+    def __init__(self, device=0, tb_budget=None):
+        self.L = load_library()
+        h = C.c_void_p()
+        _check(self.L.ksw2g_ctx_create(device, C.byref(h)))
+        self.h = h
+        if tb_budget:
+            _check(self.L.ksw2g_ctx_set_tb_budget(self.h, int(tb_budget)))
+
+    @property
+    def stream(self):
+        return self.L.ksw2g_ctx_stream(self.h)
+
+    def sync(self):
+        _check(self.L.ksw2g_ctx_sync(self.h))
+
+    def close(self):
+        if self.h:
+            self.L.ksw2g_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ext_batch(self, dual, m, mat, q, e, q2, e2, jobs, qbuf, tbuf):
+        """One-shot batch of extension jobs; returns (results, cigar words)."""
+        jobs = np.ascontiguousarray(jobs, EXT_JOB)
+        qbuf, tbuf, mat = _u8(qbuf), _u8(tbuf), np.ascontiguousarray(mat, np.int8)
+        n = len(jobs)
+        res = np.zeros(n, EXT_RESULT)
+        cap = int(((jobs["qlen"].astype(np.int64) + jobs["tlen"] + 1)).sum()) + 16
+        cig = np.zeros(cap, np.uint32)
+        used = C.c_int64()
+        _check(self.L.ksw2g_ext_batch(self.h, int(dual), m, _ptr(mat), q, e, q2, e2, n, _ptr(jobs), _ptr(qbuf),
+                                      len(qbuf), _ptr(tbuf), len(tbuf), _ptr(res), _ptr(cig), cap, C.byref(used)))
+        return res, cig[:used.value]
+
+    def ll_batch(self, size, m, mat, gapo, gape, jobs, qbuf, tbuf):
+        jobs = np.ascontiguousarray(jobs, LL_JOB)
+        qbuf, tbuf, mat = _u8(qbuf), _u8(tbuf), np.ascontiguousarray(mat, np.int8)
+        res = np.zeros(len(jobs), LL_RESULT)
+        _check(self.L.ksw2g_ll_batch(self.h, size, m, _ptr(mat), gapo, gape, len(jobs), _ptr(jobs), _ptr(qbuf),
+                                     len(qbuf), _ptr(tbuf), len(tbuf), _ptr(res)))
+        return res
+
+
+def probe_int32_peak(device=0):
+    """Measured 32-bit integer lane-ops per second of the device."""
+    v = C.c_double()
+    _check(load_library().ksw2g_probe_int32_peak(device, C.byref(v)))
+    return v.value
+
+
+class _Batch:
+    def __init__(self, ctx):
+        self.ctx, self.L, self.h = ctx, ctx.L, C.c_void_p()
+
+    def run(self):
+        _check(self.L.ksw2g_batch_run(self.ctx.h, self.h))
+
+    @property
+    def launches(self):
+        return self.L.ksw2g_batch_launches(self.h)
+
+    def free(self):
+        if self.h:
+            self.L.ksw2g_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class ExtBatch(_Batch):
+    """Resident extension batch: inputs uploaded once, run() enqueues the DP asynchronously."""
+
+    def __init__(self, ctx, dual, m, mat, q, e, q2, e2, jobs, qbuf, tbuf):
+        super().__init__(ctx)
+        jobs = np.ascontiguousarray(jobs, EXT_JOB)
+        qbuf, tbuf, mat = _u8(qbuf), _u8(tbuf), np.ascontiguousarray(mat, np.int8)
+        self.n = len(jobs)
+        self.cap = int(((jobs["qlen"].astype(np.int64) + jobs["tlen"] + 1)).sum()) + 16
+        _check(self.L.ksw2g_ext_prepare(ctx.h, int(dual), m, _ptr(mat), q, e, q2, e2, self.n, _ptr(jobs),
+                                        _ptr(qbuf), len(qbuf), _ptr(tbuf), len(tbuf), C.byref(self.h)))
+
+    def fetch(self, res=None, cig=None):
+        res = res if res is not None else np.zeros(self.n, EXT_RESULT)
+        cig = cig if cig is not None else np.zeros(self.cap, np.uint32)
+        used = C.c_int64()
+        _check(self.L.ksw2g_ext_fetch(self.ctx.h, self.h, _ptr(res), _ptr(cig), len(cig), C.byref(used)))
+        return res, cig[:used.value]
+
+
+class LLBatch(_Batch):
+    def __init__(self, ctx, size, m, mat, gapo, gape, jobs, qbuf, tbuf):
+        super().__init__(ctx)
+        jobs = np.ascontiguousarray(jobs, LL_JOB)
+        qbuf, tbuf, mat = _u8(qbuf), _u8(tbuf), np.ascontiguousarray(mat, np.int8)
+        self.n = len(jobs)
+        _check(self.L.ksw2g_ll_prepare(ctx.h, size, m, _ptr(mat), gapo, gape, self.n, _ptr(jobs), _ptr(qbuf),
+                                       len(qbuf), _ptr(tbuf), len(tbuf), C.byref(self.h)))
+
+    def fetch(self, res=None):
+        res = res if res is not None else np.zeros(self.n, LL_RESULT)
+        _check(self.L.ksw2g_ll_fetch(self.ctx.h, self.h, _ptr(res)))
+        return res

@@ -1,0 +1,191 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+No public dataset is named for this path; these generators stand in for real
+reads.  Config numbering follows the benchmark definition:
+
+  0  extz2, 150 nt, 0.1% N, 1% subst, 0.2% indels (1-3), +30 flank, w=25   (20,000 pairs)
+  1  extd2, 100-300 nt, 2% subst, 0.5% indels (geom p=.5, <=20), +50 flank,
+     1% with a 200-nt junk query suffix, w=100                             (1,000,000 pairs)
+  2  mixed: long extd2 (log-normal median 2 kb, 500 nt-30 kb, 0.5% subst,
+     0.3% indels 1-5, +100 flank, w=500, zdrop=400) + short extz2 as config 0
+  3  ksw_ll i16 rescue: 150 nt vs 500-1000 nt, 30% with a planted copy
+     (2% subst, 0.3% indels)                                               (2,000,000 jobs)
+Scoring everywhere: match +2, mismatch -8, N -1 (ksw_gen_nt4_mat(2,8,0,1)), q=12, e=2
+(q2=24, e2=1 for extd2).  RNG: splitmix64, seed 11.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .lib import EXT_JOB, LL_JOB, KSW_EZ_EXTZ_ONLY, gen_nt4_mat
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+SEED = 11
+
+
+class ExtSpec(C.Structure):
+    _fields_ = [("qlen_lo", C.c_int), ("qlen_hi", C.c_int), ("lognorm_median", C.c_double),
+                ("lognorm_sigma", C.c_double), ("clip_lo", C.c_int), ("clip_hi", C.c_int),
+                ("n_rate", C.c_double), ("sub_rate", C.c_double), ("indel_rate", C.c_double),
+                ("indel_p", C.c_double), ("indel_max", C.c_int), ("flank", C.c_int),
+                ("junk_frac", C.c_double), ("junk_len", C.c_int)]
+
+
+class LLSpec(C.Structure):
+    _fields_ = [("qlen", C.c_int), ("tlen_lo", C.c_int), ("tlen_hi", C.c_int), ("plant_frac", C.c_double),
+                ("sub_rate", C.c_double), ("indel_rate", C.c_double), ("indel_p", C.c_double),
+                ("indel_max", C.c_int)]
+
+
+_L = None
+
+
+def _lib():
+    global _L
+    if _L is None:
+        p = os.path.join(_PKG, "libksw2synth.so")
+        if not os.path.exists(p):
+            raise RuntimeError("libksw2synth.so missing: run `python -m minibwa_gb300.build`")
+        _L = C.CDLL(p)
+        args = [C.c_void_p, C.c_uint64, C.c_int] + [C.c_void_p] * 6 + [C.c_int64, C.c_void_p, C.c_int64,
+                                                                          C.c_void_p, C.c_void_p]
+        for f in (_L.synth_ext, _L.synth_ll):
+            f.restype = C.c_int
+        _L.synth_ext.argtypes = [C.POINTER(ExtSpec), C.c_uint64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        _L.synth_ll.argtypes = [C.POINTER(LLSpec), C.c_uint64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        del args
+    return _L
+
+
+SPEC_SHORT = dict(qlen_lo=150, qlen_hi=150, n_rate=0.001, sub_rate=0.01, indel_rate=0.002, indel_p=0.5,
+                  indel_max=3, flank=30)
+SPEC_MID = dict(qlen_lo=100, qlen_hi=300, sub_rate=0.02, indel_rate=0.005, indel_p=0.5, indel_max=20, flank=50,
+                junk_frac=0.01, junk_len=200)
+SPEC_LONG = dict(lognorm_median=2000.0, lognorm_sigma=0.8, clip_lo=500, clip_hi=30000, sub_rate=0.005,
+                 indel_rate=0.003, indel_p=0.5, indel_max=5, flank=100)
+
+
+class Pairs:
+    """A set of extension jobs with back-to-back sequence buffers."""
+
+    def __init__(self, jobs, qbuf, tbuf, dual, mat, q, e, q2, e2, name):
+        self.jobs, self.qbuf, self.tbuf = jobs, qbuf, tbuf
+        self.dual, self.mat, self.q, self.e, self.q2, self.e2 = dual, mat, q, e, q2, e2
+        self.name = name
+
+    def __len__(self):
+        return len(self.jobs)
+
+    def subset(self, idx):
+        """Jobs idx re-packed into compact buffers."""
+        idx = np.asarray(idx)
+        j = self.jobs[idx].copy()
+        qparts = [self.qbuf[o:o + n] for o, n in zip(j["qoff"], j["qlen"])]
+        tparts = [self.tbuf[o:o + n] for o, n in zip(j["toff"], j["tlen"])]
+        j["qoff"] = np.concatenate([[0], np.cumsum([len(x) for x in qparts])[:-1]]) if len(qparts) else []
+        j["toff"] = np.concatenate([[0], np.cumsum([len(x) for x in tparts])[:-1]]) if len(tparts) else []
+        qb = np.concatenate(qparts) if qparts else np.zeros(0, np.uint8)
+        tb = np.concatenate(tparts) if tparts else np.zeros(0, np.uint8)
+        return Pairs(j, qb, tb, self.dual, self.mat, self.q, self.e, self.q2, self.e2, self.name)
+
+    def query(self, i):
+        j = self.jobs[i]
+        return self.qbuf[j["qoff"]:j["qoff"] + j["qlen"]]
+
+    def target(self, i):
+        j = self.jobs[i]
+        return self.tbuf[j["toff"]:j["toff"] + j["tlen"]]
+
+
+def ext_pairs(n, spec, w, zdrop, end_bonus, flag=KSW_EZ_EXTZ_ONLY, dual=False, seed=SEED, name="pairs"):
+    s = ExtSpec(**{**dict(qlen_lo=0, qlen_hi=0, lognorm_median=0.0, lognorm_sigma=0.0, clip_lo=0, clip_hi=0,
+                          n_rate=0.0, sub_rate=0.0, indel_rate=0.0, indel_p=0.5, indel_max=1, flank=0,
+                          junk_frac=0.0, junk_len=0), **spec})
+    qmax = max(s.qlen_hi, s.clip_hi) + s.junk_len
+    qcap = int(n) * qmax + 64
+    tcap = int(n) * (int(qmax * (1 + 2 * s.indel_rate * s.indel_max)) + s.flank + 64) + 64
+    jobs = np.zeros(n, EXT_JOB)
+    qoff, toff = np.zeros(n, np.int64), np.zeros(n, np.int64)
+    qlen, tlen = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    qbuf, tbuf = np.zeros(qcap, np.uint8), np.zeros(tcap, np.uint8)
+    qu, tu = C.c_int64(), C.c_int64()
+    rc = _lib().synth_ext(C.byref(s), seed, n, qoff.ctypes.data, qlen.ctypes.data, toff.ctypes.data,
+                          tlen.ctypes.data, qbuf.ctypes.data, qcap, tbuf.ctypes.data, tcap, C.byref(qu), C.byref(tu))
+    if rc != 0:
+        raise RuntimeError("synth_ext: buffer capacity exceeded")
+    jobs["qoff"], jobs["toff"], jobs["qlen"], jobs["tlen"] = qoff, toff, qlen, tlen
+    jobs["w"], jobs["zdrop"], jobs["end_bonus"], jobs["flag"] = w, zdrop, end_bonus, flag
+    mat = gen_nt4_mat(2, 8, 0, 1)
+    q2, e2 = (24, 1) if dual else (12, 2)
+    return Pairs(jobs, qbuf[:qu.value].copy(), tbuf[:tu.value].copy(), dual, mat, 12, 2, q2, e2, name)
+
+
+def config0(n=20000, seed=SEED):
+    return ext_pairs(n, SPEC_SHORT, 25, 100, 10, KSW_EZ_EXTZ_ONLY, False, seed, "cfg0-extz2-150nt-w25")
+
+
+def config1(n=1000000, seed=SEED + 1):
+    return ext_pairs(n, SPEC_MID, 100, 100, 10, KSW_EZ_EXTZ_ONLY, True, seed, "cfg1-extd2-100-300nt-w100")
+
+
+def config2_long(n=200000, seed=SEED + 2):
+    return ext_pairs(n, SPEC_LONG, 500, 400, -1, KSW_EZ_EXTZ_ONLY, True, seed, "cfg2-extd2-lognorm2kb-w500")
+
+
+def config2_short(n=1000000, seed=SEED + 3):
+    return ext_pairs(n, SPEC_SHORT, 25, 100, 10, KSW_EZ_EXTZ_ONLY, False, seed, "cfg2-extz2-150nt-w25")
+
+
+class Rescue:
+    """A set of ksw_ll jobs."""
+
+    def __init__(self, jobs, qbuf, tbuf, size, mat, gapo, gape, name):
+        self.jobs, self.qbuf, self.tbuf = jobs, qbuf, tbuf
+        self.size, self.mat, self.gapo, self.gape, self.name = size, mat, gapo, gape, name
+
+    def __len__(self):
+        return len(self.jobs)
+
+    def subset(self, idx):
+        idx = np.asarray(idx)
+        j = self.jobs[idx].copy()
+        qparts = [self.qbuf[o:o + n] for o, n in zip(j["qoff"], j["qlen"])]
+        tparts = [self.tbuf[o:o + n] for o, n in zip(j["toff"], j["tlen"])]
+        j["qoff"] = np.concatenate([[0], np.cumsum([len(x) for x in qparts])[:-1]])
+        j["toff"] = np.concatenate([[0], np.cumsum([len(x) for x in tparts])[:-1]])
+        return Rescue(j, np.concatenate(qparts), np.concatenate(tparts), self.size, self.mat, self.gapo,
+                      self.gape, self.name)
+
+
+def ll_jobs(n, qlen=150, tlen_lo=500, tlen_hi=1000, plant=0.3, size=2, xtra=0, mat=None, gapo=12, gape=2,
+            seed=SEED + 4, name="rescue"):
+    s = LLSpec(qlen=qlen, tlen_lo=tlen_lo, tlen_hi=tlen_hi, plant_frac=plant, sub_rate=0.02, indel_rate=0.003,
+               indel_p=0.5, indel_max=3)
+    qcap, tcap = int(n) * qlen + 64, int(n) * tlen_hi + 64
+    qoff, toff = np.zeros(n, np.int64), np.zeros(n, np.int64)
+    ql, tl = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    qbuf, tbuf = np.zeros(qcap, np.uint8), np.zeros(tcap, np.uint8)
+    qu, tu = C.c_int64(), C.c_int64()
+    rc = _lib().synth_ll(C.byref(s), seed, n, qoff.ctypes.data, ql.ctypes.data, toff.ctypes.data, tl.ctypes.data,
+                         qbuf.ctypes.data, qcap, tbuf.ctypes.data, tcap, C.byref(qu), C.byref(tu))
+    if rc != 0:
+        raise RuntimeError("synth_ll: buffer capacity exceeded")
+    jobs = np.zeros(n, LL_JOB)
+    jobs["qoff"], jobs["toff"], jobs["qlen"], jobs["tlen"], jobs["xtra"] = qoff, toff, ql, tl, xtra
+    mat = gen_nt4_mat(2, 8, 0, 1) if mat is None else mat
+    return Rescue(jobs, qbuf[:qu.value].copy(), tbuf[:tu.value].copy(), size, mat, gapo, gape, name)
+
+
+def config3(n=2000000, seed=SEED + 4):
+    return ll_jobs(n, seed=seed, name="cfg3-ll-i16-150vs500-1000")
+
+
+def config3_pe(n=200000, seed=SEED + 5):
+    """pe.c rescue variant (pe.c:252-271): matrix scaled by a=2 (match 1, mismatch 4, N 1), gapo=6,
+    gape=1, u8 core with KSW_LL_SUBO | min_len(19)."""
+    from .lib import KSW_LL_SUBO
+    mat = gen_nt4_mat(1, 4, 0, 1)
+    return ll_jobs(n, size=1, xtra=KSW_LL_SUBO | 19, mat=mat, gapo=6, gape=1, seed=seed, name="cfg3-ll-u8-pe")

@@ -1,0 +1,122 @@
+// emu_kernels.cpp -- the CUDA kernels of minibwa_gb300/csrc compiled for the
+// host through cuda_emu.h (TEST INFRASTRUCTURE).  Lets the CPU test suite run
+// the exact device code paths -- window sliding, shuffles, votes, lockstep
+// groups, the work counter -- on small inputs without a GPU.
+#include <chrono>
+#include <thread>
+#include <vector>
+
+#include "cuda_emu.h"
+
+thread_local emu_dim3 threadIdx, blockIdx;
+emu_dim3 blockDim, gridDim;
+namespace emu {
+Warp *g_warps = nullptr;
+LaneState g_lane_state[1024];
+}
+
+#include "../../minibwa_gb300/csrc/ext_bt.cuh"
+#include "../../minibwa_gb300/csrc/ext_dp.cuh"
+#include "../../minibwa_gb300/csrc/host_common.h"
+#include "../../minibwa_gb300/csrc/ll.cuh"
+#include "../../minibwa_gb300/csrc/shapes.h"
+
+namespace ksw2g {
+int16_t ll_smem[1 << 20];
+}
+
+using namespace ksw2g;
+
+template <class F>
+static void run_block(int nthreads, F f) {
+  blockDim.x = nthreads;
+  gridDim.x = 1;
+  std::vector<emu::Warp> warps((nthreads + 31) / 32);
+  for (size_t w = 0; w < warps.size(); ++w) {
+    const int n = std::min(32, nthreads - (int)w * 32);
+    warps[w].present = n == 32 ? 0xffffffffu : ((1u << n) - 1u);
+  }
+  emu::g_warps = warps.data();
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t)
+    th.emplace_back([=] {
+      threadIdx.x = t;
+      blockIdx.x = 0;
+      f();
+    });
+  std::atomic<bool> fin{false};
+  std::thread dog([&] {
+    for (int i = 0; i < 100 && !fin; ++i) std::this_thread::sleep_for(std::chrono::milliseconds(50));
+    if (fin) return;
+    for (int t = 0; t < nthreads; ++t)
+      fprintf(stderr, "[emu watchdog] thread %d last mask %08x calls %ld\n", t, emu::g_lane_state[t].mask.load(),
+              emu::g_lane_state[t].calls.load());
+  });
+  for (auto &x : th) x.join();
+  fin = true;
+  dog.join();
+}
+
+typedef void (*ext_fn)(const ksw2g_job *, const int32_t *, int, const uint8_t *, const ksw2g_ext_params,
+                       ksw2g_ext_result *, ksw2g_bt *, uint8_t *, const int64_t *, int *);
+#define ROW(i, G, K) {{ext_dp_kernel<0, 0, G, K>, ext_dp_kernel<0, 1, G, K>, ext_dp_kernel<0, 2, G, K>}, \
+                      {ext_dp_kernel<1, 0, G, K>, ext_dp_kernel<1, 1, G, K>, ext_dp_kernel<1, 2, G, K>}},
+static const ext_fn kTab[KSW2G_NUM_SHAPES][2][3] = {KSW2G_SHAPES(ROW)};
+#undef ROW
+#define SH(i, G, K) {G, K},
+static const int kShape[KSW2G_NUM_SHAPES][2] = {KSW2G_SHAPES(SH)};
+#undef SH
+
+extern "C" {
+
+int emu_num_shapes(void) { return KSW2G_NUM_SHAPES; }
+int emu_shape_words(int s) { return kShape[s][0] * kShape[s][1]; }
+
+void emu_derive_params(int dual, int m, const int8_t *mat, int q, int e, int q2, int e2, ksw2g_ext_params *P) {
+  derive_ext_params(dual, (int8_t)m, mat, (int8_t)q, (int8_t)e, (int8_t)q2, (int8_t)e2, *P);
+}
+
+// Run the DP kernel of (dual, mode, shape) over all jobs with one emulated warp
+// (`threads` lanes), then the backtrack kernel.  The arena must already be padded
+// as the device arena is (32 zero bytes around every sequence).
+int emu_ext(int dual, int mode, int shape, const ksw2g_ext_params *P, int n, const ksw2g_job *jobs,
+            const uint8_t *arena, ksw2g_ext_result *res, ksw2g_bt *bts, uint8_t *tb_pool, const int64_t *tb_off,
+            uint32_t *cigar, long long cap, int threads) {
+  if (shape < 0 || shape >= KSW2G_NUM_SHAPES) return -1;
+  int counter = 0;
+  const ext_fn f = kTab[shape][dual][mode];
+  const ksw2g_ext_params Pc = *P;
+  run_block(threads, [&] { f(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter); });
+  if (mode != 0) {
+    unsigned long long cursor = 0;
+    int err = 0;
+    blockDim.x = 1;
+    for (int j = 0; j < n; ++j) {
+      threadIdx.x = 0;
+      blockIdx.x = j;
+      ext_bt_kernel(jobs, n, bts, tb_pool, tb_off, res, cigar, &cursor, cap, &err);
+    }
+    if (err) return -2;
+  }
+  return 0;
+}
+
+int emu_ll(int size, int slen_max, int n, const ksw2g_ll_job *jobs, const uint8_t *arena, const int8_t *mat, int m,
+           int gapo, int gape, ksw2g_ll_result *res, uint64_t *blist, const int64_t *blist_off, int threads) {
+  int counter = 0;
+  typedef void (*ll_fn)(const ksw2g_ll_job *, int, const uint8_t *, const int8_t *, int, int, int,
+                        ksw2g_ll_result *, uint64_t *, const int64_t *, int *);
+  ll_fn f = nullptr;
+  const int sl[] = {8, 16, 32, 64};
+  const ll_fn t1[] = {ll_kernel<1, 8>, ll_kernel<1, 16>, ll_kernel<1, 32>, ll_kernel<1, 64>};
+  const ll_fn t2[] = {ll_kernel<2, 8>, ll_kernel<2, 16>, ll_kernel<2, 32>, ll_kernel<2, 64>};
+  for (int i = 0; i < 4; ++i)
+    if (slen_max <= sl[i]) {
+      f = size == 1 ? t1[i] : t2[i];
+      break;
+    }
+  if (!f) return -1;
+  run_block(threads, [&] { f(jobs, n, arena, mat, m, gapo, gape, res, blist, blist_off, &counter); });
+  return 0;
+}
+}

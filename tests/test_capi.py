@@ -1,0 +1,80 @@
+"""The C ABI library without a GPU: it loads, exports every declared symbol, and the
+host-side entry points fail with error codes (not crashes) when no device exists."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_functions():
+    names = []
+    for h in ("ksw2.h", "ksw2_gb300.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(\w+)\s*\(", src, flags=re.M):
+            name = m.group(1)
+            if name.startswith(("ksw_", "ksw2g_")):
+                names.append(name)
+    return sorted(set(names))
+
+
+def test_header_declares_reference_entry_points():
+    names = _declared_functions()
+    for ref_name in ("ksw_extz2_sse", "ksw_extd2_sse", "ksw_ll_qinit", "ksw_ll_u8_core", "ksw_ll_i16_core",
+                     "ksw_ll_i16"):
+        assert ref_name in names
+
+
+def test_library_exports_every_declared_symbol(built):
+    from minibwa_gb300.lib import lib_path
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path()], capture_output=True, text=True, check=True)
+    exported = {ln.split()[-1] for ln in out.stdout.splitlines() if " T " in ln}
+    missing = [n for n in _declared_functions() if n not in exported]
+    assert not missing, missing
+    L = C.CDLL(lib_path())
+    for n in _declared_functions():
+        getattr(L, n)
+
+
+def test_no_device_gives_error_code_not_crash(built):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from minibwa_gb300.lib import load_library
+    L = load_library()
+    h = C.c_void_p()
+    rc = L.ksw2g_ctx_create(0, C.byref(h))
+    assert rc < 0
+    assert len(L.ksw2g_last_error()) > 0
+
+
+def test_shape_table(built):
+    from minibwa_gb300.lib import load_library
+    L = load_library()
+    n = L.ksw2g_ext_num_shapes()
+    assert n >= 4
+    words = []
+    for s in range(n):
+        g, k = C.c_int(), C.c_int()
+        assert L.ksw2g_ext_shape_info(s, C.byref(g), C.byref(k)) == 0
+        assert g.value in (4, 8, 16, 32) and 1 <= k.value <= 16
+        words.append(g.value * k.value)
+    assert words == sorted(words)
+    assert L.ksw2g_ext_shape_info(n, None, None) < 0
+
+
+def test_synthetic_workloads_are_seeded(built):
+    from minibwa_gb300 import synth
+    a, b = synth.config1(500), synth.config1(500)
+    assert np.array_equal(a.jobs, b.jobs) and np.array_equal(a.qbuf, b.qbuf) and np.array_equal(a.tbuf, b.tbuf)
+    assert a.jobs["qlen"].min() >= 100 and a.jobs["qlen"].max() <= 500
+    assert (a.jobs["qlen"] > 300).sum() > 0  # the 1% junk-suffix pairs
+    r = synth.config3(300)
+    assert r.jobs["qlen"].min() == 150 and 500 <= r.jobs["tlen"].min() and r.jobs["tlen"].max() <= 1000
+    s = a.subset([3, 1, 4])
+    assert np.array_equal(s.query(0), a.query(3)) and np.array_equal(s.target(2), a.target(4))

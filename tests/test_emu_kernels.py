@@ -1,0 +1,76 @@
+"""The device kernels' source, compiled for the host with tests/emu/cuda_emu.h and run
+on the CPU: the exact code paths of the CUDA kernels (window sliding, shuffles, votes,
+lockstep groups, the device work counter, the backtrack) checked against the golden
+vectors and the oracle without a GPU."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import EXT_FIELDS, LL_FIELDS, ROOT, golden_ext_cases, golden_ll_cases
+
+sys.path.insert(0, os.path.join(ROOT, "tests", "emu"))
+
+
+@pytest.fixture(scope="module")
+def emu(built):
+    import emu as E
+    E.lib()
+    return E
+
+
+def test_emulated_kernels_match_golden_extension(emu, golden):
+    cases = list(golden_ext_cases(golden))
+    for i, c in enumerate(cases[::3]):  # 200 of the 600 cases keep the CPU suite short
+        res, cig = emu.ext(c["dual"], c["m"], c["mat"], c["q"], c["e"], c["q2"], c["e2"], [c["query"]], [c["target"]],
+                           c["w"], c["zdrop"], c["end_bonus"], c["flag"])
+        got = {f: int(res[0][f]) for f in EXT_FIELDS}
+        assert got == c["out"], (i, got, c["out"])
+        assert cig[0] == c["cigar"], i
+
+
+def test_emulated_kernels_match_golden_ll(emu, golden):
+    cases = list(golden_ll_cases(golden))
+    for i, c in enumerate(cases[::3]):
+        r = emu.ll(c["size"], c["m"], c["mat"], c["gapo"], c["gape"], [c["query"]], [c["target"]], c["xtra"])[0]
+        assert {f: int(r[f]) for f in LL_FIELDS} == c["out"], (i, c["size"], c["xtra"])
+
+
+def test_emulated_lockstep_groups_and_work_counter(emu):
+    """Several groups per warp take jobs of different lengths from the work counter;
+    each result must still equal the oracle (exercises group divergence)."""
+    from minibwa_gb300 import synth
+    from oracle import oracle as O
+    p = synth.config0(24, seed=3)
+    qs = [p.query(i)[: 40 + 7 * i] for i in range(len(p))]
+    ts = [p.target(i)[: 50 + 5 * i] for i in range(len(p))]
+    for dual, flag in ((0, 0x40), (1, 0xc2), (1, 0x41), (0, 0x08)):
+        q2, e2 = (24, 1) if dual else (12, 2)
+        res, cig = emu.ext(dual, 5, p.mat, 12, 2, q2, e2, qs, ts, 25, 100, 10, flag, threads=32, shape=0)
+        for i in range(len(qs)):
+            exp, _ = O.extz(dual, qs[i], ts[i], 5, p.mat, 12, 2, q2, e2, 25, 100, 10, flag)
+            assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, i)
+            assert cig[i] == exp["cigar"], (dual, flag, i)
+    r = synth.config3_pe(12, seed=4)
+    qs = [r.qbuf[j["qoff"]:j["qoff"] + j["qlen"]] for j in r.jobs]
+    ts = [r.tbuf[j["toff"]:j["toff"] + j["tlen"] // (1 + i % 3)] for i, j in enumerate(r.jobs)]
+    res = emu.ll(1, 5, r.mat, r.gapo, r.gape, qs, ts, int(r.jobs["xtra"][0]), threads=32)
+    for i in range(len(qs)):
+        exp, _ = O.ll(1, qs[i], ts[i], 5, r.mat, r.gapo, r.gape, int(r.jobs["xtra"][0]))
+        assert {f: int(res[i][f]) for f in LL_FIELDS} == exp, i
+
+
+def test_emulated_wide_band_shapes(emu):
+    """Wide bands select the 16- and 32-thread shapes."""
+    from minibwa_gb300 import synth
+    from oracle import oracle as O
+    p = synth.config1(4, seed=9)
+    qs = [p.query(i) for i in range(len(p))]
+    ts = [p.target(i) for i in range(len(p))]
+    for w, shape in ((230, 3), (480, 4), (900, 5)):
+        res, cig = emu.ext(1, 5, p.mat, 12, 2, 24, 1, qs, ts, w, 100, 10, 0x40, shape=shape)
+        for i in range(len(qs)):
+            exp, _ = O.extz(1, qs[i], ts[i], 5, p.mat, 12, 2, 24, 1, w, 100, 10, 0x40)
+            assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (w, i)
+            assert cig[i] == exp["cigar"]
