@@ -67,7 +67,7 @@ void ksw2g_ctx_destroy(ksw2g_ctx_t *ctx);
 void *ksw2g_ctx_stream(ksw2g_ctx_t *ctx);          /* the cudaStream_t all work of ctx runs on */
 int ksw2g_ctx_sync(ksw2g_ctx_t *ctx);
 /* Device bytes a batch may hold for traceback at once (jobs run in waves
- * under this budget).  Default 8 GiB. */
+ * under this budget, longest jobs first).  Default 16 GiB. */
 int ksw2g_ctx_set_tb_budget(ksw2g_ctx_t *ctx, int64_t bytes);
 const char *ksw2g_last_error(void);
 

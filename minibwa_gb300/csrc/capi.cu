@@ -130,7 +130,7 @@ struct ksw2g_ctx {
   int device = 0;
   cudaStream_t st = nullptr;
   int nsm = 0;
-  int64_t tb_budget = (int64_t)8 << 30;
+  int64_t tb_budget = (int64_t)16 << 30;
   DevBuf tb_pool;       // traceback rows of the running wave
   DevBuf one;           // per-call drop-in scratch (device)
   PinBuf one_h;         // per-call drop-in staging (pinned)
@@ -186,8 +186,9 @@ struct Bin {
   int count;
 };
 struct Wave {
-  int j0, j1;            // contiguous job range
+  int w0, w1;            // range of the longest-first job order (batch->sorted)
   int64_t tb_bytes;
+  bool any_cig;
   std::vector<Bin> bins;
 };
 
@@ -196,7 +197,7 @@ struct ksw2g_batch {
   int n = 0;
   ksw2g_ext_params P;
   int ll_m = 0, ll_gapo = 0, ll_gape = 0, ll_size = 1, ll_slen = 0;
-  DevBuf raw, rawmeta, arena, jobs, order, tb_off, res, bts, cigar, counters, llmat, blist, blist_off;
+  DevBuf raw, rawmeta, arena, jobs, order, sorted, tb_off, res, bts, cigar, counters, llmat, blist, blist_off;
   int64_t cigar_cap = 0;
   int n_counters = 0;
   std::vector<Wave> waves;
@@ -206,7 +207,7 @@ struct ksw2g_batch {
 
 extern "C" void ksw2g_batch_free(ksw2g_batch_t *b) {
   if (!b) return;
-  for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->tb_off, &b->res, &b->bts, &b->cigar,
+  for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts, &b->cigar,
                     &b->counters, &b->llmat, &b->blist, &b->blist_off})
     d->release();
   delete b;
@@ -297,24 +298,32 @@ static int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, co
     dj[i] = ksw2g_job{qpad[i], tpad[i], jobs[i].qlen, jobs[i].tlen, jobs[i].w, jobs[i].zdrop, jobs[i].end_bonus,
                       jobs[i].flag};
   }
-  // waves under the traceback budget; bins by (mode, shape) inside each wave
+  // Longest jobs first: the persistent kernels then finish with short jobs and
+  // the waves (traceback budget) are cut from that order, so no wave waits on
+  // one long pair.  Bins by (mode, shape) inside each wave.
+  std::vector<int32_t> srt(n);
+  for (int i = 0; i < n; ++i) srt[i] = i;
+  std::stable_sort(srt.begin(), srt.end(), [&](int a, int b) {
+    return (int64_t)ql[a] + tl[a] > (int64_t)ql[b] + tl[b];
+  });
   b->waves.clear();
   std::vector<int64_t> tbo(n);
   std::vector<int32_t> ord(n);
   int64_t ordp = 0;
   for (int i = 0; i < n;) {
     Wave wv;
-    wv.j0 = i;
+    wv.w0 = i;
+    wv.any_cig = false;
     int64_t acc = 0;
-    while (i < n && (acc + foot[i] <= c->tb_budget || i == wv.j0)) tbo[i] = acc, acc += foot[i], ++i;
-    wv.j1 = i;
+    while (i < n && (acc + foot[srt[i]] <= c->tb_budget || i == wv.w0)) tbo[srt[i]] = acc, acc += foot[srt[i]], ++i;
+    wv.w1 = i;
     wv.tb_bytes = acc;
     for (int md = 0; md < 3; ++md)
-      for (int s = 0; s < kNumExtShapes; ++s) {
-        Bin bn{md, s, ordp, 0};
-        for (int j = wv.j0; j < wv.j1; ++j)
-          if (mode[j] == md && shape[j] == s) ord[ordp++] = j - wv.j0, bn.count++;
-        if (bn.count) wv.bins.push_back(bn);
+      for (int sh = 0; sh < kNumExtShapes; ++sh) {
+        Bin bn{md, sh, ordp, 0};
+        for (int k = wv.w0; k < wv.w1; ++k)
+          if (mode[srt[k]] == md && shape[srt[k]] == sh) ord[ordp++] = srt[k], bn.count++;
+        if (bn.count) wv.bins.push_back(bn), wv.any_cig |= md != 0;
       }
     b->waves.push_back(wv);
   }
@@ -322,6 +331,7 @@ static int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, co
   for (auto &wv : b->waves) b->n_counters += (int)wv.bins.size();
   if ((rc = b->jobs.ensure(sizeof(ksw2g_job) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->order.ensure(sizeof(int32_t) * (size_t)std::max(n, 1)))) return rc;
+  if ((rc = b->sorted.ensure(sizeof(int32_t) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->tb_off.ensure(sizeof(int64_t) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->res.ensure(sizeof(ksw2g_ext_result) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->bts.ensure(sizeof(ksw2g_bt) * (size_t)std::max(n, 1)))) return rc;
@@ -331,6 +341,7 @@ static int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, co
   if (n) {
     CK(cudaMemcpyAsync(b->jobs.p, dj.data(), sizeof(ksw2g_job) * n, cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(b->order.p, ord.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(b->sorted.p, srt.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(b->tb_off.p, tbo.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->st));
   }
   CK(cudaStreamSynchronize(c->st));
@@ -369,18 +380,17 @@ static int ext_run(ksw2g_ctx *c, ksw2g_batch *b) {
   ksw2g_bt *db = b->bts.as<ksw2g_bt>();
   const int64_t *dto = b->tb_off.as<int64_t>();
   const int32_t *dord = b->order.as<int32_t>();
+  const int32_t *dsrt = b->sorted.as<int32_t>();
   int ci = 0;
   for (auto &wv : b->waves) {
     for (auto &bn : wv.bins) {
-      ExtLaunch L{dj + wv.j0, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr + wv.j0, db + wv.j0,
-                  c->tb_pool.as<uint8_t>(), dto + wv.j0, jc + ci++};
+      ExtLaunch L{dj, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr, db, c->tb_pool.as<uint8_t>(), dto,
+                  jc + ci++};
       CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, c->st));
       ++b->launches;
     }
-    bool any_cig = false;
-    for (auto &bn : wv.bins) any_cig |= bn.mode != 0;
-    if (any_cig) {
-      CK(launch_ext_bt(dj + wv.j0, wv.j1 - wv.j0, db + wv.j0, c->tb_pool.as<uint8_t>(), dto + wv.j0, dr + wv.j0,
+    if (wv.any_cig) {
+      CK(launch_ext_bt(dj, dsrt + wv.w0, wv.w1 - wv.w0, db, c->tb_pool.as<uint8_t>(), dto, dr,
                        b->cigar.as<uint32_t>(), cursor, (long long)b->cigar_cap, err, c->st));
       ++b->launches;
     }
@@ -546,7 +556,7 @@ static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen
               (ksw2g_bt *)(d + o_bt), d + o_tb, (const int64_t *)(d + o_tbo), (int *)(d + 16)};
   DIE_ON(launch_ext_dp(dual, mode, shape, P, L, 1, c->st));
   if (mode)
-    DIE_ON(launch_ext_bt((const ksw2g_job *)(d + o_job), 1, (const ksw2g_bt *)(d + o_bt), d + o_tb,
+    DIE_ON(launch_ext_bt((const ksw2g_job *)(d + o_job), nullptr, 1, (const ksw2g_bt *)(d + o_bt), d + o_tb,
                          (const int64_t *)(d + o_tbo), (ksw2g_ext_result *)(d + o_res), (uint32_t *)(d + o_cig),
                          (unsigned long long *)d, (long long)ncig, (int *)(d + 8), c->st));
   DIE_ON(cudaMemcpyAsync(h + o_res, d + o_res, 64 + ncig * 4, cudaMemcpyDeviceToHost, c->st));

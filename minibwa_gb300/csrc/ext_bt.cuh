@@ -50,12 +50,15 @@ __device__ int bt_walk(const uint8_t *__restrict__ tb, int ncol16, int qlen, int
   return n;
 }
 
-__global__ void ext_bt_kernel(const ksw2g_job *__restrict__ jobs, int n_jobs, const ksw2g_bt *__restrict__ bts,
-                              const uint8_t *__restrict__ tb_pool, const int64_t *__restrict__ tb_off,
-                              ksw2g_ext_result *__restrict__ res, uint32_t *__restrict__ cigar_out,
-                              unsigned long long *__restrict__ cursor, long long cigar_cap, int *__restrict__ err) {
-  const int jid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jid >= n_jobs) return;
+// One thread per job; jobs order[0..n_jobs) (all jobs when order is null).
+__global__ void ext_bt_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ order, int n_jobs,
+                              const ksw2g_bt *__restrict__ bts, const uint8_t *__restrict__ tb_pool,
+                              const int64_t *__restrict__ tb_off, ksw2g_ext_result *__restrict__ res,
+                              uint32_t *__restrict__ cigar_out, unsigned long long *__restrict__ cursor,
+                              long long cigar_cap, int *__restrict__ err) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix >= n_jobs) return;
+  const int jid = order ? order[ix] : ix;
   const ksw2g_bt b = bts[jid];
   if (b.i0 < 0) {
     res[jid].n_cigar = 0;

@@ -94,7 +94,7 @@ int emu_ext(int dual, int mode, int shape, const ksw2g_ext_params *P, int n, con
     for (int j = 0; j < n; ++j) {
       threadIdx.x = 0;
       blockIdx.x = j;
-      ext_bt_kernel(jobs, n, bts, tb_pool, tb_off, res, cigar, &cursor, cap, &err);
+      ext_bt_kernel(jobs, nullptr, n, bts, tb_pool, tb_off, res, cigar, &cursor, cap, &err);
     }
     if (err) return -2;
   }
