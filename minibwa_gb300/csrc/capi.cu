@@ -75,6 +75,7 @@ static int set_err(int code, const char *fmt, ...) {
 
 extern "C" const char *ksw2g_last_error(void) { return tl_err.c_str(); }
 
+
 // ---------------------------------------------------------------- buffers
 struct DevBuf {
   void *p = nullptr;
