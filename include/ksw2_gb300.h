@@ -105,6 +105,40 @@ int ksw2g_ext_num_shapes(void);
 int ksw2g_ext_shape_info(int shape, int *group_threads, int *words_per_thread);
 int ksw2g_ext_set_shape(int dual, int mode, int ncol_lo, int ncol_hi, int shape);
 
+/*
+ * Extension batch that allocates nothing (no counterpart in the reference).
+ *
+ * For callers that cannot let a library call cudaMalloc: a framework that owns
+ * all device memory through its own caching allocator, or a serving loop that
+ * cannot take the device-wide synchronisation of cudaMalloc/cudaFree.  It runs
+ * the same DP and backtrack kernels as ksw2g_ext_batch; all scratch (job table
+ * copy, traceback offsets and rows, work counters) lives in one fixed static
+ * device array of KSW2G_NOALLOC_SCRATCH_BYTES that every GPU loading this part
+ * of the library keeps until the process exits.
+ *
+ *  jobs     host array; qoff/toff index d_arena, which must use the padded
+ *           layout: every sequence starts 16-byte aligned with at least 32 zero
+ *           bytes before it and zeros after it up to the next 16-byte boundary
+ *           plus 32 bytes.  All jobs of one call use the same gap mode
+ *           (score-only, left-aligned or right-aligned CIGAR).
+ *  d_res    device array of n_jobs results (as ksw2g_ext_batch fills them).
+ *  d_cigar  device array of cigar_cap words; cigar_cap must be at least the sum
+ *           of qlen+tlen+1 over the jobs when CIGARs are requested.
+ *  stream   cudaStream_t the work is enqueued on; the call returns before it ends.
+ *
+ * Rejects (KSW2G_E_CAPACITY, message in ksw2g_last_error()) any call whose
+ * scratch (traceback rows, plus 64 bytes per job and at most 1 KiB) exceeds
+ * KSW2G_NOALLOC_SCRATCH_BYTES.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Every call reuses the same array and clears its counters at the start:
+ * calls whose work overlaps on the GPU (different streams, or another host
+ * thread) race on it and must be serialised by the caller.
+ */
+#define KSW2G_NOALLOC_SCRATCH_BYTES (64ll << 20)
+int ksw2g_ext_noalloc(int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e, int8_t q2, int8_t e2,
+					  int n_jobs, const ksw2g_job_t *jobs, const uint8_t *d_arena,
+					  ksw2g_ext_result_t *d_res, uint32_t *d_cigar, int64_t cigar_cap, void *stream);
+
 /* Measured 32-bit integer instruction throughput of the device (lane-ops per
  * second), the denominator of the DP kernels' integer-pipe roofline. */
 int ksw2g_probe_int32_peak(int device, double *ops_per_s);

@@ -52,6 +52,7 @@ def build(verbose=False, force=False):
         ("ll_kernels.cu", "ll.o", []),
         ("capi.cu", "capi.o", []),
         ("probe.cu", "probe.o", []),
+        ("noalloc.cu", "noalloc.o", []),
     ]
     hdrs = _headers()
     procs, objs = [], []

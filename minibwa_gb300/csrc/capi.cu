@@ -74,7 +74,9 @@ static int set_err(int code, const char *fmt, ...) {
   } while (0)
 
 extern "C" const char *ksw2g_last_error(void) { return tl_err.c_str(); }
-
+namespace ksw2g {
+int report_error(int code, const char *msg) { return set_err(code, "%s", msg); }
+}  // namespace ksw2g
 
 // ---------------------------------------------------------------- buffers
 struct DevBuf {
