@@ -1,0 +1,117 @@
+// batch.h -- internal host-side structures of libksw2gpu.so (contexts, device
+// buffers, prepared batches), shared by the C ABI (capi.cu) and the serving
+// engine (server.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/ksw2_gb300.h"
+#include "ksw2g.h"
+
+namespace ksw2g {
+int report_error(int code, const char *msg);
+}
+
+// ---------------------------------------------------------------- buffers
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t n) {
+    if (n <= cap) return 0;
+    if (p) cudaFree(p);
+    p = nullptr, cap = 0;
+    size_t c = n < 4096 ? 4096 : n + n / 8;
+    if (cudaMalloc(&p, c) != cudaSuccess) {
+      cudaGetLastError();
+      if (cudaMalloc(&p, n) != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        return ksw2g::report_error(KSW2G_E_NOMEM, "cudaMalloc failed");
+      }
+      c = n;
+    }
+    cap = c;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr, cap = 0;
+  }
+  template <typename T>
+  T *as() const { return (T *)p; }
+};
+struct PinBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t n) {
+    if (n <= cap) return 0;
+    if (p) cudaFreeHost(p);
+    p = nullptr, cap = 0;
+    size_t c = n < 4096 ? 4096 : n + n / 8;
+    if (cudaMallocHost(&p, c) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return ksw2g::report_error(KSW2G_E_NOMEM, "cudaMallocHost failed");
+    }
+    cap = c;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr, cap = 0;
+  }
+};
+
+// ---------------------------------------------------------------- context
+struct ksw2g_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int nsm = 0;
+  int64_t tb_budget = (int64_t)16 << 30;
+  DevBuf tb_pool;       // traceback rows of the running wave
+  DevBuf one;           // per-call drop-in scratch (device)
+  PinBuf one_h;         // per-call drop-in staging (pinned)
+  ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
+};
+
+// ---------------------------------------------------------------- batches
+struct Bin {
+  int mode, shape;
+  int64_t order_off;
+  int count;
+};
+struct Wave {
+  int w0, w1;            // range of the longest-first job order (batch->sorted)
+  int64_t tb_bytes;
+  bool any_cig;
+  std::vector<Bin> bins;
+};
+
+struct ksw2g_batch {
+  int kind = 0;          // 0 extz2, 1 extd2, 2 ll u8, 3 ll i16
+  int n = 0;
+  ksw2g_ext_params P;
+  int ll_m = 0, ll_gapo = 0, ll_gape = 0, ll_size = 1, ll_slen = 0, ll_qlen_max = 0, ll_mat_max = 0, ll_force = 0;
+  DevBuf raw, rawmeta, arena, jobs, order, sorted, tb_off, res, bts, cigar, counters, llmat, blist, blist_off;
+  int64_t cigar_cap = 0;
+  int n_counters = 0;
+  std::vector<Wave> waves;
+  int launches = 0;
+  int64_t total_cells_hint = 0;
+};
+
+
+// Upload + pack the sequences and build the device job table and the wave plan
+// (synchronous on c->st, so the host buffers may be reused on return).
+int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+                     int8_t q2, int8_t e2, int n, const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+                     const uint8_t *tbuf, int64_t tbuf_len);
+int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape, int n,
+                    const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+                    int64_t tbuf_len);
+// Enqueue the DP (+ backtrack) of a prepared extension batch on st, with tb (tb_cap bytes)
+// holding the traceback rows of one wave at a time.
+int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap);
+int ll_run_on(ksw2g_batch *b, cudaStream_t st);

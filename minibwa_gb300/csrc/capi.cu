@@ -15,6 +15,7 @@
 #include "ksw2g.h"
 #include "launch.h"
 #include "host_common.h"
+#include "batch.h"
 
 static_assert(sizeof(ksw2g_job_t) == sizeof(ksw2g_job), "job layout");
 static_assert(sizeof(ksw2g_ext_result_t) == sizeof(ksw2g_ext_result), "result layout");
@@ -78,68 +79,6 @@ namespace ksw2g {
 int report_error(int code, const char *msg) { return set_err(code, "%s", msg); }
 }  // namespace ksw2g
 
-// ---------------------------------------------------------------- buffers
-struct DevBuf {
-  void *p = nullptr;
-  size_t cap = 0;
-  int ensure(size_t n) {
-    if (n <= cap) return 0;
-    if (p) cudaFree(p);
-    p = nullptr, cap = 0;
-    size_t c = n < 4096 ? 4096 : n + n / 8;
-    if (cudaMalloc(&p, c) != cudaSuccess) {
-      cudaGetLastError();
-      if (cudaMalloc(&p, n) != cudaSuccess) {
-        cudaGetLastError();
-        p = nullptr;
-        return set_err(KSW2G_E_NOMEM, "cudaMalloc(%zu) failed", n);
-      }
-      c = n;
-    }
-    cap = c;
-    return 0;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr, cap = 0;
-  }
-  template <typename T>
-  T *as() const { return (T *)p; }
-};
-struct PinBuf {
-  void *p = nullptr;
-  size_t cap = 0;
-  int ensure(size_t n) {
-    if (n <= cap) return 0;
-    if (p) cudaFreeHost(p);
-    p = nullptr, cap = 0;
-    size_t c = n < 4096 ? 4096 : n + n / 8;
-    if (cudaMallocHost(&p, c) != cudaSuccess) {
-      cudaGetLastError();
-      p = nullptr;
-      return set_err(KSW2G_E_NOMEM, "cudaMallocHost(%zu) failed", c);
-    }
-    cap = c;
-    return 0;
-  }
-  void release() {
-    if (p) cudaFreeHost(p);
-    p = nullptr, cap = 0;
-  }
-};
-
-// ---------------------------------------------------------------- context
-struct ksw2g_ctx {
-  int device = 0;
-  cudaStream_t st = nullptr;
-  int nsm = 0;
-  int64_t tb_budget = (int64_t)16 << 30;
-  DevBuf tb_pool;       // traceback rows of the running wave
-  DevBuf one;           // per-call drop-in scratch (device)
-  PinBuf one_h;         // per-call drop-in staging (pinned)
-  ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
-};
-
 extern "C" int ksw2g_ctx_create(int device, ksw2g_ctx_t **out) {
   if (!out) return set_err(KSW2G_E_ARG, "null output");
   int ndev = 0;
@@ -182,32 +121,6 @@ extern "C" int ksw2g_ctx_set_tb_budget(ksw2g_ctx_t *c, int64_t bytes) {
   return 0;
 }
 
-// ---------------------------------------------------------------- batches
-struct Bin {
-  int mode, shape;
-  int64_t order_off;
-  int count;
-};
-struct Wave {
-  int w0, w1;            // range of the longest-first job order (batch->sorted)
-  int64_t tb_bytes;
-  bool any_cig;
-  std::vector<Bin> bins;
-};
-
-struct ksw2g_batch {
-  int kind = 0;          // 0 extz2, 1 extd2, 2 ll u8, 3 ll i16
-  int n = 0;
-  ksw2g_ext_params P;
-  int ll_m = 0, ll_gapo = 0, ll_gape = 0, ll_size = 1, ll_slen = 0;
-  DevBuf raw, rawmeta, arena, jobs, order, sorted, tb_off, res, bts, cigar, counters, llmat, blist, blist_off;
-  int64_t cigar_cap = 0;
-  int n_counters = 0;
-  std::vector<Wave> waves;
-  int launches = 0;
-  int64_t total_cells_hint = 0;
-};
-
 extern "C" void ksw2g_batch_free(ksw2g_batch_t *b) {
   if (!b) return;
   for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts, &b->cigar,
@@ -219,7 +132,7 @@ extern "C" int ksw2g_batch_launches(const ksw2g_batch_t *b) { return b ? b->laun
 
 // Upload raw sequences and pack them into the padded arena.  Writes the padded
 // offsets of query s and target s to qpad[s], tpad[s].
-static int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, const int32_t *qlen,
+int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, const int32_t *qlen,
                            const int64_t *toff, const int32_t *tlen, const uint8_t *qbuf, int64_t qbuf_len,
                            const uint8_t *tbuf, int64_t tbuf_len, std::vector<int64_t> &qpad,
                            std::vector<int64_t> &tpad) {
@@ -257,7 +170,7 @@ static int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *q
   return 0;
 }
 
-static int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
                             int8_t q2, int8_t e2, int n, const ksw2g_job_t *jobs, const uint8_t *qbuf,
                             int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len) {
   if (n < 0 || (n > 0 && !jobs) || !mat) return set_err(KSW2G_E_ARG, "bad batch arguments");
@@ -304,15 +217,23 @@ static int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, co
   // Longest jobs first: the persistent kernels then finish with short jobs and
   // the waves (traceback budget) are cut from that order, so no wave waits on
   // one long pair.  Bins by (mode, shape) inside each wave.
+  // counting sort by qlen+tlen, longest first (stable)
   std::vector<int32_t> srt(n);
-  for (int i = 0; i < n; ++i) srt[i] = i;
-  std::stable_sort(srt.begin(), srt.end(), [&](int a, int b) {
-    return (int64_t)ql[a] + tl[a] > (int64_t)ql[b] + tl[b];
-  });
+  {
+    int64_t maxkey = 0;
+    for (int i = 0; i < n; ++i) maxkey = std::max<int64_t>(maxkey, (int64_t)ql[i] + tl[i]);
+    std::vector<int32_t> cnt((size_t)maxkey + 2, 0);
+    for (int i = 0; i < n; ++i) ++cnt[(size_t)(maxkey - ((int64_t)ql[i] + tl[i]))];
+    int32_t acc = 0;
+    for (auto &c : cnt) { const int32_t t = c; c = acc; acc += t; }
+    for (int i = 0; i < n; ++i) srt[cnt[(size_t)(maxkey - ((int64_t)ql[i] + tl[i]))]++] = i;
+  }
   b->waves.clear();
   std::vector<int64_t> tbo(n);
   std::vector<int32_t> ord(n);
   int64_t ordp = 0;
+  const int nbins = 3 * kNumExtShapes;
+  std::vector<int32_t> bcount(nbins), bpos(nbins);
   for (int i = 0; i < n;) {
     Wave wv;
     wv.w0 = i;
@@ -321,13 +242,17 @@ static int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, co
     while (i < n && (acc + foot[srt[i]] <= c->tb_budget || i == wv.w0)) tbo[srt[i]] = acc, acc += foot[srt[i]], ++i;
     wv.w1 = i;
     wv.tb_bytes = acc;
-    for (int md = 0; md < 3; ++md)
-      for (int sh = 0; sh < kNumExtShapes; ++sh) {
-        Bin bn{md, sh, ordp, 0};
-        for (int k = wv.w0; k < wv.w1; ++k)
-          if (mode[srt[k]] == md && shape[srt[k]] == sh) ord[ordp++] = srt[k], bn.count++;
-        if (bn.count) wv.bins.push_back(bn), wv.any_cig |= md != 0;
+    std::fill(bcount.begin(), bcount.end(), 0);
+    for (int k = wv.w0; k < wv.w1; ++k) ++bcount[mode[srt[k]] * kNumExtShapes + shape[srt[k]]];
+    for (int bi = 0; bi < nbins; ++bi) {
+      bpos[bi] = (int32_t)ordp;
+      if (bcount[bi]) {
+        wv.bins.push_back(Bin{bi / kNumExtShapes, bi % kNumExtShapes, ordp, bcount[bi]});
+        wv.any_cig |= bi / kNumExtShapes != 0;
       }
+      ordp += bcount[bi];
+    }
+    for (int k = wv.w0; k < wv.w1; ++k) ord[bpos[mode[srt[k]] * kNumExtShapes + shape[srt[k]]]++] = srt[k];
     b->waves.push_back(wv);
   }
   b->n_counters = 0;
@@ -365,19 +290,16 @@ extern "C" int ksw2g_ext_prepare(ksw2g_ctx_t *c, int dual, int8_t m, const int8_
   return 0;
 }
 
-static int ext_run(ksw2g_ctx *c, ksw2g_batch *b) {
-  CK(cudaSetDevice(c->device));
+int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap) {
   b->launches = 0;
   if (b->n == 0) return 0;
-  int64_t maxtb = 0;
-  for (auto &wv : b->waves) maxtb = std::max(maxtb, wv.tb_bytes);
-  int rc;
-  if ((rc = c->tb_pool.ensure((size_t)std::max<int64_t>(maxtb, 16)))) return rc;
+  for (auto &wv : b->waves)
+    if (wv.tb_bytes > tb_cap) return set_err(KSW2G_E_CAPACITY, "traceback wave exceeds the pool");
   int *cnt = b->counters.as<int>();
   unsigned long long *cursor = (unsigned long long *)cnt;  // bytes 0..7
   int *err = cnt + 2;                                      // bytes 8..11
   int *jc = cnt + 4;                                       // per-bin job counters
-  CK(cudaMemsetAsync(b->counters.p, 0, 16 + sizeof(int) * (size_t)b->n_counters, c->st));
+  CK(cudaMemsetAsync(b->counters.p, 0, 16 + sizeof(int) * (size_t)b->n_counters, st));
   const ksw2g_job *dj = b->jobs.as<ksw2g_job>();
   ksw2g_ext_result *dr = b->res.as<ksw2g_ext_result>();
   ksw2g_bt *db = b->bts.as<ksw2g_bt>();
@@ -387,18 +309,27 @@ static int ext_run(ksw2g_ctx *c, ksw2g_batch *b) {
   int ci = 0;
   for (auto &wv : b->waves) {
     for (auto &bn : wv.bins) {
-      ExtLaunch L{dj, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr, db, c->tb_pool.as<uint8_t>(), dto,
+      ExtLaunch L{dj, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr, db, tb, dto,
                   jc + ci++};
-      CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, c->st));
+      CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, st));
       ++b->launches;
     }
     if (wv.any_cig) {
-      CK(launch_ext_bt(dj, dsrt + wv.w0, wv.w1 - wv.w0, db, c->tb_pool.as<uint8_t>(), dto, dr,
-                       b->cigar.as<uint32_t>(), cursor, (long long)b->cigar_cap, err, c->st));
+      CK(launch_ext_bt(dj, dsrt + wv.w0, wv.w1 - wv.w0, db, tb, dto, dr,
+                       b->cigar.as<uint32_t>(), cursor, (long long)b->cigar_cap, err, st));
       ++b->launches;
     }
   }
   return 0;
+}
+
+static int ext_run(ksw2g_ctx *c, ksw2g_batch *b) {
+  CK(cudaSetDevice(c->device));
+  int64_t maxtb = 0;
+  for (auto &wv : b->waves) maxtb = std::max(maxtb, wv.tb_bytes);
+  int rc;
+  if ((rc = c->tb_pool.ensure((size_t)std::max<int64_t>(maxtb, 16)))) return rc;
+  return ext_run_on(b, c->st, c->tb_pool.as<uint8_t>(), (int64_t)c->tb_pool.cap);
 }
 
 extern "C" int ksw2g_batch_run(ksw2g_ctx_t *c, ksw2g_batch_t *b) {
@@ -595,7 +526,7 @@ extern "C" void ksw_extd2_sse(void *km, int qlen, const uint8_t *query, int tlen
 }
 
 // ================================================================ ksw_ll
-static int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape,
+int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape,
                            int n, const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
                            const uint8_t *tbuf, int64_t tbuf_len) {
   if (n < 0 || (n > 0 && !jobs) || !mat || m <= 0 || m > 64) return set_err(KSW2G_E_ARG, "bad ll batch arguments");
@@ -623,6 +554,10 @@ static int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const 
   if (slen > ll_slen_cap(size))
     return set_err(KSW2G_E_BAND, "ll query of %d segments exceeds the kernel's %d", slen, ll_slen_cap(size));
   b->ll_slen = slen;
+  b->ll_qlen_max = 0;
+  for (int i = 0; i < n; ++i) b->ll_qlen_max = std::max(b->ll_qlen_max, (int)jobs[i].qlen);
+  b->ll_mat_max = mat[0];
+  for (int a = 1; a < m * m; ++a) b->ll_mat_max = std::max(b->ll_mat_max, (int)mat[a]);
   std::vector<int64_t> qpad, tpad;
   int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), qbuf, qbuf_len, tbuf, tbuf_len, qpad,
                            tpad);
@@ -644,17 +579,25 @@ static int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const 
   return 0;
 }
 
-int ll_run(ksw2g_ctx *c, ksw2g_batch *b) {
-  CK(cudaSetDevice(c->device));
+int ll_run_on(ksw2g_batch *b, cudaStream_t st) {
+  {
+    const char *f = getenv("KSW2G_LL_KERNEL");  // "lane" or "dpx": pin one kernel family (tests)
+    b->ll_force = f ? (strcmp(f, "lane") == 0 ? 1 : strcmp(f, "dpx") == 0 ? 2 : 0) : 0;
+  }
   b->launches = 0;
   if (b->n == 0) return 0;
-  CK(cudaMemsetAsync(b->counters.p, 0, 16, c->st));
+  CK(cudaMemsetAsync(b->counters.p, 0, 16, st));
   LLLaunch L{b->jobs.as<ksw2g_ll_job>(), b->n, b->arena.as<uint8_t>(), b->llmat.as<int8_t>(), b->ll_m, b->ll_gapo,
              b->ll_gape, b->res.as<ksw2g_ll_result>(), b->blist.as<uint64_t>(), b->blist_off.as<int64_t>(),
-             b->counters.as<int>()};
-  CK(launch_ll(b->ll_size, b->ll_slen, L, 0, c->st));
+             b->counters.as<int>(), b->ll_qlen_max, b->ll_mat_max};
+  CK(launch_ll(b->ll_size, b->ll_slen, L, 0, st, b->ll_force));
   ++b->launches;
   return 0;
+}
+
+int ll_run(ksw2g_ctx *c, ksw2g_batch *b) {
+  CK(cudaSetDevice(c->device));
+  return ll_run_on(b, c->st);
 }
 
 extern "C" int ksw2g_ll_prepare(ksw2g_ctx_t *c, int size, int m, const int8_t *mat, int gapo, int gape, int n_jobs,
@@ -744,8 +687,11 @@ static ksw_llrst_t ll_one(void *q_, int tlen, const uint8_t *target, int gapo, i
   if (qlen) memcpy(hb + o_arena + J.qoff, (uint8_t *)(h + 1) + m * m, qlen);
   if (tlen) memcpy(hb + o_arena + J.toff, target, tlen);
   DIE_ON(cudaMemcpyAsync(d, hb, o_arena + arena_bytes, cudaMemcpyHostToDevice, c->st));
+  int mat_max = m > 0 ? ((const int8_t *)(h + 1))[0] : 0;
+  for (int a = 1; a < m * m; ++a) mat_max = std::max(mat_max, (int)((const int8_t *)(h + 1))[a]);
   LLLaunch L{(const ksw2g_ll_job *)(d + o_job), 1, d + o_arena, (const int8_t *)(d + o_mat), m, gapo, gape,
-             (ksw2g_ll_result *)(d + o_res), (uint64_t *)(d + o_bl), (const int64_t *)(d + o_blo), (int *)d};
+             (ksw2g_ll_result *)(d + o_res), (uint64_t *)(d + o_bl), (const int64_t *)(d + o_blo), (int *)d, qlen,
+             mat_max};
   DIE_ON(launch_ll(size, slen < 1 ? 1 : slen, L, 1, c->st));
   DIE_ON(cudaMemcpyAsync(hb + o_res, d + o_res, sizeof(ksw2g_ll_result), cudaMemcpyDeviceToHost, c->st));
   DIE_ON(cudaStreamSynchronize(c->st));

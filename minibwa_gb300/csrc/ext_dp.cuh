@@ -10,9 +10,17 @@
 // reference's first padded 16-byte block of the current anti-diagonal
 // (st_ in ksw2_extz2_sse.c:140), which moves right by at most one block per
 // anti-diagonal; when it moves, all state shifts down by four words.  W is at
-// least 4*(n_col_+1) words: the n_col_ blocks the reference computes per
-// anti-diagonal (ksw2_extz2_sse.c:68,141) plus one block that receives the
-// 16-byte score stores running past en0 (ksw2_extz2_sse.c:118-132).
+// least 4*n_col_ words, the n_col_ blocks the reference computes per
+// anti-diagonal (ksw2_extz2_sse.c:68,141).  One more slot of G words holds only
+// the substitution scores, for the 16-byte score stores that run past en0
+// into the next block (ksw2_extz2_sse.c:118-132).
+//
+// Per anti-diagonal each thread first exchanges, in one packed shuffle per
+// slot, the last bytes of its x, v (and x2) words with its neighbour, then
+// computes all its slots back to back (independent chains).  Words past the
+// band's last padded block are computed too but never read; a block that
+// enters the band is reset to the reference's initial state first.  The maximum and
+// its tie-break use single-instruction warp reductions.
 //
 // Every cell operation reproduces the reference's byte-lane semantics
 // (swar.cuh), including the cells of the 16-byte padding outside the nominal
@@ -73,7 +81,7 @@ __device__ __forceinline__ uint32_t ld_tw(const uint8_t *tp, int p, int tlen) {
 // VAR: 0 = extz2 (affine), 1 = extd2 (dual affine)
 // MODE: 0 = score only, 1 = left-aligned gaps with traceback, 2 = right-aligned gaps with traceback
 template <int VAR, int MODE, int G, int K>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, (K <= 4 ? 4 : (K <= 5 ? 3 : 2)))
 ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ order, int n_jobs,
               const uint8_t *__restrict__ arena, const ksw2g_ext_params P, ksw2g_ext_result *__restrict__ res,
               ksw2g_bt *__restrict__ bts, uint8_t *__restrict__ tb_pool, const int64_t *__restrict__ tb_off,
@@ -99,12 +107,12 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
   const int ez_e = D2 ? P.e2 : P.e;
 
   // per-slot state
-  uint32_t U[K], V[K], X[K], Y[K], X2[K], Y2[K], S[K], TW[K];
+  uint32_t U[K], V[K], X[K], Y[K], X2[K], Y2[K], S[K + 1], TW[K + 1];
   int32_t H0[K], H1[K], H2[K], H3[K];
 
   // per-group state (identical in every thread of the group)
   int jid = -1, qlen = 0, tlen = 0, w = 0, zdrop = 0, end_bonus = 0, flag = 0;
-  int r = 0, wb = 0, ncol16 = 0, n_diag = 0;
+  int r = 0, wb = 0, top = 0, ncol16 = 0, n_diag = 0;
   int64_t cells = 0;
   const uint8_t *qp = nullptr, *tp = nullptr;
   uint8_t *tb = nullptr;
@@ -149,15 +157,15 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         }
         qp = arena + J.qoff, tp = arena + J.toff;
         if (CIG) tb = tb_pool + tb_off[jid];
-        r = 0, wb = 0, H_left = KSW2G_NEG_INF, last_max_H = 0, Hz = 0, last_H0_t = 0;
+        r = 0, wb = 0, top = 0, H_left = KSW2G_NEG_INF, last_max_H = 0, Hz = 0, last_H0_t = 0;
 #pragma unroll
         for (int i = 0; i < K; ++i) {
           U[i] = V[i] = X[i] = Y[i] = init4;
           X2[i] = Y2[i] = init24;
-          S[i] = s_init4;
           H0[i] = H1[i] = H2[i] = H3[i] = KSW2G_NEG_INF;
-          TW[i] = ld_tw(tp, 4 * (k + G * i), tlen);
         }
+#pragma unroll
+        for (int i = 0; i <= K; ++i) S[i] = s_init4, TW[i] = ld_tw(tp, 4 * (k + G * i), tlen);
       }
     }
     if (__all_sync(0xffffffffu, !active)) break;
@@ -194,14 +202,14 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             shift4<G, K>(X2, init24, k, gm);
             shift4<G, K>(Y2, init24, k, gm);
           }
-          shift4<G, K>(S, s_init4, k, gm);
-          shift4<G, K>(TW, 0u, k, gm);
+          shift4<G, K + 1>(S, s_init4, k, gm);
+          shift4<G, K + 1>(TW, 0u, k, gm);
           shift4<G, K>(H0, (int32_t)KSW2G_NEG_INF, k, gm);
           shift4<G, K>(H1, (int32_t)KSW2G_NEG_INF, k, gm);
           shift4<G, K>(H2, (int32_t)KSW2G_NEG_INF, k, gm);
           shift4<G, K>(H3, (int32_t)KSW2G_NEG_INF, k, gm);
           wb = stb;
-          if (k >= G - 4) TW[K - 1] = ld_tw(tp, (wb << 4) + 4 * (k + G * (K - 1)), tlen);
+          if (k >= G - 4) TW[K] = ld_tw(tp, (wb << 4) + 4 * (k + G * K), tlen);
           x1 = xr, v1 = vr, x21 = x2r;  // (r-1, st-1) was computed on the last anti-diagonal
         } else {
           x1 = initb, v1 = initb, x21 = init2b;
@@ -214,6 +222,19 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         if (stb == 0) x1 = initb, x21 = init2b, v1 = vb;  // ksw2_extz2_sse.c:114, ksw2_extd2_sse.c:148-151
         const int base = wb << 4;
         const int en = (enb << 4) + 15;
+        if (enb > top) {
+          // A 16-byte block enters the band (at most one per anti-diagonal).  Words past
+          // the last live block are computed every anti-diagonal but never read, so the
+          // entering block gets the state the reference's untouched memory holds.
+          top = enb;
+          const int wtop = (enb - wb) << 2;
+#pragma unroll
+          for (int i = 0; i < K; ++i)
+            if (((k + G * i) & ~3) == wtop) {
+              U[i] = V[i] = X[i] = Y[i] = init4;
+              if (D2) X2[i] = Y2[i] = init24;
+            }
+        }
         if (en >= r) {  // top row boundary (ksw2_extz2_sse.c:115, ksw2_extd2_sse.c:152-155)
           const int pr = r - base, wr = pr >> 2, sh = (pr & 3) * 8;
           const uint32_t keep = ~(0xffu << sh);
@@ -232,7 +253,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           const int o = (r + 1) & 3;
           const uint32_t qsel = (uint32_t)((o + 3) | ((o + 2) << 4) | ((o + 1) << 8) | (o << 12));
 #pragma unroll
-          for (int i = 0; i < K; ++i) {
+          for (int i = 0; i <= K; ++i) {
             const int p0 = base + 4 * (k + G * i);
             if (p0 + 3 >= st0 && p0 <= fend) {
               const int idx0 = r - p0 - 3;
@@ -268,121 +289,126 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         const uint32_t extx = (!D2 && (x1 & 0x80)) ? 0xffffff00u : 0u;  // sign-extended _mm_cvtsi32_si128
         const uint32_t extv = (!D2 && (v1 & 0x80)) ? 0xffffff00u : 0u;
         uint32_t *row = CIG ? (uint32_t *)(tb + (size_t)r * ncol16) : nullptr;
+        // last bytes of x, v, x2 of every word, packed, and handed to the next word's owner
+        uint32_t rv[K];
+        {
+          uint32_t pk[K];
 #pragma unroll
-        for (int i = K - 1; i >= 0; --i) {
+          for (int i = 0; i < K; ++i) {
+            pk[i] = __byte_perm(X[i], V[i], 0x0073);
+            if (D2) pk[i] = __byte_perm(pk[i], X2[i], 0x0710);
+          }
+#pragma unroll
+          for (int i = 0; i < K; ++i) {
+            const uint32_t send = (k == G - 1) ? (i > 0 ? pk[i > 0 ? i - 1 : 0] : 0u) : pk[i];
+            rv[i] = __shfl_sync(gm, send, (k - 1) & (G - 1), G);
+          }
+          if (k == 0) rv[0] = x1 | (v1 << 8) | (x21 << 16);
+        }
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
           const int wi = k + G * i;
-          const uint32_t sx = (k == G - 1) ? (i > 0 ? X[i > 0 ? i - 1 : 0] : 0u) : X[i];
-          const uint32_t sv = (k == G - 1) ? (i > 0 ? V[i > 0 ? i - 1 : 0] : 0u) : V[i];
-          uint32_t px = __shfl_sync(gm, sx, (k - 1) & (G - 1), G);
-          uint32_t pv = __shfl_sync(gm, sv, (k - 1) & (G - 1), G);
-          uint32_t px2 = 0;
-          if (D2) {
-            const uint32_t sx2 = (k == G - 1) ? (i > 0 ? X2[i > 0 ? i - 1 : 0] : 0u) : X2[i];
-            px2 = __shfl_sync(gm, sx2, (k - 1) & (G - 1), G);
-          }
-          if (i == 0 && k == 0) px = x1 << 24, pv = v1 << 24, px2 = x21 << 24;
-          if (wi < nlive) {
-            uint32_t xt1 = __funnelshift_l(px, X[i], 8);  // x[r-1][t-1 .. t+2]
-            uint32_t vt1 = __funnelshift_l(pv, V[i], 8);
-            if (!D2 && i == 0 && k == 0) xt1 |= extx, vt1 |= extv;
-            const uint32_t ut = U[i];
-            uint32_t z = S[i], a = add8(xt1, vt1), b = add8(Y[i], ut), d = 0;
-            if (!D2) {
-              if (MODE == 0) {
-                z = maxs8(z, a);
-              } else if (MODE == 1) {
-                const uint32_t M = bmask(gts8(a, z));
-                d = M & 0x01010101u;
-                z = sel(M, a, z);
-                d = sel(bmask(gts8(b, z)), 0x02020202u, d);
-              } else {
-                const uint32_t M = bmask(gts8(z, a));
-                d = ~M & 0x01010101u;
-                z = sel(M, z, a);
-                d = sel(bmask(gts8(z, b)), d, 0x02020202u);
-              }
-              z = maxu8(z, b);
-              z = minu8(z, maxsc4);
-              U[i] = sub8(z, vt1);
-              V[i] = sub8(z, ut);
-              z = sub8(z, q4);
-              a = sub8(a, z);
-              b = sub8(b, z);
-              if (MODE == 0) {
-                X[i] = relu8(a);
-                Y[i] = relu8(b);
-              } else if (MODE == 1) {
-                const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi;
-                X[i] = a & bmask(ga);
-                Y[i] = b & bmask(gb);
-                d |= (ga >> 4) | (gb >> 3);
-              } else {
-                X[i] = relu8(a);
-                Y[i] = relu8(b);
-                d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3);
-              }
+          const bool live = wi < nlive;
+          uint32_t xt1 = __byte_perm(rv[i], X[i], 0x6540);  // x[r-1][t-1 .. t+2]
+          uint32_t vt1 = __byte_perm(rv[i], V[i], 0x6541);
+          if (!D2 && i == 0 && k == 0) xt1 |= extx, vt1 |= extv;
+          const uint32_t ut = U[i];
+          uint32_t z = S[i], a = add8(xt1, vt1), b = add8(Y[i], ut), d = 0;
+          uint32_t nu, nv, nx, ny, nx2 = 0, ny2 = 0;
+          if (!D2) {
+            if (MODE == 0) {
+              z = maxs8(z, a);
+            } else if (MODE == 1) {
+              const uint32_t M = bmask(gts8(a, z));
+              d = M & 0x01010101u;
+              z = sel(M, a, z);
+              d = sel(bmask(gts8(b, z)), 0x02020202u, d);
             } else {
-              const uint32_t x2t1 = __funnelshift_l(px2, X2[i], 8);
-              uint32_t a2 = add8(x2t1, vt1), b2 = add8(Y2[i], ut);
-              if (MODE == 0) {
-                z = maxs8(z, a);
-                z = maxs8(z, b);
-                z = maxs8(z, a2);
-                z = maxs8(z, b2);
-              } else if (MODE == 1) {
-                uint32_t M = bmask(gts8(a, z));
-                d = M & 0x01010101u;
-                z = sel(M, a, z);
-                M = bmask(gts8(b, z));
-                d = sel(M, 0x02020202u, d);
-                z = sel(M, b, z);
-                M = bmask(gts8(a2, z));
-                d = sel(M, 0x03030303u, d);
-                z = sel(M, a2, z);
-                M = bmask(gts8(b2, z));
-                d = sel(M, 0x04040404u, d);
-                z = sel(M, b2, z);
-              } else {
-                uint32_t M = bmask(gts8(z, a));
-                d = ~M & 0x01010101u;
-                z = sel(M, z, a);
-                M = bmask(gts8(z, b));
-                d = sel(M, d, 0x02020202u);
-                z = sel(M, z, b);
-                M = bmask(gts8(z, a2));
-                d = sel(M, d, 0x03030303u);
-                z = sel(M, z, a2);
-                M = bmask(gts8(z, b2));
-                d = sel(M, d, 0x04040404u);
-                z = sel(M, z, b2);
-              }
-              z = mins8(z, mchraw4);
-              U[i] = sub8(z, vt1);
-              V[i] = sub8(z, ut);
-              uint32_t tq = sub8(z, q4);
-              a = sub8(a, tq);
-              b = sub8(b, tq);
-              tq = sub8(z, q24);
-              a2 = sub8(a2, tq);
-              b2 = sub8(b2, tq);
-              if (MODE == 1) {
-                const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi, ga2 = gt0s8(a2) & kHi, gb2 = gt0s8(b2) & kHi;
-                X[i] = sub8(a & bmask(ga), qe4);
-                Y[i] = sub8(b & bmask(gb), qe4);
-                X2[i] = sub8(a2 & bmask(ga2), qe24);
-                Y2[i] = sub8(b2 & bmask(gb2), qe24);
-                d |= (ga >> 4) | (gb >> 3) | (ga2 >> 2) | (gb2 >> 1);
-              } else {
-                X[i] = sub8(relu8(a), qe4);
-                Y[i] = sub8(relu8(b), qe4);
-                X2[i] = sub8(relu8(a2), qe24);
-                Y2[i] = sub8(relu8(b2), qe24);
-                if (MODE == 2)
-                  d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3) | ((~a2 & kHi) >> 2) | ((~b2 & kHi) >> 1);
-              }
+              const uint32_t M = bmask(gts8(z, a));
+              d = ~M & 0x01010101u;
+              z = sel(M, z, a);
+              d = sel(bmask(gts8(z, b)), d, 0x02020202u);
             }
-            if (CIG) row[wi] = d;
+            z = maxu8(z, b);
+            z = minu8(z, maxsc4);
+            nu = sub8(z, vt1);
+            nv = sub8(z, ut);
+            z = sub8(z, q4);
+            a = sub8(a, z);
+            b = sub8(b, z);
+            if (MODE == 1) {
+              const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi;
+              nx = a & bmask(ga);
+              ny = b & bmask(gb);
+              d |= (ga >> 4) | (gb >> 3);
+            } else {
+              nx = relu8(a);
+              ny = relu8(b);
+              if (MODE == 2) d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3);
+            }
+          } else {
+            const uint32_t x2t1 = __byte_perm(rv[i], X2[i], 0x6542);
+            uint32_t a2 = add8(x2t1, vt1), b2 = add8(Y2[i], ut);
+            if (MODE == 0) {
+              z = maxs8(z, a);
+              z = maxs8(z, b);
+              z = maxs8(z, a2);
+              z = maxs8(z, b2);
+            } else if (MODE == 1) {
+              uint32_t M = bmask(gts8(a, z));
+              d = M & 0x01010101u;
+              z = sel(M, a, z);
+              M = bmask(gts8(b, z));
+              d = sel(M, 0x02020202u, d);
+              z = sel(M, b, z);
+              M = bmask(gts8(a2, z));
+              d = sel(M, 0x03030303u, d);
+              z = sel(M, a2, z);
+              M = bmask(gts8(b2, z));
+              d = sel(M, 0x04040404u, d);
+              z = sel(M, b2, z);
+            } else {
+              uint32_t M = bmask(gts8(z, a));
+              d = ~M & 0x01010101u;
+              z = sel(M, z, a);
+              M = bmask(gts8(z, b));
+              d = sel(M, d, 0x02020202u);
+              z = sel(M, z, b);
+              M = bmask(gts8(z, a2));
+              d = sel(M, d, 0x03030303u);
+              z = sel(M, z, a2);
+              M = bmask(gts8(z, b2));
+              d = sel(M, d, 0x04040404u);
+              z = sel(M, z, b2);
+            }
+            z = mins8(z, mchraw4);
+            nu = sub8(z, vt1);
+            nv = sub8(z, ut);
+            uint32_t tq = sub8(z, q4);
+            a = sub8(a, tq);
+            b = sub8(b, tq);
+            tq = sub8(z, q24);
+            a2 = sub8(a2, tq);
+            b2 = sub8(b2, tq);
+            if (MODE == 1) {
+              const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi, ga2 = gt0s8(a2) & kHi, gb2 = gt0s8(b2) & kHi;
+              nx = sub8(a & bmask(ga), qe4);
+              ny = sub8(b & bmask(gb), qe4);
+              nx2 = sub8(a2 & bmask(ga2), qe24);
+              ny2 = sub8(b2 & bmask(gb2), qe24);
+              d |= (ga >> 4) | (gb >> 3) | (ga2 >> 2) | (gb2 >> 1);
+            } else {
+              nx = sub8(relu8(a), qe4);
+              ny = sub8(relu8(b), qe4);
+              nx2 = sub8(relu8(a2), qe24);
+              ny2 = sub8(relu8(b2), qe24);
+              if (MODE == 2)
+                d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3) | ((~a2 & kHi) >> 2) | ((~b2 & kHi) >> 1);
+            }
           }
+          U[i] = nu, V[i] = nv, X[i] = nx, Y[i] = ny;
+          if (D2) X2[i] = nx2, Y2[i] = ny2;
+          if (CIG && live) row[wi] = d;
         }
         ++n_diag;
         cells += en0 - st0 + 1;
@@ -430,9 +456,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               }
             }
           }
-          int32_t gmax = lmax;
-#pragma unroll
-          for (int off = G / 2; off > 0; off >>= 1) gmax = max(gmax, __shfl_xor_sync(gm, gmax, off, G));
+          const int32_t gmax = __reduce_max_sync(gm, lmax);
           // tie-break of the reference: en0 first, then four int32 lanes over
           // [st0, en1) (lowest lane, then lowest t), then the scalar tail [en1, en0)
           uint32_t key = 0xffffffffu;
@@ -455,8 +479,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               }
             }
           }
-#pragma unroll
-          for (int off = G / 2; off > 0; off >>= 1) key = min(key, __shfl_xor_sync(gm, key, off, G));
+          key = __reduce_min_sync(gm, key);
           const int32_t max_H = gmax;
           const int mt = key == 0 ? en0 : st0 + (int)(key & 0xffffffu);
           if (en0 == tlen - 1 && Hen0 > mte) mte = Hen0, mte_q = r - en0;

@@ -30,7 +30,7 @@ const ExtShape kExtShapes[kNumExtShapes] = {KSW2G_SHAPES(KSW2G_SHAPE)};
 
 int ext_shape_for(int n_col) {
   for (int i = 0; i < kNumExtShapes; ++i)
-    if (kExtShapes[i].G * kExtShapes[i].K >= 4 * (n_col + 1)) return i;
+    if (kExtShapes[i].G * kExtShapes[i].K >= 4 * n_col) return i;
   return -1;
 }
 

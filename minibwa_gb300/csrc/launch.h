@@ -8,7 +8,7 @@
 namespace ksw2g {
 
 // Thread-group shapes instantiated for the extension DP kernel.  A pair with
-// n_col_ 16-byte blocks per anti-diagonal needs G*K >= 4*(n_col_+1) words.
+// n_col_ 16-byte blocks per anti-diagonal needs G*K >= 4*n_col_ words.
 struct ExtShape {
   int G, K;
 };
@@ -55,8 +55,15 @@ struct LLLaunch {
   uint64_t *blist;          // per-job second-best scratch (KSW_LL_SUBO), may be null
   const int64_t *blist_off;
   int *job_counter;
+  int qlen_max;             // longest query of the launch
+  int mat_max;              // largest matrix entry
 };
-cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st);
+// Picks the DPX kernel (two lanes per thread) when it is exact for the
+// launch -- always for u8; for i16 when no H value can reach 32767 and the gap
+// costs are in [0, 32767] -- else the one-lane-per-thread kernel.
+// force: 0 automatic, 1 one lane per thread, 2 DPX (only where exact).
+cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st, int force = 0);
+bool ll_dpx_exact(int size, const LLLaunch &L);
 int ll_slen_cap(int size);
 
 int num_sms(int device);

@@ -209,3 +209,186 @@ ll_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__re
 }
 
 }  // namespace ksw2g
+
+namespace ksw2g {
+
+// Two SSE lanes per thread, in the two halfwords of every register, on the DPX
+// 16x2 instructions: thread t of a group of T = LANES/2 threads holds lanes t
+// (low half) and t+T (high half) of one job.  Every step of the reference's
+// recurrences is one instruction for both lanes:
+//   u8 :  h = max(max(min(h + S, 255) - shift, 0), e, f)     (adds/subs_epu8)
+//   i16:  h = max(h + S, e, f)                                (adds_epi16 without saturation)
+//   t = max(h - goe, 0);  e = max(e - ge, t);  f = max(f - ge, t)  (subs_epu*, max_ep*)
+// The u8 form is exact for every input.  The i16 form is exact when the host
+// has checked that no H value can reach 32767 and that 0 <= gape, gapo+gape
+// <= 32767; otherwise the host launches ll_kernel above.
+template <int SIZE, int SLEN>
+__global__ void __launch_bounds__(128)
+ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__restrict__ arena,
+              const int8_t *__restrict__ mat_g, int m, int gapo, int gape, ksw2g_ll_result *__restrict__ res,
+              uint64_t *__restrict__ blist, const int64_t *__restrict__ blist_off, int *__restrict__ job_counter) {
+  constexpr int LANES = SIZE == 1 ? 16 : 8;
+  constexpr int T = LANES / 2;
+  const int lane = threadIdx.x & 31;
+  const int t = lane & (T - 1);
+  const int grp = threadIdx.x / T;
+  const unsigned gm = ((1u << T) - 1u) << (lane & ~(T - 1));
+  extern __shared__ uint32_t lld_smem[];
+  const int prof_stride = m * SLEN * T + T;  // +T words staggers the groups over the banks
+  uint32_t *prof = lld_smem + grp * prof_stride;
+
+  int shift = 127, mdiff = 0;  // ksw2_ll_sse.c:66-74
+  for (int a = 0; a < m * m; ++a) {
+    const int v = mat_g[a];
+    if (v < (int)(int8_t)(uint8_t)shift) shift = (uint8_t)v;
+    if (v > (int)(int8_t)(uint8_t)mdiff) mdiff = (uint8_t)v;
+  }
+  const int qmax = mdiff;
+  shift = (256 - shift) & 0xff;
+  const int goe = SIZE == 1 ? ((gapo + gape) & 0xff) : (gapo + gape);
+  const int ge = SIZE == 1 ? (gape & 0xff) : gape;
+  auto pk = [](int lo, int hi) -> uint32_t { return (uint32_t)(uint16_t)lo | ((uint32_t)(uint16_t)hi << 16); };
+  const uint32_t NGOE = pk(-goe, -goe), NGE = pk(-ge, -ge), NSHIFT = pk(-shift, -shift), C255 = pk(255, 255);
+
+  uint32_t H[SLEN], E[SLEN], HM[SLEN];
+  int jid = -1, slen = 0, qlen = 0, tlen = 0, xtra = 0, i = 0, te = -1, gmax = 0, n_b = 0, minsc = 0, endsc = 0;
+  const uint8_t *tp = nullptr;
+  uint64_t *bl = nullptr;
+  bool active = false, need = true;
+
+  for (;;) {
+    if (need) {
+      int j = 0;
+      if (t == 0) j = atomicAdd(job_counter, 1);
+      j = __shfl_sync(gm, j, 0, T);
+      need = false;
+      active = j < n_jobs;
+      if (active) {
+        jid = j;
+        const ksw2g_ll_job J = jobs[jid];
+        qlen = J.qlen, tlen = J.tlen, xtra = J.xtra;
+        slen = (qlen + LANES - 1) / LANES;
+        tp = arena + J.toff;
+        const uint8_t *qp = arena + J.qoff;
+        // striped profile (ksw2_ll_sse.c:77-95): lane l of segment s scores query position s + l*slen
+        for (int a = 0; a < m; ++a)
+#pragma unroll
+          for (int s = 0; s < SLEN; ++s) {
+            if (s < slen) {
+              int v2[2];
+#pragma unroll
+              for (int h = 0; h < 2; ++h) {
+                const int k = s + (t + h * T) * slen;
+                const int qc = k >= qlen ? 0 : qp[k];
+                const int v = k >= qlen ? -1 : mat_g[a * m + (qc < m ? qc : m - 1)];  // codes must be < m
+                v2[h] = SIZE == 1 ? ((v + shift) & 0xff) : v;
+              }
+              prof[(a * SLEN + s) * T + t] = pk(v2[0], v2[1]);
+            }
+          }
+        __syncwarp(gm);
+        minsc = (xtra & KSW2G_LL_SUBO) ? (xtra & 0xffff) : 0x10000;
+        endsc = (xtra & KSW2G_LL_STOP) ? (xtra & 0xffff) : 0x10000;
+        bl = (blist && (xtra & KSW2G_LL_SUBO)) ? blist + blist_off[jid] : nullptr;
+#pragma unroll
+        for (int s = 0; s < SLEN; ++s) H[s] = 0, E[s] = 0, HM[s] = 0;
+        i = 0, te = -1, gmax = 0, n_b = 0;
+      }
+    }
+    if (__all_sync(0xffffffffu, !active)) break;
+    if (!active) continue;
+
+    bool done = i >= tlen;
+    if (!done) {
+      const int a = tp[i] < m ? tp[i] : m - 1;
+      const uint32_t *S = prof + a * SLEN * T + t;
+      uint32_t hlast = H[0];
+#pragma unroll
+      for (int s = 1; s < SLEN; ++s) hlast = (s == slen - 1) ? H[s] : hlast;
+      // one-lane shift of the last segment (ksw2_ll_sse.c:146-147): lane l <- lane l-1, lane 0 <- 0
+      const uint32_t up = __shfl_up_sync(gm, hlast, 1, T), wrap = __shfl_sync(gm, hlast, T - 1, T);
+      uint32_t h = t ? up : (wrap << 16);
+      uint32_t f = 0, mx = 0;
+#pragma unroll
+      for (int s = 0; s < SLEN; ++s) {
+        if (s < slen) {
+          const uint32_t sc = S[s * T];
+          uint32_t hv;
+          if (SIZE == 1) hv = __viaddmax_s16x2(__viaddmin_s16x2(h, sc, C255), NSHIFT, 0u);
+          else hv = __vadd2(h, sc);
+          hv = __vimax3_s16x2(hv, E[s], f);
+          mx = __vmaxs2(mx, hv);
+          h = H[s];
+          H[s] = hv;
+          const uint32_t tt = __viaddmax_s16x2(hv, NGOE, 0u);
+          E[s] = __viaddmax_s16x2(E[s], NGE, tt);
+          f = __viaddmax_s16x2(f, NGE, tt);
+        }
+      }
+      bool fin = false;  // lazy-F (ksw2_ll_sse.c:175-185 / 287-297)
+      for (int kk = 0; kk < 16 && !fin; ++kk) {
+        const uint32_t fu = __shfl_up_sync(gm, f, 1, T), fw = __shfl_sync(gm, f, T - 1, T);
+        f = t ? fu : (fw << 16);
+#pragma unroll
+        for (int s = 0; s < SLEN; ++s) {
+          if (s < slen && !fin) {
+            const uint32_t hv = __vmaxs2(H[s], f);
+            H[s] = hv;
+            const uint32_t hh = __viaddmax_s16x2(hv, NGOE, 0u);
+            f = __viaddmax_s16x2(f, NGE, 0u);
+            fin = __all_sync(gm, (__vmaxs2(f, hh) ^ hh) == 0u);  // f <= hh in every lane
+          }
+        }
+      }
+      int m2 = max((int)(int16_t)(uint16_t)mx, (int)(int16_t)(uint16_t)(mx >> 16));
+      const int imax = __reduce_max_sync(gm, m2);
+      if (imax >= minsc && bl != nullptr && t == 0) {  // second best (ksw2_ll_sse.c:188-193)
+        if (n_b == 0 || (int32_t)bl[n_b - 1] + 1 != i) bl[n_b++] = (uint64_t)imax << 32 | (uint32_t)i;
+        else if ((int)(bl[n_b - 1] >> 32) < imax) bl[n_b - 1] = (uint64_t)imax << 32 | (uint32_t)i;
+      }
+      if (imax >= minsc && bl != nullptr) n_b = __shfl_sync(gm, n_b, 0, T);
+      if (imax > gmax) {
+        gmax = imax, te = i;
+#pragma unroll
+        for (int s = 0; s < SLEN; ++s) HM[s] = H[s];
+        if ((SIZE == 1 && gmax + shift >= 255) || gmax >= endsc) done = true;
+      }
+      ++i;
+      if (i >= tlen) done = true;
+    }
+    if (done) {
+      ksw2g_ll_result o;
+      o.score = SIZE == 1 ? (gmax + shift < 255 ? gmax : 255) : gmax;
+      o.te = te, o.qe = -1, o.score2 = -1, o.te2 = -1, o.rows = i;
+      if (SIZE == 2 || o.score != 255) {
+        uint32_t best = 0;
+        bool any = false;
+#pragma unroll
+        for (int s = 0; s < SLEN; ++s) {
+          if (s < slen) {
+#pragma unroll
+            for (int hf = 0; hf < 2; ++hf) {
+              const uint32_t v = (HM[s] >> (16 * hf)) & 0xffffu;
+              const uint32_t key = (v << 16) | (uint32_t)(0xffff - (s + (t + hf * T) * slen));
+              if (!any || key > best) best = key, any = true;
+            }
+          }
+        }
+        best = __reduce_max_sync(gm, best);
+        if (slen > 0) o.qe = 0xffff - (int)(best & 0xffff);
+        if (bl != nullptr && t == 0 && n_b > 0) {
+          const int c = qmax > 0 ? (o.score + qmax - 1) / qmax : 0;
+          const int low = te - c, high = te + c;
+          for (int b = 0; b < n_b; ++b) {
+            const int e = (int32_t)bl[b];
+            if ((e < low || e > high) && (int)(bl[b] >> 32) > o.score2) o.score2 = (int)(bl[b] >> 32), o.te2 = e;
+          }
+        }
+      }
+      if (t == 0) res[jid] = o;
+      need = true;
+    }
+  }
+}
+
+}  // namespace ksw2g

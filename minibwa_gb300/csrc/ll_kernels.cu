@@ -11,11 +11,59 @@ typedef void (*ll_fn)(const ksw2g_ll_job *, int, const uint8_t *, const int8_t *
 static const int kSlen[] = {8, 16, 32, 64};
 static const ll_fn kLL[2][4] = {{ll_kernel<1, 8>, ll_kernel<1, 16>, ll_kernel<1, 32>, ll_kernel<1, 64>},
                                 {ll_kernel<2, 8>, ll_kernel<2, 16>, ll_kernel<2, 32>, ll_kernel<2, 64>}};
+static const int kSlenD[] = {8, 16, 24, 32, 48};
+static const ll_fn kLLD[2][5] = {
+    {ll_dpx_kernel<1, 8>, ll_dpx_kernel<1, 16>, ll_dpx_kernel<1, 24>, ll_dpx_kernel<1, 32>, ll_dpx_kernel<1, 48>},
+    {ll_dpx_kernel<2, 8>, ll_dpx_kernel<2, 16>, ll_dpx_kernel<2, 24>, ll_dpx_kernel<2, 32>, ll_dpx_kernel<2, 48>}};
 
 int ll_slen_cap(int size) { (void)size; return 64; }
 
-cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st) {
+bool ll_dpx_exact(int size, const LLLaunch &L) {
+  if (size == 1) return true;
+  const int goe = L.gapo + L.gape;
+  if (L.gape < 0 || goe < 0 || goe > 32767) return false;
+  const long long mpos = L.mat_max > 0 ? L.mat_max : 0;
+  return ((long long)L.qlen_max + 1) * mpos <= 32767;
+}
+
+static cudaError_t launch_dpx(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st, bool &done) {
+  done = false;
+  int si = -1;
+  for (int i = 0; i < 5; ++i)
+    if (slen_max <= kSlenD[i]) {
+      si = i;
+      break;
+    }
+  if (si < 0) return cudaSuccess;
+  const ll_fn fn = kLLD[size - 1][si];
+  const int T = size == 1 ? 8 : 4, groups = 128 / T;
+  const size_t smem = (size_t)groups * (L.m * kSlenD[si] * T + T) * sizeof(uint32_t);
+  if (smem > 200 * 1024) return cudaSuccess;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int occ = 0, sms = 0, d = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 128, smem);
+  cudaGetDevice(&d);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+  int blocks = (L.n_jobs + groups - 1) / groups;
+  const int cap = sms * (occ > 0 ? occ : 1);
+  if (blocks > cap) blocks = cap;
+  if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
+  fn<<<blocks, 128, smem, st>>>(L.jobs, L.n_jobs, L.arena, L.mat, L.m, L.gapo, L.gape, L.res, L.blist, L.blist_off,
+                                L.job_counter);
+  done = true;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st, int force) {
   if (L.n_jobs <= 0) return cudaSuccess;
+  if (force != 1 && (size == 1 || size == 2) && ll_dpx_exact(size, L)) {
+    bool done = false;
+    cudaError_t e = launch_dpx(size, slen_max, L, max_blocks, st, done);
+    if (e != cudaSuccess || done) return e;
+  }
   int si = -1;
   for (int i = 0; i < 4; ++i)
     if (slen_max <= kSlen[i]) {

@@ -26,7 +26,7 @@
 #define __device__
 #define __host__
 #define __forceinline__ inline
-#define __launch_bounds__(x)
+#define __launch_bounds__(...)
 #define __restrict__
 #define __shared__
 
@@ -184,6 +184,31 @@ inline uint32_t __byte_perm(uint32_t x, uint32_t y, uint32_t s) {
 inline uint32_t __funnelshift_l(uint32_t lo, uint32_t hi, uint32_t sh) {
   const uint64_t v = ((uint64_t)hi << 32) | lo;
   return (uint32_t)((v << (sh & 31)) >> 32);
+}
+// 16x2 SIMD / DPX built-ins: per halfword, signed 16-bit, additions wrap
+namespace emu {
+inline int16_t lo16(uint32_t x) { return (int16_t)(uint16_t)x; }
+inline int16_t hi16(uint32_t x) { return (int16_t)(uint16_t)(x >> 16); }
+inline uint32_t pk16(int lo, int hi) { return (uint32_t)(uint16_t)lo | ((uint32_t)(uint16_t)hi << 16); }
+template <class F>
+inline uint32_t map16(uint32_t a, uint32_t b, uint32_t c, F f) {
+  return pk16(f(lo16(a), lo16(b), lo16(c)), f(hi16(a), hi16(b), hi16(c)));
+}
+}  // namespace emu
+inline uint32_t __vadd2(uint32_t a, uint32_t b) {
+  return emu::map16(a, b, 0, [](int x, int y, int) { return (int16_t)(x + y); });
+}
+inline uint32_t __vmaxs2(uint32_t a, uint32_t b) {
+  return emu::map16(a, b, 0, [](int x, int y, int) { return x > y ? x : y; });
+}
+inline uint32_t __viaddmax_s16x2(uint32_t a, uint32_t b, uint32_t c) {
+  return emu::map16(a, b, c, [](int x, int y, int z) { const int s = (int16_t)(x + y); return s > z ? s : z; });
+}
+inline uint32_t __viaddmin_s16x2(uint32_t a, uint32_t b, uint32_t c) {
+  return emu::map16(a, b, c, [](int x, int y, int z) { const int s = (int16_t)(x + y); return s < z ? s : z; });
+}
+inline uint32_t __vimax3_s16x2(uint32_t a, uint32_t b, uint32_t c) {
+  return emu::map16(a, b, c, [](int x, int y, int z) { return std::max(x, std::max(y, z)); });
 }
 template <typename T>
 inline T __ldg(const T *p) { return *p; }

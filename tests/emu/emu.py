@@ -43,11 +43,13 @@ def lib():
         _L.emu_ext.restype = i
         _L.emu_ext.argtypes = [i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, C.c_longlong, i]
         _L.emu_ll.restype = i
-        _L.emu_ll.argtypes = [i, i, i, vp, vp, vp, i, i, i, vp, vp, vp, i]
+        _L.emu_ll.argtypes = [i, i, i, vp, vp, vp, i, i, i, vp, vp, vp, i, i]
         _L.emu_derive_params.restype = None
         _L.emu_derive_params.argtypes = [i, i, vp, i, i, i, i, vp]
         _L.emu_shape_words.restype = i
         _L.emu_shape_words.argtypes = [i]
+        _L.emu_shape_threads.restype = i
+        _L.emu_shape_threads.argtypes = [i]
         _L.emu_num_shapes.restype = i
     return _L
 
@@ -83,7 +85,7 @@ def ncol(ql, tl, w):
 def shape_for(nc):
     L = lib()
     for s in range(L.emu_num_shapes()):
-        if L.emu_shape_words(s) >= 4 * (nc + 1):
+        if L.emu_shape_words(s) >= 4 * nc:
             return s
     return -1
 
@@ -103,10 +105,13 @@ def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=N
     mat = np.ascontiguousarray(mat, np.int8)
     L.emu_derive_params(int(dual), m, mat.ctypes.data, q, e, q2, e2, P.ctypes.data)
     mode = 0 if flag & 1 else (2 if flag & 2 else 1)
+    need = max(shape_for(ncol(len(a), len(b), w)) for a, b in zip(qs, ts))
     if shape is None:
-        shape = max(shape_for(ncol(len(a), len(b), w)) for a, b in zip(qs, ts))
+        shape = need
+    if L.emu_shape_words(shape) < L.emu_shape_words(need):
+        raise ValueError("shape too small for the band")
     if threads is None:  # one thread group per emulated warp
-        threads = [4, 8, 8, 16, 32, 32][shape]
+        threads = L.emu_shape_threads(shape)
     foot = [((len(a) + len(b) - 1) * ncol(len(a), len(b), w) * 16 + 15) & ~15 if mode else 0 for a, b in zip(qs, ts)]
     tb_off = np.concatenate([[0], np.cumsum(foot)[:-1]]).astype(np.int64)
     tb = np.zeros(max(sum(foot), 16), np.uint8)
@@ -122,7 +127,7 @@ def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=N
     return res, cigars
 
 
-def ll(size, m, mat, gapo, gape, qs, ts, xtra, threads=None):
+def ll(size, m, mat, gapo, gape, qs, ts, xtra, threads=None, dpx=False):
     L = lib()
     n = len(qs)
     arena, qo, to = pack(qs, ts)
@@ -139,7 +144,7 @@ def ll(size, m, mat, gapo, gape, qs, ts, xtra, threads=None):
     bl = np.zeros(max(1, sum(len(t) for t in ts)), np.uint64)
     mat = np.ascontiguousarray(mat, np.int8)
     rc = L.emu_ll(size, slen, n, jobs.ctypes.data, arena.ctypes.data, mat.ctypes.data, m, gapo, gape,
-                  res.ctypes.data, bl.ctypes.data, blo.ctypes.data, threads)
+                  res.ctypes.data, bl.ctypes.data, blo.ctypes.data, threads, int(dpx))
     if rc != 0:
         raise RuntimeError(f"emu_ll rc={rc}")
     return res

@@ -23,6 +23,7 @@ LaneState g_lane_state[1024];
 
 namespace ksw2g {
 int16_t ll_smem[1 << 20];
+uint32_t lld_smem[1 << 20];
 }
 
 using namespace ksw2g;
@@ -71,6 +72,7 @@ extern "C" {
 
 int emu_num_shapes(void) { return KSW2G_NUM_SHAPES; }
 int emu_shape_words(int s) { return kShape[s][0] * kShape[s][1]; }
+int emu_shape_threads(int s) { return kShape[s][0]; }
 
 void emu_derive_params(int dual, int m, const int8_t *mat, int q, int e, int q2, int e2, ksw2g_ext_params *P) {
   derive_ext_params(dual, (int8_t)m, mat, (int8_t)q, (int8_t)e, (int8_t)q2, (int8_t)e2, *P);
@@ -102,7 +104,8 @@ int emu_ext(int dual, int mode, int shape, const ksw2g_ext_params *P, int n, con
 }
 
 int emu_ll(int size, int slen_max, int n, const ksw2g_ll_job *jobs, const uint8_t *arena, const int8_t *mat, int m,
-           int gapo, int gape, ksw2g_ll_result *res, uint64_t *blist, const int64_t *blist_off, int threads) {
+           int gapo, int gape, ksw2g_ll_result *res, uint64_t *blist, const int64_t *blist_off, int threads,
+           int dpx) {
   int counter = 0;
   typedef void (*ll_fn)(const ksw2g_ll_job *, int, const uint8_t *, const int8_t *, int, int, int,
                         ksw2g_ll_result *, uint64_t *, const int64_t *, int *);
@@ -115,6 +118,20 @@ int emu_ll(int size, int slen_max, int n, const ksw2g_ll_job *jobs, const uint8_
       f = size == 1 ? t1[i] : t2[i];
       break;
     }
+  if (dpx) {
+    const int sd[] = {8, 16, 24, 32, 48};
+    const ll_fn d1[] = {ll_dpx_kernel<1, 8>, ll_dpx_kernel<1, 16>, ll_dpx_kernel<1, 24>, ll_dpx_kernel<1, 32>,
+                        ll_dpx_kernel<1, 48>};
+    const ll_fn d2[] = {ll_dpx_kernel<2, 8>, ll_dpx_kernel<2, 16>, ll_dpx_kernel<2, 24>, ll_dpx_kernel<2, 32>,
+                        ll_dpx_kernel<2, 48>};
+    f = nullptr;
+    for (int i = 0; i < 5; ++i)
+      if (slen_max <= sd[i]) {
+        f = size == 1 ? d1[i] : d2[i];
+        break;
+      }
+    threads = (size == 1 ? 8 : 4) * (threads / (size == 1 ? 16 : 8));
+  }
   if (!f) return -1;
   run_block(threads, [&] { f(jobs, n, arena, mat, m, gapo, gape, res, blist, blist_off, &counter); });
   return 0;

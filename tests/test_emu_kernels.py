@@ -48,6 +48,8 @@ def test_emulated_lockstep_groups_and_work_counter(emu):
     for dual, flag in ((0, 0x40), (1, 0xc2), (1, 0x41), (0, 0x08)):
         q2, e2 = (24, 1) if dual else (12, 2)
         res, cig = emu.ext(dual, 5, p.mat, 12, 2, q2, e2, qs, ts, 25, 100, 10, flag, threads=32, shape=0)
+        res3, cig3 = emu.ext(dual, 5, p.mat, 12, 2, q2, e2, qs, ts, 25, 100, 10, flag, threads=32, shape=1)
+        assert np.array_equal(res, res3) and cig == cig3
         for i in range(len(qs)):
             exp, _ = O.extz(dual, qs[i], ts[i], 5, p.mat, 12, 2, q2, e2, 25, 100, 10, flag)
             assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, i)
@@ -68,9 +70,26 @@ def test_emulated_wide_band_shapes(emu):
     p = synth.config1(4, seed=9)
     qs = [p.query(i) for i in range(len(p))]
     ts = [p.target(i) for i in range(len(p))]
-    for w, shape in ((230, 3), (480, 4), (900, 5)):
+    for w, shape in ((100, 3), (100, 4), (180, 6), (230, 6), (480, 7), (480, 8), (900, 9)):
         res, cig = emu.ext(1, 5, p.mat, 12, 2, 24, 1, qs, ts, w, 100, 10, 0x40, shape=shape)
         for i in range(len(qs)):
             exp, _ = O.extz(1, qs[i], ts[i], 5, p.mat, 12, 2, 24, 1, w, 100, 10, 0x40)
             assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (w, i)
             assert cig[i] == exp["cigar"]
+
+
+def test_emulated_dpx_ll_kernel_matches_golden(emu, golden):
+    """The two-lanes-per-thread DPX kernel, wherever the host would choose it."""
+    n = 0
+    for i, c in enumerate(golden_ll_cases(golden)):
+        mat_max = int(c["mat"].max())
+        exact = c["size"] == 1 or (c["gape"] >= 0 and 0 <= c["gapo"] + c["gape"] <= 32767 and
+                                   (len(c["query"]) + 1) * max(mat_max, 0) <= 32767)
+        lanes = 16 if c["size"] == 1 else 8
+        if not exact or (len(c["query"]) + lanes - 1) // lanes > 48:
+            continue
+        r = emu.ll(c["size"], c["m"], c["mat"], c["gapo"], c["gape"], [c["query"]], [c["target"]], c["xtra"],
+                   dpx=True)[0]
+        assert {f: int(r[f]) for f in LL_FIELDS} == c["out"], (i, c["size"], c["xtra"])
+        n += 1
+    assert n > 200

@@ -93,3 +93,18 @@ def test_full_size_config3_sample(ctx):
     ores = O.ll_batch("orc", s.size, 5, s.mat, s.gapo, s.gape, s.jobs, s.qbuf, s.tbuf, 8)
     compare_ll(res[idx], ores)
     assert (res["rows"] == r.jobs["tlen"]).all()
+
+
+@pytest.mark.parametrize("family", ["lane", "dpx"])
+def test_both_kernel_families(ctx, family, monkeypatch):
+    """One lane per thread and the DPX two-lanes-per-thread kernel, pinned in turn, on
+    i16 and u8 rescue jobs of several query lengths."""
+    from minibwa_gb300 import synth
+    from minibwa_gb300.lib import gen_nt4_mat
+    monkeypatch.setenv("KSW2G_LL_KERNEL", family)
+    for ql, size in ((37, 2), (150, 2), (300, 2), (150, 1), (400, 1)):
+        r = synth.ll_jobs(1500, qlen=ql, tlen_lo=50, tlen_hi=900, size=size, seed=ql * 7 + size,
+                          xtra=(0x40000 | 19) if size == 1 else 0,
+                          mat=gen_nt4_mat(1, 4, 0, 1) if size == 1 else None, gapo=6 if size == 1 else 12,
+                          gape=1 if size == 1 else 2)
+        _batch(ctx, r)
