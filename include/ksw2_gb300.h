@@ -139,6 +139,30 @@ int ksw2g_ext_noalloc(int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
 					  int n_jobs, const ksw2g_job_t *jobs, const uint8_t *d_arena,
 					  ksw2g_ext_result_t *d_res, uint32_t *d_cigar, int64_t cigar_cap, void *stream);
 
+/* ---- serving engine: continuous batching over a fixed traceback budget ----
+ * Requests are admitted in arrival order as soon as one of n_slots slots is
+ * free and the request's traceback rows (the reference's footprint,
+ * ksw2_extz2_sse.c:84, summed over its jobs) fit in the tb_budget bytes of
+ * device memory the engine owns.  Admitted requests run concurrently on the
+ * slots' streams.  The caller's buffers (jobs, sequences, results, CIGAR) must
+ * stay valid until ksw2g_server_wait returns for that request. */
+typedef struct ksw2g_server ksw2g_server_t;
+int ksw2g_server_create(int device, int n_slots, int64_t tb_budget, ksw2g_server_t **server);
+void ksw2g_server_destroy(ksw2g_server_t *server);          /* drains queued requests first */
+/* Returns a request id (> 0) or a negative error code. */
+int64_t ksw2g_server_submit_ext(ksw2g_server_t *server, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+								int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs, const uint8_t *qbuf,
+								int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ext_result_t *res,
+								uint32_t *cigar, int64_t cigar_cap);
+int64_t ksw2g_server_submit_ll(ksw2g_server_t *server, int size, int m, const int8_t *mat, int gapo, int gape,
+							   int n_jobs, const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+							   const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ll_result_t *res);
+/* Blocks until the request is done; returns its status (0 or an error code) and
+ * its latency (submit to results in the caller's buffers) and queueing time. */
+int ksw2g_server_wait(ksw2g_server_t *server, int64_t id, double *latency_ms, double *queue_ms, int64_t *cigar_used);
+int ksw2g_server_stats(ksw2g_server_t *server, int64_t *admitted, int64_t *done, int64_t *peak_inflight,
+					   int64_t *peak_pool_bytes);
+
 /* Measured 32-bit integer instruction throughput of the device (lane-ops per
  * second), the denominator of the DP kernels' integer-pipe roofline. */
 int ksw2g_probe_int32_peak(int device, double *ops_per_s);

@@ -4,6 +4,7 @@
 
 libksw2gpu.so   CUDA kernels for sm_103a + the C ABI (include/ksw2.h, include/ksw2_gb300.h)
 libksw2synth.so host-only synthetic workload generator (gcc)
+libksw2loadgen.so open-loop load generator of the serving benchmark (g++, links libksw2gpu.so)
 
 Objects go to minibwa_gb300/_build/; the translation units compile in parallel.
 """
@@ -17,6 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB_GPU = os.path.join(PKG, "libksw2gpu.so")
 LIB_SYNTH = os.path.join(PKG, "libksw2synth.so")
+LIB_LOADGEN = os.path.join(PKG, "libksw2loadgen.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
@@ -53,6 +55,7 @@ def build(verbose=False, force=False):
         ("capi.cu", "capi.o", []),
         ("probe.cu", "probe.o", []),
         ("noalloc.cu", "noalloc.o", []),
+        ("server.cu", "server.o", []),
     ]
     hdrs = _headers()
     procs, objs = [], []
@@ -77,6 +80,13 @@ def build(verbose=False, force=False):
     src = os.path.join(CSRC, "synth.c")
     if force or _stale(LIB_SYNTH, [src]):
         cmd = ["gcc", "-O2", "-fPIC", "-shared", "-o", LIB_SYNTH, src, "-lm"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.check_call(cmd)
+    src = os.path.join(CSRC, "loadgen.cc")
+    if force or _stale(LIB_LOADGEN, [src, LIB_GPU] + hdrs):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", LIB_LOADGEN, src, "-L" + PKG, "-lksw2gpu",
+               "-Wl,-rpath,$ORIGIN", "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.check_call(cmd)

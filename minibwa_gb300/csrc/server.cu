@@ -1,0 +1,370 @@
+// server.cu -- continuous-batching serving engine for extension and rescue jobs.
+//
+// Requests (one batch of jobs of one kind and scoring scheme each) arrive at
+// any time from any host thread.  A scheduler thread admits them in arrival
+// order as soon as (a) one of the engine's slots is free and (b) the request's
+// traceback rows fit in the engine's device traceback pool, a fixed budget of
+// HBM managed by a first-fit allocator.  Each slot owns a CUDA stream and a
+// reusable batch (sequence arena, job table, results, CIGAR arena), so the
+// work of several requests overlaps on the device while later requests queue.
+// A host-function callback at the end of each slot's stream copies the results
+// to the caller's buffers, stamps the completion time and frees the slot and
+// its pool range, which wakes the scheduler.  Admission uses the reference's
+// traceback footprint: the rows of (qlen+tlen-1) anti-diagonals of n_col_*16
+// bytes each (ksw2_extz2_sse.c:84), summed over the request.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ksw2_gb300.h"
+#include "batch.h"
+#include "host_common.h"
+
+using namespace ksw2g;
+
+namespace {
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// First-fit allocator of [0, cap) with coalescing frees.
+struct RangeAlloc {
+  int64_t cap = 0;
+  std::map<int64_t, int64_t> free_;  // offset -> size
+  void init(int64_t c) {
+    cap = c;
+    free_.clear();
+    if (c > 0) free_[0] = c;
+  }
+  int64_t take(int64_t n) {
+    if (n <= 0) return 0;
+    for (auto it = free_.begin(); it != free_.end(); ++it)
+      if (it->second >= n) {
+        const int64_t off = it->first, rest = it->second - n;
+        free_.erase(it);
+        if (rest) free_[off + n] = rest;
+        return off;
+      }
+    return -1;
+  }
+  void give(int64_t off, int64_t n) {
+    if (n <= 0) return;
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) it->second += nx->second, free_.erase(nx);
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) pv->second += it->second, free_.erase(it);
+    }
+  }
+  int64_t free_bytes() const {
+    int64_t s = 0;
+    for (auto &kv : free_) s += kv.second;
+    return s;
+  }
+};
+
+struct Req {
+  int64_t id = 0;
+  int kind = 0;  // 0 extz2, 1 extd2, 2 ll u8, 3 ll i16
+  int n = 0;
+  int8_t m = 0, q = 0, e = 0, q2 = 0, e2 = 0;
+  int gapo = 0, gape = 0;
+  std::vector<int8_t> mat;
+  const void *jobs = nullptr;
+  const uint8_t *qbuf = nullptr, *tbuf = nullptr;
+  int64_t qlen = 0, tlen = 0;
+  void *res = nullptr;
+  uint32_t *cigar = nullptr;
+  int64_t cigar_cap = 0, cigar_used = 0;
+  int64_t need = 0;  // traceback bytes reserved while in flight
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  int status = 1;  // 1 queued/running, 0 done, < 0 error
+};
+
+struct Slot {
+  ksw2g_ctx ctx;
+  ksw2g_batch batch;
+  PinBuf res_pin, cig_pin, hdr_pin;
+  Req *req = nullptr;
+  int64_t pool_off = 0;
+  struct ksw2g_server *srv = nullptr;
+};
+
+}  // namespace
+
+struct ksw2g_server {
+  int device = 0;
+  std::vector<Slot *> slots;
+  std::vector<Slot *> idle;
+  DevBuf pool;
+  RangeAlloc alloc;
+  std::deque<Req *> queue;
+  std::unordered_map<int64_t, Req *> reqs;
+  std::mutex mu;
+  std::condition_variable cv_sched, cv_done;
+  std::thread sched;
+  bool stop = false;
+  int64_t next_id = 1;
+  int64_t n_admitted = 0, n_done = 0, peak_inflight = 0, peak_pool = 0, inflight = 0;
+};
+
+namespace {
+
+void CUDART_CB on_done(void *arg) {
+  Slot *s = (Slot *)arg;
+  ksw2g_server *S = s->srv;
+  Req *r = s->req;
+  // The waiter may free r as soon as it sees a final status, so everything that
+  // touches r after the status changes happens under the lock, status last.
+  int st = 0;
+  int64_t used = 0;
+  if (r->kind <= 1) {
+    memcpy(r->res, s->res_pin.p, sizeof(ksw2g_ext_result) * (size_t)r->n);
+    struct {
+      unsigned long long cursor;
+      int err, pad;
+    } hdr;
+    memcpy(&hdr, s->hdr_pin.p, sizeof hdr);
+    used = (int64_t)hdr.cursor;
+    if (hdr.err || used > r->cigar_cap) st = KSW2G_E_CAPACITY;
+    else if (used) memcpy(r->cigar, s->cig_pin.p, sizeof(uint32_t) * (size_t)used);
+  } else {
+    memcpy(r->res, s->res_pin.p, sizeof(ksw2g_ll_result) * (size_t)r->n);
+  }
+  const double t = now_ms();
+  std::lock_guard<std::mutex> g(S->mu);
+  S->alloc.give(s->pool_off, r->need);
+  r->cigar_used = used;
+  r->t_done = t;
+  r->status = st;
+  s->req = nullptr;
+  S->idle.push_back(s);
+  --S->inflight;
+  ++S->n_done;
+  S->cv_sched.notify_all();
+  S->cv_done.notify_all();
+}
+
+int64_t ext_need(const Req *r, int64_t budget) {
+  const ksw2g_job_t *J = (const ksw2g_job_t *)r->jobs;
+  int64_t f = 0;
+  for (int i = 0; i < r->n; ++i) {
+    if (J[i].qlen <= 0 || J[i].tlen <= 0 || ext_mode(J[i].flag) == 0) continue;
+    f += (((int64_t)(J[i].qlen + J[i].tlen - 1) * ext_ncol(J[i].qlen, J[i].tlen, J[i].w) * 16) + 15) & ~(int64_t)15;
+  }
+  return f < budget ? f : budget;
+}
+
+// Prepare (synchronous uploads on the slot's stream) and enqueue run, copies and the callback.
+int launch_req(Slot *s, Req *r) {
+  ksw2g_ctx &c = s->ctx;
+  ksw2g_batch &b = s->batch;
+  int rc;
+  if (r->kind <= 1) {
+    c.tb_budget = r->need > 0 ? r->need : 16;
+    rc = ext_prepare_into(&c, &b, r->kind, r->m, r->mat.data(), r->q, r->e, r->q2, r->e2, r->n,
+                          (const ksw2g_job_t *)r->jobs, r->qbuf, r->qlen, r->tbuf, r->tlen);
+    if (rc) return rc;
+    if ((rc = s->res_pin.ensure(sizeof(ksw2g_ext_result) * (size_t)std::max(r->n, 1))) ||
+        (rc = s->cig_pin.ensure(sizeof(uint32_t) * (size_t)b.cigar_cap)) || (rc = s->hdr_pin.ensure(64)))
+      return rc;
+    memset(s->hdr_pin.p, 0, 16);
+    if ((rc = ext_run_on(&b, c.st, s->srv->pool.as<uint8_t>() + s->pool_off, std::max<int64_t>(r->need, 16))))
+      return rc;
+    if (r->n > 0 &&
+        (cudaMemcpyAsync(s->res_pin.p, b.res.p, sizeof(ksw2g_ext_result) * (size_t)r->n, cudaMemcpyDeviceToHost,
+                         c.st) != cudaSuccess ||
+         cudaMemcpyAsync(s->hdr_pin.p, b.counters.p, 16, cudaMemcpyDeviceToHost, c.st) != cudaSuccess ||
+         (b.cigar_cap > 0 && cudaMemcpyAsync(s->cig_pin.p, b.cigar.p, sizeof(uint32_t) * (size_t)b.cigar_cap,
+                                             cudaMemcpyDeviceToHost, c.st) != cudaSuccess)))
+      return report_error(KSW2G_E_CUDA, "server: result copy failed");
+  } else {
+    rc = ll_prepare_into(&c, &b, r->kind == 2 ? 1 : 2, r->m, r->mat.data(), r->gapo, r->gape, r->n,
+                         (const ksw2g_ll_job_t *)r->jobs, r->qbuf, r->qlen, r->tbuf, r->tlen);
+    if (rc) return rc;
+    if ((rc = s->res_pin.ensure(sizeof(ksw2g_ll_result) * (size_t)std::max(r->n, 1)))) return rc;
+    if ((rc = ll_run_on(&b, c.st))) return rc;
+    if (r->n > 0 && cudaMemcpyAsync(s->res_pin.p, b.res.p, sizeof(ksw2g_ll_result) * (size_t)r->n, cudaMemcpyDeviceToHost,
+                        c.st) != cudaSuccess)
+      return report_error(KSW2G_E_CUDA, "server: result copy failed");
+  }
+  if (cudaLaunchHostFunc(c.st, on_done, s) != cudaSuccess)
+    return report_error(KSW2G_E_CUDA, "server: cudaLaunchHostFunc failed");
+  return 0;
+}
+
+void scheduler(ksw2g_server *S) {
+  cudaSetDevice(S->device);
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    S->cv_sched.wait(lk, [&] { return (S->stop && S->queue.empty()) || (!S->queue.empty() && !S->idle.empty()); });
+    if (S->stop && S->queue.empty()) return;
+    Req *r = S->queue.front();
+    const int64_t off = r->need > 0 ? S->alloc.take(r->need) : 0;
+    if (off < 0) {  // not enough contiguous pool yet: wait for a completion
+      S->cv_sched.wait(lk);
+      continue;
+    }
+    S->queue.pop_front();
+    Slot *s = S->idle.back();
+    S->idle.pop_back();
+    s->req = r;
+    s->pool_off = off;
+    r->t_admit = now_ms();
+    ++S->n_admitted;
+    ++S->inflight;
+    S->peak_inflight = std::max(S->peak_inflight, S->inflight);
+    S->peak_pool = std::max(S->peak_pool, S->alloc.cap - S->alloc.free_bytes());
+    lk.unlock();
+    const int rc = launch_req(s, r);
+    lk.lock();
+    if (rc) {  // nothing of this request is on the stream any more
+      cudaStreamSynchronize(s->ctx.st);
+      r->status = rc;
+      r->t_done = now_ms();
+      S->alloc.give(s->pool_off, r->need);
+      s->req = nullptr;
+      S->idle.push_back(s);
+      --S->inflight;
+      ++S->n_done;
+      S->cv_done.notify_all();
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int ksw2g_server_create(int device, int n_slots, int64_t tb_budget, ksw2g_server_t **out) {
+  if (!out || n_slots < 1 || n_slots > 256 || tb_budget < (1 << 20))
+    return report_error(KSW2G_E_ARG, "server: need 1..256 slots and a traceback budget >= 1 MiB");
+  if (cudaSetDevice(device) != cudaSuccess) return report_error(KSW2G_E_CUDA, "server: bad device");
+  ksw2g_server *S = new ksw2g_server;
+  S->device = device;
+  int rc;
+  if ((rc = S->pool.ensure((size_t)tb_budget))) {
+    delete S;
+    return rc;
+  }
+  S->alloc.init(tb_budget);
+  for (int i = 0; i < n_slots; ++i) {
+    Slot *s = new Slot;
+    s->srv = S;
+    s->ctx.device = device;
+    if (cudaStreamCreateWithFlags(&s->ctx.st, cudaStreamNonBlocking) != cudaSuccess) {
+      delete s;
+      ksw2g_server_destroy(S);
+      return report_error(KSW2G_E_CUDA, "server: cudaStreamCreate failed");
+    }
+    S->slots.push_back(s);
+    S->idle.push_back(s);
+  }
+  S->sched = std::thread(scheduler, S);
+  *out = S;
+  return 0;
+}
+
+extern "C" void ksw2g_server_destroy(ksw2g_server_t *S) {
+  if (!S) return;
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    S->stop = true;
+    S->cv_sched.notify_all();
+  }
+  if (S->sched.joinable()) S->sched.join();
+  cudaSetDevice(S->device);
+  for (Slot *s : S->slots) {
+    cudaStreamSynchronize(s->ctx.st);
+    for (DevBuf *d : {&s->batch.raw, &s->batch.rawmeta, &s->batch.arena, &s->batch.jobs, &s->batch.order,
+                      &s->batch.sorted, &s->batch.tb_off, &s->batch.res, &s->batch.bts, &s->batch.cigar,
+                      &s->batch.counters, &s->batch.llmat, &s->batch.blist, &s->batch.blist_off})
+      d->release();
+    s->res_pin.release(), s->cig_pin.release(), s->hdr_pin.release();
+    cudaStreamDestroy(s->ctx.st);
+    delete s;
+  }
+  for (auto &kv : S->reqs) delete kv.second;
+  S->pool.release();
+  delete S;
+}
+
+static int64_t submit(ksw2g_server *S, Req *r) {
+  r->t_submit = now_ms();
+  std::lock_guard<std::mutex> g(S->mu);
+  if (S->stop) {
+    delete r;
+    return report_error(KSW2G_E_ARG, "server: stopping");
+  }
+  r->id = S->next_id++;
+  S->reqs[r->id] = r;
+  S->queue.push_back(r);
+  S->cv_sched.notify_all();
+  return r->id;
+}
+
+extern "C" int64_t ksw2g_server_submit_ext(ksw2g_server_t *S, int dual, int8_t m, const int8_t *mat, int8_t q,
+                                           int8_t e, int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs,
+                                           const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+                                           int64_t tbuf_len, ksw2g_ext_result_t *res, uint32_t *cigar,
+                                           int64_t cigar_cap) {
+  if (!S || !mat || n_jobs < 0 || (n_jobs > 0 && (!jobs || !res)) || m <= 0)
+    return report_error(KSW2G_E_ARG, "server: bad request");
+  Req *r = new Req;
+  r->kind = dual ? 1 : 0, r->n = n_jobs, r->m = m, r->q = q, r->e = e, r->q2 = q2, r->e2 = e2;
+  r->mat.assign(mat, mat + m * m);
+  r->jobs = jobs, r->qbuf = qbuf, r->tbuf = tbuf, r->qlen = qbuf_len, r->tlen = tbuf_len;
+  r->res = res, r->cigar = cigar, r->cigar_cap = cigar_cap;
+  r->need = ext_need(r, S->alloc.cap);
+  return submit(S, r);
+}
+
+extern "C" int64_t ksw2g_server_submit_ll(ksw2g_server_t *S, int size, int m, const int8_t *mat, int gapo, int gape,
+                                          int n_jobs, const ksw2g_ll_job_t *jobs, const uint8_t *qbuf,
+                                          int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len,
+                                          ksw2g_ll_result_t *res) {
+  if (!S || !mat || n_jobs < 0 || (n_jobs > 0 && (!jobs || !res)) || m <= 0)
+    return report_error(KSW2G_E_ARG, "server: bad request");
+  Req *r = new Req;
+  r->kind = size > 1 ? 3 : 2, r->n = n_jobs, r->m = (int8_t)m, r->gapo = gapo, r->gape = gape;
+  r->mat.assign(mat, mat + m * m);
+  r->jobs = jobs, r->qbuf = qbuf, r->tbuf = tbuf, r->qlen = qbuf_len, r->tlen = tbuf_len, r->res = res;
+  r->need = 0;
+  return submit(S, r);
+}
+
+extern "C" int ksw2g_server_wait(ksw2g_server_t *S, int64_t id, double *latency_ms, double *queue_ms,
+                                 int64_t *cigar_used) {
+  if (!S) return report_error(KSW2G_E_ARG, "server: null");
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(id);
+  if (it == S->reqs.end()) return report_error(KSW2G_E_ARG, "server: unknown request");
+  Req *r = it->second;
+  S->cv_done.wait(lk, [&] { return r->status != 1; });
+  const int st = r->status;
+  if (latency_ms) *latency_ms = r->t_done - r->t_submit;
+  if (queue_ms) *queue_ms = r->t_admit - r->t_submit;
+  if (cigar_used) *cigar_used = r->cigar_used;
+  S->reqs.erase(it);
+  delete r;
+  return st;
+}
+
+extern "C" int ksw2g_server_stats(ksw2g_server_t *S, int64_t *admitted, int64_t *done, int64_t *peak_inflight,
+                                  int64_t *peak_pool_bytes) {
+  if (!S) return report_error(KSW2G_E_ARG, "server: null");
+  std::lock_guard<std::mutex> g(S->mu);
+  if (admitted) *admitted = S->n_admitted;
+  if (done) *done = S->n_done;
+  if (peak_inflight) *peak_inflight = S->peak_inflight;
+  if (peak_pool_bytes) *peak_pool_bytes = S->peak_pool;
+  return 0;
+}

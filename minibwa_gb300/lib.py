@@ -97,6 +97,12 @@ def load_library():
         "ksw2g_ext_shape_info": (i32, [i32, C.POINTER(i32), C.POINTER(i32)]),
         "ksw2g_ext_set_shape": (i32, [i32, i32, i32, i32, i32]),
         "ksw2g_probe_int32_peak": (i32, [i32, C.POINTER(C.c_double)]),
+        "ksw2g_server_create": (i32, [i32, i32, i64, C.POINTER(vp)]),
+        "ksw2g_server_destroy": (None, [vp]),
+        "ksw2g_server_submit_ext": (i64, [vp, i32, i8, vp, i8, i8, i8, i8, i32, vp, u8p, i64, u8p, i64, vp, vp, i64]),
+        "ksw2g_server_submit_ll": (i64, [vp, i32, i32, vp, i32, i32, i32, vp, u8p, i64, u8p, i64, vp]),
+        "ksw2g_server_wait": (i32, [vp, i64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(i64)]),
+        "ksw2g_server_stats": (i32, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
         "ksw_extz2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i32, i32, i32, i32, C.POINTER(KswExtz)]),
         "ksw_extd2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i8, i8, i32, i32, i32, i32,
                                  C.POINTER(KswExtz)]),
@@ -320,3 +326,67 @@ class LLBatch(_Batch):
         res = res if res is not None else np.zeros(self.n, LL_RESULT)
         _check(self.L.ksw2g_ll_fetch(self.ctx.h, self.h, _ptr(res)))
         return res
+
+
+class Request:
+    """A request in flight on a Server; keeps its buffers alive until wait()."""
+
+    def __init__(self, server, rid, kind, keep, res, cig):
+        self.server, self.id, self.kind, self._keep, self.res, self.cig = server, rid, kind, keep, res, cig
+
+    def wait(self):
+        """Returns (results, cigar words, latency_ms, queue_ms)."""
+        lat, que, used = C.c_double(), C.c_double(), C.c_int64()
+        rc = self.server.L.ksw2g_server_wait(self.server.h, self.id, C.byref(lat), C.byref(que), C.byref(used))
+        _check(rc)
+        cig = self.cig[:used.value] if self.cig is not None else None
+        return self.res, cig, lat.value, que.value
+
+
+class Server:
+    """Continuous-batching serving engine (ksw2g_server_t): requests admitted by traceback
+    footprint against a fixed device budget, run concurrently on `slots` streams."""
+
+    def __init__(self, device=0, slots=8, tb_budget=40 << 30):
+        self.L = load_library()
+        h = C.c_void_p()
+        _check(self.L.ksw2g_server_create(device, slots, int(tb_budget), C.byref(h)))
+        self.h = h
+
+    def submit_ext(self, dual, m, mat, q, e, q2, e2, jobs, qbuf, tbuf):
+        jobs = np.ascontiguousarray(jobs, EXT_JOB)
+        qbuf, tbuf, mat = _u8(qbuf), _u8(tbuf), np.ascontiguousarray(mat, np.int8)
+        res = np.zeros(len(jobs), EXT_RESULT)
+        cap = int((jobs["qlen"].astype(np.int64) + jobs["tlen"] + 1).sum()) + 16
+        cig = np.zeros(cap, np.uint32)
+        rid = self.L.ksw2g_server_submit_ext(self.h, int(dual), m, _ptr(mat), q, e, q2, e2, len(jobs), _ptr(jobs),
+                                             _ptr(qbuf), len(qbuf), _ptr(tbuf), len(tbuf), _ptr(res), _ptr(cig), cap)
+        if rid < 0:
+            _check(int(rid))
+        return Request(self, rid, "ext", (jobs, qbuf, tbuf, mat), res, cig)
+
+    def submit_ll(self, size, m, mat, gapo, gape, jobs, qbuf, tbuf):
+        jobs = np.ascontiguousarray(jobs, LL_JOB)
+        qbuf, tbuf, mat = _u8(qbuf), _u8(tbuf), np.ascontiguousarray(mat, np.int8)
+        res = np.zeros(len(jobs), LL_RESULT)
+        rid = self.L.ksw2g_server_submit_ll(self.h, size, m, _ptr(mat), gapo, gape, len(jobs), _ptr(jobs),
+                                            _ptr(qbuf), len(qbuf), _ptr(tbuf), len(tbuf), _ptr(res))
+        if rid < 0:
+            _check(int(rid))
+        return Request(self, rid, "ll", (jobs, qbuf, tbuf, mat), res, None)
+
+    def stats(self):
+        a, d, p, b = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        _check(self.L.ksw2g_server_stats(self.h, C.byref(a), C.byref(d), C.byref(p), C.byref(b)))
+        return dict(admitted=a.value, done=d.value, peak_inflight=p.value, peak_pool_bytes=b.value)
+
+    def close(self):
+        if self.h:
+            self.L.ksw2g_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
