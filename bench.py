@@ -1,13 +1,19 @@
-"""Benchmark of the ksw2 extension hot path on GB300.
+"""Benchmark of the ksw2 extension / rescue hot path on GB300.
 
-Workload (N=1): 1,000,000 seeded extd2 (dual-affine) extension pairs with CIGAR,
-query 100-300 nt, target = query with 2% substitutions / 0.5% indels + 50 flanking bases,
-1% with a 200-nt junk query suffix, band w=100, zdrop=100, end_bonus=10.
-A step is one pass of DP + backtrack over all pairs.
+Default workload (N=1), the one the headline metric is quoted on: 1,000,000 seeded extd2
+(dual-affine) extension pairs with CIGAR, query 100-300 nt, target = query with 2%
+substitutions / 0.5% indels + 50 flanking bases, 1% with a 200-nt junk query suffix, band
+w=100, zdrop=100, end_bonus=10.  A step is one pass of DP + backtrack over all pairs.
 
-  value   alignments/s with the inputs resident in HBM (CUDA events on the library's stream)
-  e2e     the same metric through the C ABI one-shot batch call (ksw2g_ext_batch) with pinned
-          host buffers: H2D of sequences + jobs and D2H of results + CIGARs inside the timed step
+  value     alignments/s with the inputs resident in HBM (CUDA events on the library's stream)
+  e2e       the same metric through the C ABI one-shot batch call (ksw2g_ext_batch) with pinned
+            host buffers: H2D of sequences + jobs and D2H of results + CIGARs inside the timed step
+  roofline  the DP kernel alone: integer ops of the reference's SSE lane-op count per cell x cells,
+            over the DP launches' summed duration (CUDA events around every launch, on the
+            launching stream, during the timed steps); traffic = DRAM bytes per cell from ncu x cells
+
+Other workloads (--workload): cfg0 (20k extz2 pairs), cfg2 (200k long extd2 + 1M short extz2 in one
+CUDA graph, two branches), cfg3 (2M ksw_ll i16 rescue jobs).
 
 `--impl reference` times the reference's CPU implementation of the path on the host cores
 (oracle/_ref when the reference could be built here, else the scalar restatement in oracle/).
@@ -15,6 +21,7 @@ Under torchrun every rank runs its own replica of the workload (pairs are indepe
 collective); value is the sum over ranks divided by the max-over-ranks time.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -28,15 +35,31 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "alignments/s"
-UNIT = "aln/s"
-WORKLOAD = "cfg1: 1M extd2 extension pairs, 100-300 nt, w=100, CIGAR"
-# Lane operations the reference SSE code spends per nominal cell of ksw_extd2_sse with CIGAR
-# (ksw2_extd2_sse.c:30-58,226-265: 54 byte-lane ops per 16-byte block of 16 cells, plus 6 for the
-# substitution scores, extd2:157-172), and int32 lane ops of the exact max (extd2:326-341: 5 per
-# 4 cells).  One 32-bit instruction carries 4 byte lanes, so the algorithmic int32 work is
-# (54 + 6) / 4 + 5 / 4 = 16.25 instructions per cell.
-INT32_OPS_PER_CELL = (54 + 6) / 4 + 5 / 4
+# Lane operations the reference SSE code spends per nominal cell (one 32-bit instruction carries
+# four byte lanes or two 16-bit lanes):
+#  extd2 with CIGAR: 54 byte-lane ops per 16-cell block (ksw2_extd2_sse.c:183-265) + 6 for the
+#    substitution scores (extd2:157-172), and 6 int32 lane ops of the exact max (extd2:315-345);
+#  extz2 with CIGAR: 29 + 6 byte-lane ops (ksw2_extz2_sse.c:117-136,163-188) and 5 int32 (extz2:216-243);
+#  ksw_ll i16: 10 int16-lane ops per cell (ksw2_ll_sse.c:265-286), lazy-F passes not counted.
+OPS_PER_CELL = {
+    "extd2": (54 + 6) / 4 + 6 / 4,
+    "extz2": (29 + 6) / 4 + 5 / 4,
+    "ll_i16": 10 / 2,
+}
+# DRAM bytes per nominal cell of the DP kernel, from ncu (dram__bytes_read.sum + dram__bytes_write.sum
+# of one captured launch / its cells), scaled to the workload's launches by their cell counts.
+# extd2: 1,036,943,360 B over 674,520,661 cells (ext_dp_kernel<1,1,8,4>, 20,000 config-1 pairs);
+# ll_i16: 112,092,672 B over 11,259,234,900 cells (ll_dpx_kernel<2,24>, 100,000 config-3 jobs).
+# Both grow with the cells a launch processes (traceback rows and sequences), so they scale.
+DRAM_BYTES_PER_CELL = {"extd2": 1036943360 / 674520661, "extz2": None, "ll_i16": 112092672 / 11259234900}
+
+WORKLOADS = {
+    "cfg1": "cfg1: 1M extd2 extension pairs, 100-300 nt, w=100, CIGAR",
+    "cfg0": "cfg0: 20k extz2 extension pairs, 150 nt, w=25, CIGAR",
+    "cfg2": "cfg2: 200k long extd2 (log-normal median 2 kb, w=500) + 1M short extz2 (150 nt, w=25), "
+            "one CUDA graph, CIGAR",
+    "cfg3": "cfg3: 2M ksw_ll i16 rescue jobs, 150 nt vs 500-1000 nt",
+}
 
 
 def parse():
@@ -45,8 +68,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--pairs", type=int, default=1000000)
-    ap.add_argument("--cpu-sample", type=int, default=40000, help="pairs in the CPU baseline sample")
+    ap.add_argument("--workload", default="cfg1", choices=sorted(WORKLOADS))
+    ap.add_argument("--pairs", type=int, default=None, help="override the workload's unit count")
+    ap.add_argument("--cpu-sample", type=int, default=None, help="units in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -66,34 +90,40 @@ def barrier(world):
         dist.barrier()
 
 
-def allmax(x, world):
+def _reduce(x, world, op):
     if world > 1:
         import torch
         import torch.distributed as dist
         t = torch.tensor([float(x)], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=op)
         return float(t.item())
+    return float(x)
+
+
+def allmax(x, world):
+    if world > 1:
+        import torch.distributed as dist
+        return _reduce(x, world, dist.ReduceOp.MAX)
     return float(x)
 
 
 def allsum(x, world):
     if world > 1:
-        import torch
         import torch.distributed as dist
-        t = torch.tensor([float(x)], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        return float(t.item())
+        return _reduce(x, world, dist.ReduceOp.SUM)
     return float(x)
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """nvidia-smi clock / throttle samples during the timed region (started, and its first
+    sample awaited, before the region begins)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
         self.index, self.p, self.lines = index, None, []
+        self.first = threading.Event()
 
     def __enter__(self):
         try:
@@ -102,6 +132,7 @@ class ClockSampler:
                                       stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=5)
         except Exception:
             self.p = None
         return self
@@ -109,6 +140,7 @@ class ClockSampler:
     def _read(self):
         for ln in self.p.stdout:
             self.lines.append(ln.strip())
+            self.first.set()
 
     def __exit__(self, *a):
         if self.p:
@@ -138,39 +170,101 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(p, sample, reference_preferred=True):
-    """Time the CPU implementation on a bounded sample of the same pairs with all host threads."""
+# ------------------------------------------------------------------ workloads
+class Workload:
+    """The inputs of one benchmark configuration and how to run them."""
+
+    def __init__(self, name, args, rank):
+        from minibwa_gb300 import synth
+        self.name, self.desc = name, WORKLOADS[name]
+        seed_shift = rank * 1000
+        n = args.pairs
+        if name == "cfg1":
+            self.sets = [synth.config1(n or 1000000, seed=synth.SEED + 1 + seed_shift)]
+        elif name == "cfg0":
+            self.sets = [synth.config0(n or 20000, seed=synth.SEED + seed_shift)]
+        elif name == "cfg2":
+            nl = (n or 1200000) // 6
+            self.sets = [synth.config2_long(nl, seed=synth.SEED + 2 + seed_shift),
+                         synth.config2_short(nl * 5, seed=synth.SEED + 3 + seed_shift)]
+        else:
+            self.sets = [synth.config3(n or 2000000, seed=synth.SEED + 4 + seed_shift)]
+        self.ll = name == "cfg3"
+        self.metric = "jobs/s" if self.ll else "alignments/s"
+        self.unit = "jobs/s" if self.ll else "aln/s"
+        self.kind = "ll_i16" if self.ll else ("extd2" if self.sets[0].dual else "extz2")
+        self.n = sum(len(s) for s in self.sets)
+
+    def kernel_kinds(self):
+        return ["ll_i16" if self.ll else ("extd2" if s.dual else "extz2") for s in self.sets]
+
+
+def prepare(ctx, s):
+    from minibwa_gb300 import ExtBatch, LLBatch
+    if hasattr(s, "size"):
+        return LLBatch(ctx, s.size, 5, s.mat, s.gapo, s.gape, s.jobs, s.qbuf, s.tbuf)
+    return ExtBatch(ctx, s.dual, 5, s.mat, s.q, s.e, s.q2, s.e2, s.jobs, s.qbuf, s.tbuf)
+
+
+def cells_of(s, res):
+    if hasattr(s, "size"):
+        return int((res["rows"].astype(np.int64) * s.jobs["qlen"]).sum())
+    return int(res["cells"].sum())
+
+
+def cpu_baseline(w, sample, reference_preferred=True):
+    """Time the CPU implementation on a bounded sample of the same units with all host threads."""
     from oracle import oracle as O
     kind = "reference" if (reference_preferred and O.have_ref()) else "port"
+    which = "ref" if kind == "reference" else "orc"
     threads = os.cpu_count() or 1
-    sub = p.subset(np.arange(min(sample, len(p))))
-    t0 = time.perf_counter()
-    O.ext_batch("ref" if kind == "reference" else "orc", sub.dual, 5, sub.mat, sub.q, sub.e, sub.q2, sub.e2,
-                sub.jobs, sub.qbuf, sub.tbuf, threads)
+    # the sample keeps the workload's mix: the same fraction of every set
+    frac = min(1.0, sample / w.n)
+    n_done, t0 = 0, time.perf_counter()
+    for s in w.sets:
+        k = max(1, int(round(len(s) * frac)))
+        sub = s.subset(np.arange(k))
+        if hasattr(sub, "size"):
+            O.ll_batch(which, sub.size, 5, sub.mat, sub.gapo, sub.gape, sub.jobs, sub.qbuf, sub.tbuf, threads)
+        else:
+            O.ext_batch(which, sub.dual, 5, sub.mat, sub.q, sub.e, sub.q2, sub.e2, sub.jobs, sub.qbuf, sub.tbuf,
+                        threads)
+        n_done += k
     dt = time.perf_counter() - t0
-    return {"value": len(sub) / dt, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"first {len(sub)} pairs of the workload, {threads} threads, {dt:.2f} s wall"}, dt
+    return {"value": n_done / dt, "unit": w.unit, "cores": threads, "kind": kind,
+            "sample": f"first {n_done} units of the workload (same mix), {threads} threads, {dt:.2f} s wall"}, dt
+
+
+DEFAULT_SAMPLE = {"cfg1": 40000, "cfg0": 20000, "cfg2": 6000, "cfg3": 40000}
 
 
 def run_reference(args, rank, world):
-    from minibwa_gb300 import synth
     if rank != 0:
         return
-    p = synth.config1(max(args.cpu_sample, 1000))
+    w = Workload(args.workload, args, 0) if args.workload != "cfg1" else None
+    if w is None:
+        from minibwa_gb300 import synth
+
+        class _W:
+            pass
+        w = _W()
+        w.sets = [synth.config1(max(args.cpu_sample or DEFAULT_SAMPLE["cfg1"], 1000))]
+        w.n, w.unit, w.metric, w.desc = len(w.sets[0]), "aln/s", "alignments/s", WORKLOADS["cfg1"]
+    sample = args.cpu_sample or DEFAULT_SAMPLE[args.workload]
     for _ in range(args.warmup):
-        cpu_baseline(p, min(args.cpu_sample, 2000))
-    vals, times = [], []
+        cpu_baseline(w, max(1, sample // 20))
+    times = []
     for _ in range(args.steps):
-        cb, dt = cpu_baseline(p, args.cpu_sample)
-        vals.append(cb["value"])
+        cb, dt = cpu_baseline(w, sample)
         times.append(dt)
-    v = len(times) * args.cpu_sample / sum(times)
+    v = len(times) * sample / sum(times)
     cb["value"] = v
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": w.metric, "value": v, "unit": w.unit, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8",
-            "data": "synthetic (seeded splitmix64)", "config": {"workload": WORKLOAD, "pairs_per_step": args.cpu_sample},
-            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int16" if args.workload == "cfg3" else "int8",
+            "data": "synthetic (seeded splitmix64)", "config": {"workload": w.desc, "units_per_step": sample},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": w.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -181,82 +275,122 @@ def main():
         run_reference(args, rank, world)
         return
     import torch
-    from minibwa_gb300 import Context, ExtBatch, synth
+    from minibwa_gb300 import Context, Graph
     from minibwa_gb300 import lib as K
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    K.load_library()
-    p = synth.config1(args.pairs, seed=synth.SEED + 1 + rank * 1000)
-    n = len(p)
+    L = K.load_library()
+    w = Workload(args.workload, args, rank)
     ctx = Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
 
     # ---------------- value: resident inputs, device timing
-    b = ExtBatch(ctx, p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf)
+    batches = [prepare(ctx, s) for s in w.sets]
+    graph = Graph(ctx, batches) if len(batches) > 1 else None
+
+    def step():
+        if graph is not None:
+            graph.launch()
+        else:
+            batches[0].run()
+
     for _ in range(args.warmup):
-        b.run()
+        step()
     ctx.sync()
-    res, cig = b.fetch()
-    cells = int(res["cells"].sum())
-    diags = res["n_diag"].astype(np.int64)
+    results = [b.fetch() for b in batches]
+    res_list = [r if w.ll else r[0] for r in results]
+    cells = [cells_of(s, r) for s, r in zip(w.sets, res_list)]
+    if graph is None:
+        batches[0].set_timing(True)
     barrier(world)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
         e0.record(stream)
         for _ in range(args.steps):
-            b.run()
+            step()
         e1.record(stream)
         ctx.sync()
     torch.cuda.synchronize()
     barrier(world)
     ms = e0.elapsed_time(e1) / args.steps
-    launches_per_step = b.launches
+    launches_per_step = graph.launches if graph is not None else batches[0].launches
     ms_max = allmax(ms, world)
-    tot_pairs = allsum(n, world)
-    value = tot_pairs / (ms_max * 1e-3)
+    tot = allsum(w.n, world)
+    value = tot / (ms_max * 1e-3)
+    tot_cells = sum(cells)
 
-    # dominant kernel alone (the DP launch of the single bin), for the roofline
-    # the batch of one bin = one DP kernel + one backtrack kernel per wave; time DP share via a DP-only clone
+    # ---------------- roofline of the dominant kernel (the DP kernel)
     int_peak = K.probe_int32_peak(dev)
-    achieved_int = cells * INT32_OPS_PER_CELL / (ms * 1e-3)
-    # algorithmic HBM bytes per pair: traceback rows written once + read back along the path,
-    # inputs, result, CIGAR (SURVEY formula)
-    ncol = ((np.minimum(np.minimum(p.jobs["qlen"], p.jobs["tlen"]), 101) + 15) // 16 + 1).astype(np.int64)
-    tb_bytes = int((diags * ncol * 16).sum())
-    in_bytes = int(p.jobs["qlen"].sum() + p.jobs["tlen"].sum())
-    path_bytes = in_bytes
-    alg_bytes = tb_bytes + path_bytes + in_bytes + 4 * int(res["n_cigar"].sum()) + 64 * n
+    kinds = w.kernel_kinds()
+    ops = sum(c * OPS_PER_CELL[k] for c, k in zip(cells, kinds))
+    n_dp = 1
+    if graph is None:
+        dp_ms, bt_ms, n_dp, n_bt = batches[0].kernel_ms()
+        n_dp = max(1, n_dp // args.steps)
+        dp_ms_step = dp_ms / args.steps
+        kernel_note = (f"DP kernel: {n_dp} launches per step, {dp_ms_step:.2f} ms per step "
+                       f"(backtrack {bt_ms / args.steps:.2f} ms), CUDA events around each launch")
+    else:
+        dp_ms_step = ms  # branches overlap inside the graph: the whole graph is the timed unit
+        kernel_note = "whole graph (DP branches overlap); CUDA events around each graph launch"
+    achieved = ops / (dp_ms_step * 1e-3)
+    bpc = [DRAM_BYTES_PER_CELL.get(k) for k in kinds]
+    # per DP launch (per graph launch for a graph), like achieved
+    traffic = sum(c * b for c, b in zip(cells, bpc)) / n_dp if all(b is not None for b in bpc) else None
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    # algorithmic HBM bytes per step (traceback rows written once and read along the path,
+    # inputs, results and CIGARs)
+    alg_bytes = 0
+    for s, r in zip(w.sets, res_list):
+        if hasattr(s, "size"):
+            alg_bytes += int(s.jobs["qlen"].sum() + s.jobs["tlen"].sum()) + 24 * len(s)
+        else:
+            jq, jt = s.jobs["qlen"].astype(np.int64), s.jobs["tlen"].astype(np.int64)
+            ww = np.where(s.jobs["w"] < 0, np.maximum(jq, jt), s.jobs["w"]).astype(np.int64)
+            ncol = (np.minimum(np.minimum(jq, jt), ww + 1) + 15) // 16 + 1
+            tb = int((r["n_diag"].astype(np.int64) * ncol * 16).sum())
+            alg_bytes += tb + 2 * int(jq.sum() + jt.sum()) + 4 * int(r["n_cigar"].sum()) + 64 * len(s)
     achieved_gbs = alg_bytes / (ms * 1e-3) / 1e9
 
-    # ---------------- e2e through the C ABI with pinned host buffers
+    # ---------------- e2e through the C ABI one-shot calls with pinned host buffers
     def pinned(a):
-        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
-        t.numpy()[:] = a.view(np.uint8).reshape(-1)
+        t = torch.empty(max(1, a.nbytes), dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:a.nbytes] = a.view(np.uint8).reshape(-1)
         return t
 
-    jobs_h, q_h, t_h = pinned(p.jobs), pinned(p.qbuf), pinned(p.tbuf)
-    res_h = torch.empty(n * K.EXT_RESULT.itemsize, dtype=torch.uint8, pin_memory=True)
-    cap = int((p.jobs["qlen"].astype(np.int64) + p.jobs["tlen"] + 1).sum()) + 16
-    cig_h = torch.empty(cap * 4, dtype=torch.uint8, pin_memory=True)
-    import ctypes as C
-    L = K.load_library()
-    used = C.c_int64()
+    host = []
+    for s in w.sets:
+        d = {"jobs": pinned(s.jobs), "q": pinned(s.qbuf), "t": pinned(s.tbuf)}
+        if hasattr(s, "size"):
+            d["res"] = torch.empty(len(s) * K.LL_RESULT.itemsize, dtype=torch.uint8, pin_memory=True)
+        else:
+            d["res"] = torch.empty(len(s) * K.EXT_RESULT.itemsize, dtype=torch.uint8, pin_memory=True)
+            d["cap"] = int((s.jobs["qlen"].astype(np.int64) + s.jobs["tlen"] + 1).sum()) + 16
+            d["cig"] = torch.empty(d["cap"] * 4, dtype=torch.uint8, pin_memory=True)
+        host.append(d)
+    used = [C.c_int64() for _ in w.sets]
 
     def e2e_step():
-        rc = L.ksw2g_ext_batch(ctx.h, int(p.dual), 5, p.mat.ctypes.data, p.q, p.e, p.q2, p.e2, n,
-                               jobs_h.data_ptr(), q_h.data_ptr(), len(p.qbuf), t_h.data_ptr(), len(p.tbuf),
-                               res_h.data_ptr(), cig_h.data_ptr(), cap, C.byref(used))
-        if rc != 0:
-            raise RuntimeError(L.ksw2g_last_error().decode())
+        for s, d, u in zip(w.sets, host, used):
+            if hasattr(s, "size"):
+                rc = L.ksw2g_ll_batch(ctx.h, s.size, 5, s.mat.ctypes.data, s.gapo, s.gape, len(s),
+                                      d["jobs"].data_ptr(), d["q"].data_ptr(), len(s.qbuf), d["t"].data_ptr(),
+                                      len(s.tbuf), d["res"].data_ptr())
+            else:
+                rc = L.ksw2g_ext_batch(ctx.h, int(s.dual), 5, s.mat.ctypes.data, s.q, s.e, s.q2, s.e2, len(s),
+                                       d["jobs"].data_ptr(), d["q"].data_ptr(), len(s.qbuf), d["t"].data_ptr(),
+                                       len(s.tbuf), d["res"].data_ptr(), d["cig"].data_ptr(), d["cap"],
+                                       C.byref(u))
+            if rc != 0:
+                raise RuntimeError(L.ksw2g_last_error().decode())
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, min(args.warmup, 2))):
         e2e_step()
     barrier(world)
     torch.cuda.synchronize()
@@ -266,45 +400,52 @@ def main():
     torch.cuda.synchronize()
     e2e_s = allmax((time.perf_counter() - t0) / args.steps, world)
     barrier(world)
-    e2e_value = tot_pairs / e2e_s
-    # sanity: the e2e results equal the resident-run results
-    r2 = np.frombuffer(res_h.numpy().tobytes(), K.EXT_RESULT)
-    assert np.array_equal(r2["max"], res["max"]) and np.array_equal(r2["n_cigar"], res["n_cigar"])
-    h2d = len(p.qbuf) + len(p.tbuf) + p.jobs.nbytes
-    d2h = res.nbytes + 4 * int(used.value)
+    e2e_value = tot / e2e_s
+    # the e2e results equal the resident-run results
+    h2d = d2h = 0
+    for s, d, r, u in zip(w.sets, host, res_list, used):
+        dt = K.LL_RESULT if hasattr(s, "size") else K.EXT_RESULT
+        r2 = np.frombuffer(d["res"].numpy().tobytes(), dt)
+        assert np.array_equal(r2["score"], r["score"])
+        h2d += len(s.qbuf) + len(s.tbuf) + s.jobs.nbytes
+        d2h += r.nbytes + 4 * int(u.value)
 
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb, _ = cpu_baseline(p, args.cpu_sample)
+        cb, _ = cpu_baseline(w, args.cpu_sample or DEFAULT_SAMPLE[args.workload])
 
     if rank == 0:
+        l2note = ("inputs and traceback rows (%.1f GB per step) exceed the 129 MB L2" % (alg_bytes / 1e9))
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": w.metric, "value": value, "unit": w.unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int8", "data": "synthetic (seeded splitmix64, no public dataset)",
-            "config": {"workload": WORKLOAD, "pairs_per_gpu": n, "kernel": "extd2 left-aligned with CIGAR",
-                       "l2": "inputs (%.0f MB arena) and traceback rows (%.1f GB per step) exceed the 129 MB L2"
-                             % ((in_bytes + 128 * n) / 1e6, tb_bytes / 1e9),
-                       "parallelism": f"replicas x{world}"},
-            "gcups": cells / (ms * 1e-3) / 1e9,
-            "cells_per_step": cells,
+            "vs_baseline": None, "dtype": "int16" if w.ll else "int8",
+            "data": "synthetic (seeded splitmix64, no public dataset)",
+            "config": {"workload": w.desc, "units_per_gpu": w.n, "l2": l2note, "parallelism": f"replicas x{world}",
+                       "graph": graph is not None},
+            "gcups": tot_cells / (ms * 1e-3) / 1e9,
+            "cells_per_step": tot_cells,
             "gpu_launches": launches_per_step * args.steps,
-            "roofline": {"bound": "int", "achieved": achieved_int / 1e12, "peak": int_peak / 1e12,
-                         "unit": "Tops/s", "frac": achieved_int / int_peak, "traffic": None,
-                         "ops_per_cell": INT32_OPS_PER_CELL,
+            "roofline": {"bound": "int", "achieved": achieved / 1e12, "peak": int_peak / 1e12, "unit": "Tops/s",
+                         "frac": achieved / int_peak, "traffic": traffic,
+                         "ops_per_cell": {k: OPS_PER_CELL[k] for k in sorted(set(kinds))},
+                         "kernel": kernel_note,
                          "peak_source": "measured in-bench: IADD3+LOP3 chains on every SM (MEASURED_PEAKS.json "
                                         "has no integer figure)"},
             "roofline_hbm": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                              "frac": achieved_gbs / hbm_peak, "algorithmic_bytes_per_step": alg_bytes,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": e2e_s * 1e3},
             "clocks": clk.summary(),
         }
         if cb:
             line["cpu_baseline"] = cb
         print(json.dumps(line), flush=True)
-    b.free()
+    if graph is not None:
+        graph.close()
+    for b in batches:
+        b.free()
     ctx.close()
 
 

@@ -97,6 +97,27 @@ int ksw2g_ll_fetch(ksw2g_ctx_t *ctx, ksw2g_batch_t *batch, ksw2g_ll_result_t *re
 /* Kernel launches the last run of this batch enqueued. */
 int ksw2g_batch_launches(const ksw2g_batch_t *batch);
 void ksw2g_batch_free(ksw2g_batch_t *batch);
+/* Per-kernel timing of a batch's runs: with timing on, every kernel of a run is
+ * bracketed by CUDA events on the launching stream.  ksw2g_batch_kernel_ms
+ * waits for the runs and returns the DP-kernel and backtrack-kernel time (sums
+ * over all launches since timing was last switched on) and the launch counts.
+ * Off by default; not for batches captured in a graph. */
+int ksw2g_batch_set_timing(ksw2g_batch_t *batch, int on);
+int ksw2g_batch_kernel_ms(ksw2g_batch_t *batch, double *dp_ms, double *bt_ms, int *n_dp, int *n_bt);
+
+/* ---- CUDA graphs: one launch runs several prepared batches concurrently ----
+ * Captures the kernels of n prepared batches (extension or ll) into one CUDA
+ * graph.  Each batch is a branch of the graph, so the batches run
+ * concurrently; each extension batch gets its own traceback region, sized for
+ * its largest wave.  ksw2g_graph_launch enqueues the whole graph on ctx's
+ * stream; the results are read with ksw2g_ext_fetch / ksw2g_ll_fetch, as after
+ * ksw2g_batch_run.  The batches must stay alive, and must not be prepared
+ * again, while the graph exists. */
+typedef struct ksw2g_graph ksw2g_graph_t;
+int ksw2g_graph_create(ksw2g_ctx_t *ctx, int n_batches, ksw2g_batch_t *const *batches, ksw2g_graph_t **graph);
+int ksw2g_graph_launch(ksw2g_ctx_t *ctx, ksw2g_graph_t *graph);
+int ksw2g_graph_launches(const ksw2g_graph_t *graph);  /* kernel launches in one graph launch */
+void ksw2g_graph_destroy(ksw2g_graph_t *graph);
 
 /* Select the thread-group shape used for extension jobs whose reference
  * n_col_ (16-byte blocks per anti-diagonal) lies in [ncol_lo, ncol_hi];

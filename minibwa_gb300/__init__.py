@@ -20,6 +20,7 @@ from .lib import (  # noqa: F401
     KSW_LL_STOP,
     KSW_LL_SUBO,
     Context,
+    Graph,
     Server,
     ExtBatch,
     LLBatch,

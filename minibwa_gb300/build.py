@@ -56,6 +56,7 @@ def build(verbose=False, force=False):
         ("probe.cu", "probe.o", []),
         ("noalloc.cu", "noalloc.o", []),
         ("server.cu", "server.o", []),
+        ("graph.cu", "graph.o", []),
     ]
     hdrs = _headers()
     procs, objs = [], []

@@ -100,6 +100,11 @@ struct ksw2g_batch {
   std::vector<Wave> waves;
   int launches = 0;
   int64_t total_cells_hint = 0;
+  // optional per-launch timing: an event pair around every kernel of a run
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;  // 2 per timed launch
+  std::vector<int> tkind;        // 0 DP kernel, 1 backtrack kernel, per timed launch
+  int n_timed = 0;
 };
 
 

@@ -126,9 +126,34 @@ extern "C" void ksw2g_batch_free(ksw2g_batch_t *b) {
   for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts, &b->cigar,
                     &b->counters, &b->llmat, &b->blist, &b->blist_off})
     d->release();
+  for (cudaEvent_t e : b->tev) cudaEventDestroy(e);
   delete b;
 }
 extern "C" int ksw2g_batch_launches(const ksw2g_batch_t *b) { return b ? b->launches : 0; }
+
+extern "C" int ksw2g_batch_set_timing(ksw2g_batch_t *b, int on) {
+  if (!b) return set_err(KSW2G_E_ARG, "null batch");
+  b->timing = on != 0;
+  b->n_timed = 0;
+  return 0;
+}
+
+extern "C" int ksw2g_batch_kernel_ms(ksw2g_batch_t *b, double *dp_ms, double *bt_ms, int *n_dp, int *n_bt) {
+  if (!b) return set_err(KSW2G_E_ARG, "null batch");
+  double t[2] = {0, 0};
+  int c[2] = {0, 0};
+  for (int i = 0; i < b->n_timed; ++i) {
+    float ms = 0;
+    CK(cudaEventSynchronize(b->tev[2 * i + 1]));
+    CK(cudaEventElapsedTime(&ms, b->tev[2 * i], b->tev[2 * i + 1]));
+    t[b->tkind[i]] += ms, ++c[b->tkind[i]];
+  }
+  if (dp_ms) *dp_ms = t[0];
+  if (bt_ms) *bt_ms = t[1];
+  if (n_dp) *n_dp = c[0];
+  if (n_bt) *n_bt = c[1];
+  return 0;
+}
 
 // Upload raw sequences and pack them into the padded arena.  Writes the padded
 // offsets of query s and target s to qpad[s], tpad[s].
@@ -290,6 +315,28 @@ extern "C" int ksw2g_ext_prepare(ksw2g_ctx_t *c, int dual, int8_t m, const int8_
   return 0;
 }
 
+// Per-launch timing (ksw2g_batch_set_timing): an event pair on the launching
+// stream around each kernel.
+static cudaError_t timed_begin(ksw2g_batch *b, int kind, cudaStream_t st) {
+  if (!b->timing) return cudaSuccess;
+  const size_t need = 2 * (size_t)(b->n_timed + 1);
+  while (b->tev.size() < need) {
+    cudaEvent_t e;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return r;
+    b->tev.push_back(e);
+  }
+  if (b->tkind.size() < (size_t)b->n_timed + 1) b->tkind.resize(b->n_timed + 1);
+  b->tkind[b->n_timed] = kind;
+  return cudaEventRecord(b->tev[2 * b->n_timed], st);
+}
+static cudaError_t timed_end(ksw2g_batch *b, cudaStream_t st) {
+  if (!b->timing) return cudaSuccess;
+  const cudaError_t r = cudaEventRecord(b->tev[2 * b->n_timed + 1], st);
+  ++b->n_timed;
+  return r;
+}
+
 int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap) {
   b->launches = 0;
   if (b->n == 0) return 0;
@@ -311,12 +358,16 @@ int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap) {
     for (auto &bn : wv.bins) {
       ExtLaunch L{dj, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr, db, tb, dto,
                   jc + ci++};
+      CK(timed_begin(b, 0, st));
       CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, st));
+      CK(timed_end(b, st));
       ++b->launches;
     }
     if (wv.any_cig) {
+      CK(timed_begin(b, 1, st));
       CK(launch_ext_bt(dj, dsrt + wv.w0, wv.w1 - wv.w0, db, tb, dto, dr,
                        b->cigar.as<uint32_t>(), cursor, (long long)b->cigar_cap, err, st));
+      CK(timed_end(b, st));
       ++b->launches;
     }
   }
@@ -590,7 +641,9 @@ int ll_run_on(ksw2g_batch *b, cudaStream_t st) {
   LLLaunch L{b->jobs.as<ksw2g_ll_job>(), b->n, b->arena.as<uint8_t>(), b->llmat.as<int8_t>(), b->ll_m, b->ll_gapo,
              b->ll_gape, b->res.as<ksw2g_ll_result>(), b->blist.as<uint64_t>(), b->blist_off.as<int64_t>(),
              b->counters.as<int>(), b->ll_qlen_max, b->ll_mat_max};
+  CK(timed_begin(b, 0, st));
   CK(launch_ll(b->ll_size, b->ll_slen, L, 0, st, b->ll_force));
+  CK(timed_end(b, st));
   ++b->launches;
   return 0;
 }

@@ -97,6 +97,13 @@ def load_library():
         "ksw2g_ext_shape_info": (i32, [i32, C.POINTER(i32), C.POINTER(i32)]),
         "ksw2g_ext_set_shape": (i32, [i32, i32, i32, i32, i32]),
         "ksw2g_probe_int32_peak": (i32, [i32, C.POINTER(C.c_double)]),
+        "ksw2g_batch_set_timing": (i32, [vp, i32]),
+        "ksw2g_batch_kernel_ms": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(i32),
+                                        C.POINTER(i32)]),
+        "ksw2g_graph_create": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
+        "ksw2g_graph_launch": (i32, [vp, vp]),
+        "ksw2g_graph_launches": (i32, [vp]),
+        "ksw2g_graph_destroy": (None, [vp]),
         "ksw2g_server_create": (i32, [i32, i32, i64, C.POINTER(vp)]),
         "ksw2g_server_destroy": (None, [vp]),
         "ksw2g_server_submit_ext": (i64, [vp, i32, i8, vp, i8, i8, i8, i8, i32, vp, u8p, i64, u8p, i64, vp, vp, i64]),
@@ -281,6 +288,16 @@ class _Batch:
     def launches(self):
         return self.L.ksw2g_batch_launches(self.h)
 
+    def set_timing(self, on=True):
+        _check(self.L.ksw2g_batch_set_timing(self.h, int(on)))
+
+    def kernel_ms(self):
+        """(DP-kernel ms, backtrack-kernel ms, DP launches, backtrack launches), summed over the runs
+        since set_timing(True)."""
+        dp, bt, ndp, nbt = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+        _check(self.L.ksw2g_batch_kernel_ms(self.h, C.byref(dp), C.byref(bt), C.byref(ndp), C.byref(nbt)))
+        return dp.value, bt.value, ndp.value, nbt.value
+
     def free(self):
         if self.h:
             self.L.ksw2g_batch_free(self.h)
@@ -326,6 +343,35 @@ class LLBatch(_Batch):
         res = res if res is not None else np.zeros(self.n, LL_RESULT)
         _check(self.L.ksw2g_ll_fetch(self.ctx.h, self.h, _ptr(res)))
         return res
+
+
+class Graph:
+    """One CUDA graph over several prepared batches (ksw2g_graph_t); every batch is a branch,
+    so one launch runs them all concurrently.  Fetch results from the batches afterwards."""
+
+    def __init__(self, ctx, batches):
+        self.L, self.ctx, self.batches = ctx.L, ctx, list(batches)
+        arr = (C.c_void_p * len(self.batches))(*[b.h.value for b in self.batches])
+        self.h = C.c_void_p()
+        _check(self.L.ksw2g_graph_create(ctx.h, len(self.batches), arr, C.byref(self.h)))
+
+    @property
+    def launches(self):
+        return self.L.ksw2g_graph_launches(self.h)
+
+    def launch(self):
+        _check(self.L.ksw2g_graph_launch(self.ctx.h, self.h))
+
+    def close(self):
+        if self.h:
+            self.L.ksw2g_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Request:
