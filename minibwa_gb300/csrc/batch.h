@@ -74,6 +74,10 @@ struct ksw2g_ctx {
   DevBuf one;           // per-call drop-in scratch (device)
   PinBuf one_h;         // per-call drop-in staging (pinned)
   ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
+  // two sub-contexts (own stream and traceback pool, half the budget each) that the
+  // one-shot extension call alternates between, so the host prepares one chunk
+  // while the device runs the previous one
+  ksw2g_ctx *sub[2] = {nullptr, nullptr};
 };
 
 // ---------------------------------------------------------------- batches

@@ -103,6 +103,8 @@ extern "C" void ksw2g_ctx_destroy(ksw2g_ctx_t *c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->st);
   if (c->scratch) ksw2g_batch_free(c->scratch);
+  for (ksw2g_ctx *sc : c->sub)
+    if (sc) ksw2g_ctx_destroy(sc);
   c->tb_pool.release();
   c->one.release();
   c->one_h.release();
@@ -415,11 +417,114 @@ extern "C" int ksw2g_ext_fetch(ksw2g_ctx_t *c, ksw2g_batch_t *b, ksw2g_ext_resul
   return 0;
 }
 
+// One-shot extension batches of more than kChunkJobs jobs run as chunks that
+// alternate between two sub-contexts: while the device runs chunk i, the host
+// prepares chunk i+1 (job table, wave plan, uploads) on the other stream.
+// Each chunk's CIGARs are appended to the caller's buffer as the chunk
+// completes, and its results' cigar_off are shifted to match.
+static const int kChunkJobs = 131072;
+
+static int sub_ctx(ksw2g_ctx *c, int i, ksw2g_ctx **out) {
+  if (!c->sub[i]) {
+    int rc = ksw2g_ctx_create(c->device, &c->sub[i]);
+    if (rc) return rc;
+    c->sub[i]->scratch = new ksw2g_batch;
+  }
+  c->sub[i]->tb_budget = std::max<int64_t>(c->tb_budget / 2, 1 << 20);
+  *out = c->sub[i];
+  return 0;
+}
+
+static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e, int8_t q2,
+                             int8_t e2, int n, const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+                             const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ext_result_t *res, uint32_t *cigar,
+                             int64_t cigar_cap, int64_t *cigar_used) {
+  const int nch = (n + kChunkJobs - 1) / kChunkJobs;
+  const int per = (n + nch - 1) / nch;
+  ksw2g_ctx *sc[2];
+  int rc;
+  for (int i = 0; i < 2; ++i)
+    if ((rc = sub_ctx(c, i, &sc[i]))) return rc;
+  int64_t used = 0;
+  int pending[2] = {-1, -1};  // chunk index in flight on each sub-context
+  auto finish = [&](int s) -> int {
+    const int ch = pending[s];
+    if (ch < 0) return 0;
+    pending[s] = -1;
+    ksw2g_ctx *x = sc[s];
+    ksw2g_batch *b = x->scratch;
+    const int j0 = ch * per;
+    struct {
+      unsigned long long cursor;
+      int err, pad;
+    } hdr = {0, 0, 0};
+    CK(cudaMemcpyAsync(&hdr, b->counters.p, sizeof hdr, cudaMemcpyDeviceToHost, x->st));
+    CK(cudaStreamSynchronize(x->st));  // the chunk's results are in res by now
+    if (hdr.err) return set_err(KSW2G_E_CAPACITY, "device CIGAR arena overflow");
+    if (hdr.cursor) {
+      if (!cigar || used + (int64_t)hdr.cursor > cigar_cap)
+        return set_err(KSW2G_E_CAPACITY, "CIGAR buffer holds %lld words, more needed", (long long)cigar_cap);
+      CK(cudaMemcpyAsync(cigar + used, b->cigar.p, sizeof(uint32_t) * hdr.cursor, cudaMemcpyDeviceToHost, x->st));
+      if (res)
+        for (int i = 0; i < b->n; ++i) res[j0 + i].cigar_off += used;
+      used += (int64_t)hdr.cursor;
+      CK(cudaStreamSynchronize(x->st));
+    }
+    return 0;
+  };
+  for (int ch = 0; ch < nch && !rc; ++ch) {
+    const int s = ch & 1;
+    if ((rc = finish(s))) break;
+    const int j0 = ch * per, nj = std::min(per, n - j0);
+    ksw2g_ctx *x = sc[s];
+    ksw2g_batch *b = x->scratch;
+    // upload only the part of the sequence buffers this chunk's jobs read
+    int64_t qlo = qbuf_len, qhi = 0, tlo = tbuf_len, thi = 0;
+    for (int i = j0; i < j0 + nj; ++i) {
+      const ksw2g_job_t &J = jobs[i];
+      if (J.qoff < 0 || J.toff < 0 || J.qlen < 0 || J.tlen < 0 || J.qoff + J.qlen > qbuf_len ||
+          J.toff + J.tlen > tbuf_len) {
+        rc = set_err(KSW2G_E_ARG, "job %d: sequence out of buffer bounds", i);
+        break;
+      }
+      qlo = std::min(qlo, J.qoff), qhi = std::max<int64_t>(qhi, J.qoff + J.qlen);
+      tlo = std::min(tlo, J.toff), thi = std::max<int64_t>(thi, J.toff + J.tlen);
+    }
+    if (rc) break;
+    if (qlo > qhi) qlo = qhi = 0;
+    if (tlo > thi) tlo = thi = 0;
+    std::vector<ksw2g_job_t> cj(jobs + j0, jobs + j0 + nj);
+    for (auto &J : cj) J.qoff -= qlo, J.toff -= tlo;
+    if ((rc = ext_prepare_into(x, b, dual, m, mat, q, e, q2, e2, nj, cj.data(), qbuf + qlo, qhi - qlo, tbuf + tlo,
+                               thi - tlo)))
+      break;
+    if ((rc = ext_run(x, b))) break;
+    if (res && nj)
+      CK(cudaMemcpyAsync(res + j0, b->res.p, sizeof(ksw2g_ext_result) * nj, cudaMemcpyDeviceToHost, x->st));
+    pending[s] = ch;
+  }
+  // drain in chunk order (the CIGAR buffer is filled in chunk order)
+  for (int k = 0; k < 2 && !rc; ++k) {
+    int s = pending[0] >= 0 && (pending[1] < 0 || pending[0] < pending[1]) ? 0 : 1;
+    rc = finish(s);
+  }
+  if (rc) {
+    for (int s = 0; s < 2; ++s) cudaStreamSynchronize(sc[s]->st);
+    return rc;
+  }
+  if (cigar_used) *cigar_used = used;
+  return 0;
+}
+
 extern "C" int ksw2g_ext_batch(ksw2g_ctx_t *c, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
                                int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs, const uint8_t *qbuf,
                                int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ext_result_t *res,
                                uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used) {
   if (!c) return set_err(KSW2G_E_ARG, "null ctx");
+  CK(cudaSetDevice(c->device));
+  if (n_jobs > kChunkJobs)
+    return ext_batch_chunked(c, dual, m, mat, q, e, q2, e2, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len, res, cigar,
+                             cigar_cap, cigar_used);
   if (!c->scratch) c->scratch = new ksw2g_batch;
   int rc = ext_prepare_into(c, c->scratch, dual, m, mat, q, e, q2, e2, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len);
   if (rc) return rc;

@@ -459,8 +459,11 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           const int32_t gmax = __reduce_max_sync(gm, lmax);
           // tie-break of the reference: en0 first, then four int32 lanes over
           // [st0, en1) (lowest lane, then lowest t), then the scalar tail [en1, en0)
+          // The position of the maximum is used only when this anti-diagonal sets a new
+          // maximum or may z-drop (ksw_apply_zdrop, ksw2.h:181-197); otherwise it is skipped.
+          const bool need_mt = ez_e < 0 || gmax > ez_max || (zdrop >= 0 && ez_max - gmax > zdrop);
           uint32_t key = 0xffffffffu;
-          if (lmax == gmax) {
+          if (need_mt && lmax == gmax) {
             const int en1 = st0 + (((en0 - st0) >> 2) << 2);
 #pragma unroll
             for (int i = 0; i < K; ++i) {
@@ -479,7 +482,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               }
             }
           }
-          key = __reduce_min_sync(gm, key);
+          if (need_mt) key = __reduce_min_sync(gm, key);
           const int32_t max_H = gmax;
           const int mt = key == 0 ? en0 : st0 + (int)(key & 0xffffffu);
           if (en0 == tlen - 1 && Hen0 > mte) mte = Hen0, mte_q = r - en0;
@@ -491,7 +494,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           // ksw_apply_zdrop (ksw2.h:181-197)
           if (max_H > ez_max) {
             ez_max = max_H, max_t = mt, max_q = r - mt;
-          } else if (mt >= max_t && r - mt >= max_q) {
+          } else if (need_mt && mt >= max_t && r - mt >= max_q) {
             const int tl = mt - max_t, ql = (r - mt) - max_q, l = tl > ql ? tl - ql : ql - tl;
             if (zdrop >= 0 && ez_max - max_H > zdrop + l * ez_e) zdropped = 1, done = true;
           }

@@ -198,6 +198,7 @@ inline uint32_t map16(uint32_t a, uint32_t b, uint32_t c, F f) {
 inline uint32_t __vadd2(uint32_t a, uint32_t b) {
   return emu::map16(a, b, 0, [](int x, int y, int) { return (int16_t)(x + y); });
 }
+inline int __vimax3_s32(int a, int b, int c) { return std::max(a, std::max(b, c)); }
 inline uint32_t __vmaxs2(uint32_t a, uint32_t b) {
   return emu::map16(a, b, 0, [](int x, int y, int) { return x > y ? x : y; });
 }

@@ -212,3 +212,31 @@ def test_full_size_config1_properties(ctx):
             assert ql == p.jobs["qlen"][i] and tl == r1["mqe_t"][i] + 1
         else:
             assert ql == r1["max_q"][i] + 1 and tl == r1["max_t"][i] + 1
+
+
+def test_one_shot_chunked_equals_resident(built):
+    """One-shot batches above the chunk size run as overlapped chunks on two streams; every
+    result and CIGAR equals the resident single-launch run of the same jobs."""
+    from minibwa_gb300 import Context, ExtBatch, synth
+    from conftest import EXT_FIELDS
+    p = synth.config0(300000, seed=77)
+    ctx = Context(0)
+    res, cig = ctx.ext_batch(p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf)
+    b = ExtBatch(ctx, p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf)
+    b.run()
+    want, wcig = b.fetch()
+    b.free()
+    ctx.close()
+    for f in EXT_FIELDS:
+        assert np.array_equal(res[f], want[f]), f
+    assert len(cig) == len(wcig)
+    for i in range(0, len(p), 997):
+        o, n = int(res["cigar_off"][i]), int(res["n_cigar"][i])
+        wo = int(want["cigar_off"][i])
+        assert np.array_equal(cig[o:o + n], wcig[wo:wo + n]), i
+    # the CIGARs tile the used part of the buffer without overlap
+    live = res["n_cigar"] > 0
+    o = res["cigar_off"][live].astype(np.int64)
+    n = res["n_cigar"][live].astype(np.int64)
+    k = np.argsort(o, kind="stable")
+    assert (o[k][1:] >= o[k][:-1] + n[k][:-1]).all() and o[k][-1] + n[k][-1] <= len(cig)
