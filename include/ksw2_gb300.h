@@ -164,8 +164,9 @@ int ksw2g_ext_noalloc(int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
  * Requests are admitted in arrival order as soon as one of n_slots slots is
  * free and the request's traceback rows (the reference's footprint,
  * ksw2_extz2_sse.c:84, summed over its jobs) fit in the tb_budget bytes of
- * device memory the engine owns.  Admitted requests run concurrently on the
- * slots' streams.  The caller's buffers (jobs, sequences, results, CIGAR) must
+ * device memory the engine owns; queued requests of the same kind and
+ * scoring scheme join the admitted request's launch.  Admitted requests run
+ * concurrently on the slots' streams.  The caller's buffers (jobs, sequences, results, CIGAR) must
  * stay valid until ksw2g_server_wait returns for that request. */
 typedef struct ksw2g_server ksw2g_server_t;
 int ksw2g_server_create(int device, int n_slots, int64_t tb_budget, ksw2g_server_t **server);
@@ -183,6 +184,10 @@ int64_t ksw2g_server_submit_ll(ksw2g_server_t *server, int size, int m, const in
 int ksw2g_server_wait(ksw2g_server_t *server, int64_t id, double *latency_ms, double *queue_ms, int64_t *cigar_used);
 int ksw2g_server_stats(ksw2g_server_t *server, int64_t *admitted, int64_t *done, int64_t *peak_inflight,
 					   int64_t *peak_pool_bytes);
+/* Launches issued and the most requests merged into one launch.  Queued
+ * requests of the head request's kind and scoring scheme are merged into its
+ * launch while they fit the pool (at most 65,536 jobs per launch). */
+int ksw2g_server_launch_stats(ksw2g_server_t *server, int64_t *launches, int64_t *max_merged);
 
 /* Measured 32-bit integer instruction throughput of the device (lane-ops per
  * second), the denominator of the DP kernels' integer-pipe roofline. */

@@ -18,17 +18,25 @@ int report_error(int code, const char *msg);
 struct DevBuf {
   void *p = nullptr;
   size_t cap = 0;
+  // With a stream, growth is stream-ordered (cudaMallocAsync / cudaFreeAsync from the
+  // device's memory pool) and does not synchronise the device; otherwise cudaMalloc.
+  cudaStream_t st = nullptr;
+  cudaError_t alloc_(void **q, size_t c) { return st ? cudaMallocAsync(q, c, st) : cudaMalloc(q, c); }
+  void free_(void *q) {
+    if (st) cudaFreeAsync(q, st);
+    else cudaFree(q);
+  }
   int ensure(size_t n) {
     if (n <= cap) return 0;
-    if (p) cudaFree(p);
+    if (p) free_(p);
     p = nullptr, cap = 0;
-    size_t c = n < 4096 ? 4096 : n + n / 8;
-    if (cudaMalloc(&p, c) != cudaSuccess) {
+    size_t c = n < 4096 ? 4096 : n + (st ? n / 2 : n / 8);
+    if (alloc_(&p, c) != cudaSuccess) {
       cudaGetLastError();
-      if (cudaMalloc(&p, n) != cudaSuccess) {
+      if (alloc_(&p, n) != cudaSuccess) {
         cudaGetLastError();
         p = nullptr;
-        return ksw2g::report_error(KSW2G_E_NOMEM, "cudaMalloc failed");
+        return ksw2g::report_error(KSW2G_E_NOMEM, "device allocation failed");
       }
       c = n;
     }
@@ -36,7 +44,7 @@ struct DevBuf {
     return 0;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) free_(p);
     p = nullptr, cap = 0;
   }
   template <typename T>
@@ -49,7 +57,7 @@ struct PinBuf {
     if (n <= cap) return 0;
     if (p) cudaFreeHost(p);
     p = nullptr, cap = 0;
-    size_t c = n < 4096 ? 4096 : n + n / 8;
+    size_t c = n < 4096 ? 4096 : n + n / 2;
     if (cudaMallocHost(&p, c) != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
@@ -111,6 +119,30 @@ struct ksw2g_batch {
   int n_timed = 0;
 };
 
+
+// Make every device buffer of the batch grow in stream order on st.
+inline void batch_bind_stream(ksw2g_batch *b, cudaStream_t st) {
+  for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts,
+                    &b->cigar, &b->counters, &b->llmat, &b->blist, &b->blist_off})
+    d->st = st;
+}
+
+// A run of jobs whose qoff/toff index their own query and target buffers.  A
+// batch may be prepared from several segments (the serving engine merges the
+// requests of one scoring scheme this way); job offsets are rebased onto the
+// concatenation of the segments' buffers.
+struct SeqSeg {
+  const void *jobs;  // ksw2g_job_t[] or ksw2g_ll_job_t[]
+  int n;
+  const uint8_t *qbuf;
+  int64_t qlen;
+  const uint8_t *tbuf;
+  int64_t tlen;
+};
+int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+                     int8_t q2, int8_t e2, int nseg, const SeqSeg *segs);
+int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape, int nseg,
+                    const SeqSeg *segs);
 
 // Upload + pack the sequences and build the device job table and the wave plan
 // (synchronous on c->st, so the host buffers may be reused on return).

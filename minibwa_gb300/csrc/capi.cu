@@ -159,10 +159,12 @@ extern "C" int ksw2g_batch_kernel_ms(ksw2g_batch_t *b, double *dp_ms, double *bt
 
 // Upload raw sequences and pack them into the padded arena.  Writes the padded
 // offsets of query s and target s to qpad[s], tpad[s].
+// qoff/toff index the concatenation of the segments' query / target buffers.
 int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, const int32_t *qlen,
-                           const int64_t *toff, const int32_t *tlen, const uint8_t *qbuf, int64_t qbuf_len,
-                           const uint8_t *tbuf, int64_t tbuf_len, std::vector<int64_t> &qpad,
-                           std::vector<int64_t> &tpad) {
+                           const int64_t *toff, const int32_t *tlen, int nseg, const SeqSeg *segs,
+                           std::vector<int64_t> &qpad, std::vector<int64_t> &tpad) {
+  int64_t qbuf_len = 0, tbuf_len = 0;
+  for (int k = 0; k < nseg; ++k) qbuf_len += segs[k].qlen, tbuf_len += segs[k].tlen;
   qpad.resize(n), tpad.resize(n);
   int64_t a = 0;
   for (int i = 0; i < n; ++i) {
@@ -185,8 +187,14 @@ int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, co
     ro[n + i] = qbuf_len + toff[i], ln[n + i] = tlen[i], dof[n + i] = tpad[i];
   }
   uint8_t *raw = b->raw.as<uint8_t>();
-  if (qbuf_len) CK(cudaMemcpyAsync(raw, qbuf, qbuf_len, cudaMemcpyHostToDevice, c->st));
-  if (tbuf_len) CK(cudaMemcpyAsync(raw + qbuf_len, tbuf, tbuf_len, cudaMemcpyHostToDevice, c->st));
+  {
+    int64_t qa = 0, ta = qbuf_len;
+    for (int k = 0; k < nseg; ++k) {
+      if (segs[k].qlen) CK(cudaMemcpyAsync(raw + qa, segs[k].qbuf, segs[k].qlen, cudaMemcpyHostToDevice, c->st));
+      if (segs[k].tlen) CK(cudaMemcpyAsync(raw + ta, segs[k].tbuf, segs[k].tlen, cudaMemcpyHostToDevice, c->st));
+      qa += segs[k].qlen, ta += segs[k].tlen;
+    }
+  }
   CK(cudaMemcpyAsync(b->rawmeta.p, hm.data(), meta, cudaMemcpyHostToDevice, c->st));
   const int64_t *dro = b->rawmeta.as<int64_t>();
   const int32_t *dln = (const int32_t *)(dro + 2 * n);
@@ -197,9 +205,57 @@ int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, co
   return 0;
 }
 
+// Jobs of all segments with offsets rebased onto the concatenated buffers; each
+// job must stay inside its own segment's buffers.
+template <typename J>
+static int flatten_segs(int nseg, const SeqSeg *segs, std::vector<J> &flat, const J *&jobs, int &n,
+                        int64_t &qtot, int64_t &ttot) {
+  n = 0, qtot = 0, ttot = 0;
+  for (int k = 0; k < nseg; ++k) {
+    if (segs[k].n < 0 || (segs[k].n > 0 && !segs[k].jobs) || segs[k].qlen < 0 || segs[k].tlen < 0)
+      return set_err(KSW2G_E_ARG, "bad batch segment %d", k);
+    n += segs[k].n;
+  }
+  if (nseg == 1) {
+    jobs = (const J *)segs[0].jobs, qtot = segs[0].qlen, ttot = segs[0].tlen;
+    return 0;
+  }
+  flat.resize(n);
+  int at = 0;
+  for (int k = 0; k < nseg; ++k) {
+    const J *src = (const J *)segs[k].jobs;
+    for (int i = 0; i < segs[k].n; ++i, ++at) {
+      J j = src[i];
+      if (j.qlen < 0 || j.tlen < 0 || j.qoff < 0 || j.toff < 0 || j.qoff + j.qlen > segs[k].qlen ||
+          j.toff + j.tlen > segs[k].tlen)
+        return set_err(KSW2G_E_ARG, "segment %d job %d: sequence out of buffer bounds", k, i);
+      j.qoff += qtot, j.toff += ttot;
+      flat[at] = j;
+    }
+    qtot += segs[k].qlen, ttot += segs[k].tlen;
+  }
+  jobs = flat.data();
+  return 0;
+}
+
 int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
-                            int8_t q2, int8_t e2, int n, const ksw2g_job_t *jobs, const uint8_t *qbuf,
-                            int64_t qbuf_len, const uint8_t *tbuf, int64_t tbuf_len) {
+                     int8_t q2, int8_t e2, int n, const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+                     const uint8_t *tbuf, int64_t tbuf_len) {
+  if (n < 0 || (n > 0 && !jobs)) return set_err(KSW2G_E_ARG, "bad batch arguments");
+  const SeqSeg seg{jobs, n, qbuf, qbuf_len, tbuf, tbuf_len};
+  return ext_prepare_segs(c, b, dual, m, mat, q, e, q2, e2, 1, &seg);
+}
+
+int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
+                     int8_t q2, int8_t e2, int nseg, const SeqSeg *segs) {
+  std::vector<ksw2g_job_t> flat;
+  const ksw2g_job_t *jobs = nullptr;
+  int n = 0;
+  int64_t qbuf_len = 0, tbuf_len = 0;
+  {
+    const int rc0 = flatten_segs(nseg, segs, flat, jobs, n, qbuf_len, tbuf_len);
+    if (rc0) return rc0;
+  }
   if (n < 0 || (n > 0 && !jobs) || !mat) return set_err(KSW2G_E_ARG, "bad batch arguments");
   CK(cudaSetDevice(c->device));
   b->kind = dual ? 1 : 0;
@@ -232,8 +288,7 @@ int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     if (mode[i] != 0) cig += J.qlen + J.tlen + 1;
   }
   std::vector<int64_t> qpad, tpad;
-  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), qbuf, qbuf_len, tbuf, tbuf_len,
-                           qpad, tpad);
+  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad);
   if (rc) return rc;
   // device job table
   std::vector<ksw2g_job> dj(n);
@@ -682,9 +737,24 @@ extern "C" void ksw_extd2_sse(void *km, int qlen, const uint8_t *query, int tlen
 }
 
 // ================================================================ ksw_ll
-int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape,
-                           int n, const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
-                           const uint8_t *tbuf, int64_t tbuf_len) {
+int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape, int n,
+                    const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+                    int64_t tbuf_len) {
+  if (n < 0 || (n > 0 && !jobs)) return set_err(KSW2G_E_ARG, "bad ll batch arguments");
+  const SeqSeg seg{jobs, n, qbuf, qbuf_len, tbuf, tbuf_len};
+  return ll_prepare_segs(c, b, size, m, mat, gapo, gape, 1, &seg);
+}
+
+int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape, int nseg,
+                    const SeqSeg *segs) {
+  std::vector<ksw2g_ll_job_t> flat;
+  const ksw2g_ll_job_t *jobs = nullptr;
+  int n = 0;
+  int64_t qbuf_len = 0, tbuf_len = 0;
+  {
+    const int rc0 = flatten_segs(nseg, segs, flat, jobs, n, qbuf_len, tbuf_len);
+    if (rc0) return rc0;
+  }
   if (n < 0 || (n > 0 && !jobs) || !mat || m <= 0 || m > 64) return set_err(KSW2G_E_ARG, "bad ll batch arguments");
   CK(cudaSetDevice(c->device));
   size = size > 1 ? 2 : 1;
@@ -715,8 +785,7 @@ int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t 
   b->ll_mat_max = mat[0];
   for (int a = 1; a < m * m; ++a) b->ll_mat_max = std::max(b->ll_mat_max, (int)mat[a]);
   std::vector<int64_t> qpad, tpad;
-  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), qbuf, qbuf_len, tbuf, tbuf_len, qpad,
-                           tpad);
+  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad);
   if (rc) return rc;
   std::vector<ksw2g_ll_job> dj(n);
   for (int i = 0; i < n; ++i) dj[i] = ksw2g_ll_job{qpad[i], tpad[i], jobs[i].qlen, jobs[i].tlen, jobs[i].xtra, 0};

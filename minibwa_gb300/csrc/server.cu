@@ -2,19 +2,25 @@
 //
 // Requests (one batch of jobs of one kind and scoring scheme each) arrive at
 // any time from any host thread.  A scheduler thread admits them in arrival
-// order as soon as (a) one of the engine's slots is free and (b) the request's
+// order as soon as (a) one of the engine's slots is free and (b) their
 // traceback rows fit in the engine's device traceback pool, a fixed budget of
-// HBM managed by a first-fit allocator.  Each slot owns a CUDA stream and a
-// reusable batch (sequence arena, job table, results, CIGAR arena), so the
-// work of several requests overlaps on the device while later requests queue.
-// A host-function callback at the end of each slot's stream copies the results
-// to the caller's buffers, stamps the completion time and frees the slot and
-// its pool range, which wakes the scheduler.  Admission uses the reference's
-// traceback footprint: the rows of (qlen+tlen-1) anti-diagonals of n_col_*16
-// bytes each (ksw2_extz2_sse.c:84), summed over the request.
+// HBM managed by a first-fit allocator.  When the head request is admitted,
+// the queued requests behind it that share its kind and scoring scheme are
+// merged into the same launch while they fit the pool and a job cap, so a
+// queue that builds up under load is drained by large launches that fill the
+// GPU, while a lone request runs at once.  Each slot owns a CUDA stream and a
+// reusable batch (sequence arena, job table, results, CIGAR arena) whose
+// buffers grow in stream order, so the work of several slots overlaps on the
+// device.  A host-function callback at the end of each slot's stream copies
+// every merged request's results and CIGARs to its caller's buffers, stamps
+// the completion time and frees the slot and its pool range, which wakes the
+// scheduler.  Admission uses the reference's traceback footprint: the rows of
+// (qlen+tlen-1) anti-diagonals of n_col_*16 bytes each (ksw2_extz2_sse.c:84),
+// summed over the request.
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -31,6 +37,9 @@
 using namespace ksw2g;
 
 namespace {
+
+const int kMergeScan = 256;         // queued requests examined for merging
+const int kMergeMaxJobs = 1 << 16;  // jobs of one merged launch
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -66,6 +75,11 @@ struct RangeAlloc {
       if (pv->first + pv->second == it->first) pv->second += it->second, free_.erase(it);
     }
   }
+  int64_t largest() const {
+    int64_t m = 0;
+    for (auto &kv : free_) m = std::max(m, kv.second);
+    return m;
+  }
   int64_t free_bytes() const {
     int64_t s = 0;
     for (auto &kv : free_) s += kv.second;
@@ -91,12 +105,18 @@ struct Req {
   int status = 1;  // 1 queued/running, 0 done, < 0 error
 };
 
+bool same_class(const Req *a, const Req *b) {
+  if (a->kind != b->kind || a->m != b->m || a->mat != b->mat) return false;
+  if (a->kind <= 1) return a->q == b->q && a->e == b->e && a->q2 == b->q2 && a->e2 == b->e2;
+  return a->gapo == b->gapo && a->gape == b->gape;
+}
+
 struct Slot {
   ksw2g_ctx ctx;
   ksw2g_batch batch;
   PinBuf res_pin, cig_pin, hdr_pin;
-  Req *req = nullptr;
-  int64_t pool_off = 0;
+  std::vector<Req *> group;  // the merged requests in flight, in launch order
+  int64_t pool_off = 0, pool_len = 0;
   struct ksw2g_server *srv = nullptr;
 };
 
@@ -116,41 +136,71 @@ struct ksw2g_server {
   bool stop = false;
   int64_t next_id = 1;
   int64_t n_admitted = 0, n_done = 0, peak_inflight = 0, peak_pool = 0, inflight = 0;
+  int64_t n_launches = 0, max_group = 0;
 };
 
 namespace {
 
+// Runs on CUDA's callback thread once the slot's stream has finished: no CUDA calls here.
 void CUDART_CB on_done(void *arg) {
   Slot *s = (Slot *)arg;
   ksw2g_server *S = s->srv;
-  Req *r = s->req;
-  // The waiter may free r as soon as it sees a final status, so everything that
-  // touches r after the status changes happens under the lock, status last.
-  int st = 0;
-  int64_t used = 0;
-  if (r->kind <= 1) {
-    memcpy(r->res, s->res_pin.p, sizeof(ksw2g_ext_result) * (size_t)r->n);
+  std::vector<int> st(s->group.size(), 0);
+  std::vector<int64_t> used(s->group.size(), 0);
+  if (!s->group.empty() && s->group[0]->kind <= 1) {
     struct {
       unsigned long long cursor;
       int err, pad;
     } hdr;
     memcpy(&hdr, s->hdr_pin.p, sizeof hdr);
-    used = (int64_t)hdr.cursor;
-    if (hdr.err || used > r->cigar_cap) st = KSW2G_E_CAPACITY;
-    else if (used) memcpy(r->cigar, s->cig_pin.p, sizeof(uint32_t) * (size_t)used);
+    const ksw2g_ext_result *all = (const ksw2g_ext_result *)s->res_pin.p;
+    const uint32_t *cig = (const uint32_t *)s->cig_pin.p;
+    int64_t j0 = 0;
+    for (size_t g = 0; g < s->group.size(); ++g) {
+      Req *r = s->group[g];
+      ksw2g_ext_result *out = (ksw2g_ext_result *)r->res;
+      if (r->n) memcpy(out, all + j0, sizeof(ksw2g_ext_result) * (size_t)r->n);
+      if (hdr.err) {
+        st[g] = KSW2G_E_CAPACITY;
+      } else {
+        // this request's CIGARs, packed in job order into its own buffer
+        int64_t at = 0;
+        for (int i = 0; i < r->n; ++i) {
+          const int64_t k = out[i].n_cigar;
+          if (at + k > r->cigar_cap) {
+            st[g] = KSW2G_E_CAPACITY;
+            break;
+          }
+          if (k) memcpy(r->cigar + at, cig + out[i].cigar_off, sizeof(uint32_t) * (size_t)k);
+          out[i].cigar_off = at;
+          at += k;
+        }
+        used[g] = at;
+      }
+      j0 += r->n;
+    }
   } else {
-    memcpy(r->res, s->res_pin.p, sizeof(ksw2g_ll_result) * (size_t)r->n);
+    const ksw2g_ll_result *all = (const ksw2g_ll_result *)s->res_pin.p;
+    int64_t j0 = 0;
+    for (Req *r : s->group) {
+      if (r->n) memcpy(r->res, all + j0, sizeof(ksw2g_ll_result) * (size_t)r->n);
+      j0 += r->n;
+    }
   }
   const double t = now_ms();
-  std::lock_guard<std::mutex> g(S->mu);
-  S->alloc.give(s->pool_off, r->need);
-  r->cigar_used = used;
-  r->t_done = t;
-  r->status = st;
-  s->req = nullptr;
+  std::lock_guard<std::mutex> lk(S->mu);
+  // a waiter may free a request as soon as it sees a final status: status is set last
+  S->alloc.give(s->pool_off, s->pool_len);
+  for (size_t g = 0; g < s->group.size(); ++g) {
+    Req *r = s->group[g];
+    r->cigar_used = used[g];
+    r->t_done = t;
+    r->status = st[g];
+  }
+  S->inflight -= (int64_t)s->group.size();
+  S->n_done += (int64_t)s->group.size();
+  s->group.clear();
   S->idle.push_back(s);
-  --S->inflight;
-  ++S->n_done;
   S->cv_sched.notify_all();
   S->cv_done.notify_all();
 }
@@ -165,37 +215,45 @@ int64_t ext_need(const Req *r, int64_t budget) {
   return f < budget ? f : budget;
 }
 
-// Prepare (synchronous uploads on the slot's stream) and enqueue run, copies and the callback.
-int launch_req(Slot *s, Req *r) {
+// Prepare (synchronous uploads on the slot's stream) and enqueue the run, the
+// result copies and the completion callback of a merged group.
+int launch_group(Slot *s) {
   ksw2g_ctx &c = s->ctx;
   ksw2g_batch &b = s->batch;
+  const Req *h = s->group[0];
+  std::vector<SeqSeg> segs;
+  int n = 0;
+  for (const Req *r : s->group) {
+    segs.push_back(SeqSeg{r->jobs, r->n, r->qbuf, r->qlen, r->tbuf, r->tlen});
+    n += r->n;
+  }
   int rc;
-  if (r->kind <= 1) {
-    c.tb_budget = r->need > 0 ? r->need : 16;
-    rc = ext_prepare_into(&c, &b, r->kind, r->m, r->mat.data(), r->q, r->e, r->q2, r->e2, r->n,
-                          (const ksw2g_job_t *)r->jobs, r->qbuf, r->qlen, r->tbuf, r->tlen);
+  if (h->kind <= 1) {
+    c.tb_budget = std::max<int64_t>(s->pool_len, 16);
+    rc = ext_prepare_segs(&c, &b, h->kind, h->m, h->mat.data(), h->q, h->e, h->q2, h->e2, (int)segs.size(),
+                          segs.data());
     if (rc) return rc;
-    if ((rc = s->res_pin.ensure(sizeof(ksw2g_ext_result) * (size_t)std::max(r->n, 1))) ||
+    if ((rc = s->res_pin.ensure(sizeof(ksw2g_ext_result) * (size_t)std::max(n, 1))) ||
         (rc = s->cig_pin.ensure(sizeof(uint32_t) * (size_t)b.cigar_cap)) || (rc = s->hdr_pin.ensure(64)))
       return rc;
     memset(s->hdr_pin.p, 0, 16);
-    if ((rc = ext_run_on(&b, c.st, s->srv->pool.as<uint8_t>() + s->pool_off, std::max<int64_t>(r->need, 16))))
+    if ((rc = ext_run_on(&b, c.st, s->srv->pool.as<uint8_t>() + s->pool_off, std::max<int64_t>(s->pool_len, 16))))
       return rc;
-    if (r->n > 0 &&
-        (cudaMemcpyAsync(s->res_pin.p, b.res.p, sizeof(ksw2g_ext_result) * (size_t)r->n, cudaMemcpyDeviceToHost,
+    if (n > 0 &&
+        (cudaMemcpyAsync(s->res_pin.p, b.res.p, sizeof(ksw2g_ext_result) * (size_t)n, cudaMemcpyDeviceToHost,
                          c.st) != cudaSuccess ||
          cudaMemcpyAsync(s->hdr_pin.p, b.counters.p, 16, cudaMemcpyDeviceToHost, c.st) != cudaSuccess ||
          (b.cigar_cap > 0 && cudaMemcpyAsync(s->cig_pin.p, b.cigar.p, sizeof(uint32_t) * (size_t)b.cigar_cap,
                                              cudaMemcpyDeviceToHost, c.st) != cudaSuccess)))
       return report_error(KSW2G_E_CUDA, "server: result copy failed");
   } else {
-    rc = ll_prepare_into(&c, &b, r->kind == 2 ? 1 : 2, r->m, r->mat.data(), r->gapo, r->gape, r->n,
-                         (const ksw2g_ll_job_t *)r->jobs, r->qbuf, r->qlen, r->tbuf, r->tlen);
+    rc = ll_prepare_segs(&c, &b, h->kind == 2 ? 1 : 2, h->m, h->mat.data(), h->gapo, h->gape, (int)segs.size(),
+                         segs.data());
     if (rc) return rc;
-    if ((rc = s->res_pin.ensure(sizeof(ksw2g_ll_result) * (size_t)std::max(r->n, 1)))) return rc;
+    if ((rc = s->res_pin.ensure(sizeof(ksw2g_ll_result) * (size_t)std::max(n, 1)))) return rc;
     if ((rc = ll_run_on(&b, c.st))) return rc;
-    if (r->n > 0 && cudaMemcpyAsync(s->res_pin.p, b.res.p, sizeof(ksw2g_ll_result) * (size_t)r->n, cudaMemcpyDeviceToHost,
-                        c.st) != cudaSuccess)
+    if (n > 0 && cudaMemcpyAsync(s->res_pin.p, b.res.p, sizeof(ksw2g_ll_result) * (size_t)n, cudaMemcpyDeviceToHost,
+                                 c.st) != cudaSuccess)
       return report_error(KSW2G_E_CUDA, "server: result copy failed");
   }
   if (cudaLaunchHostFunc(c.st, on_done, s) != cudaSuccess)
@@ -210,33 +268,47 @@ void scheduler(ksw2g_server *S) {
     S->cv_sched.wait(lk, [&] { return (S->stop && S->queue.empty()) || (!S->queue.empty() && !S->idle.empty()); });
     if (S->stop && S->queue.empty()) return;
     Req *r = S->queue.front();
-    const int64_t off = r->need > 0 ? S->alloc.take(r->need) : 0;
-    if (off < 0) {  // not enough contiguous pool yet: wait for a completion
+    const int64_t room = S->alloc.largest();
+    if (r->need > room) {  // not enough contiguous pool yet: wait for a completion
       S->cv_sched.wait(lk);
       continue;
     }
-    S->queue.pop_front();
+    // merge the queued requests of the same class behind the head
     Slot *s = S->idle.back();
     S->idle.pop_back();
-    s->req = r;
-    s->pool_off = off;
-    r->t_admit = now_ms();
-    ++S->n_admitted;
-    ++S->inflight;
+    s->group.assign(1, r);
+    int64_t need = r->need, jobs = r->n;
+    std::deque<Req *> rest;
+    for (size_t i = 1; i < S->queue.size(); ++i) {
+      Req *x = S->queue[i];
+      if ((int)i <= kMergeScan && same_class(r, x) && jobs + x->n <= kMergeMaxJobs && need + x->need <= room)
+        s->group.push_back(x), need += x->need, jobs += x->n;
+      else
+        rest.push_back(x);
+    }
+    S->queue.swap(rest);
+    const int64_t off = need > 0 ? S->alloc.take(need) : 0;  // fits: need <= the largest free range
+    s->pool_off = off < 0 ? 0 : off, s->pool_len = need;
+    const double t = now_ms();
+    for (Req *x : s->group) x->t_admit = t;
+    S->n_admitted += (int64_t)s->group.size();
+    S->inflight += (int64_t)s->group.size();
+    ++S->n_launches;
+    S->max_group = std::max<int64_t>(S->max_group, (int64_t)s->group.size());
     S->peak_inflight = std::max(S->peak_inflight, S->inflight);
     S->peak_pool = std::max(S->peak_pool, S->alloc.cap - S->alloc.free_bytes());
     lk.unlock();
-    const int rc = launch_req(s, r);
+    const int rc = launch_group(s);
     lk.lock();
-    if (rc) {  // nothing of this request is on the stream any more
+    if (rc) {  // nothing of this group is on the stream any more
       cudaStreamSynchronize(s->ctx.st);
-      r->status = rc;
-      r->t_done = now_ms();
-      S->alloc.give(s->pool_off, r->need);
-      s->req = nullptr;
+      const double td = now_ms();
+      S->alloc.give(s->pool_off, s->pool_len);
+      for (Req *x : s->group) x->status = rc, x->t_done = td;
+      S->inflight -= (int64_t)s->group.size();
+      S->n_done += (int64_t)s->group.size();
+      s->group.clear();
       S->idle.push_back(s);
-      --S->inflight;
-      ++S->n_done;
       S->cv_done.notify_all();
     }
   }
@@ -248,6 +320,15 @@ extern "C" int ksw2g_server_create(int device, int n_slots, int64_t tb_budget, k
   if (!out || n_slots < 1 || n_slots > 256 || tb_budget < (1 << 20))
     return report_error(KSW2G_E_ARG, "server: need 1..256 slots and a traceback budget >= 1 MiB");
   if (cudaSetDevice(device) != cudaSuccess) return report_error(KSW2G_E_CUDA, "server: bad device");
+  // keep the memory the slots' stream-ordered buffers free cached in the device pool
+  {
+    cudaMemPool_t mp;
+    if (cudaDeviceGetDefaultMemPool(&mp, device) == cudaSuccess) {
+      uint64_t thr = ~0ull;
+      cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    cudaGetLastError();
+  }
   ksw2g_server *S = new ksw2g_server;
   S->device = device;
   int rc;
@@ -265,7 +346,12 @@ extern "C" int ksw2g_server_create(int device, int n_slots, int64_t tb_budget, k
       ksw2g_server_destroy(S);
       return report_error(KSW2G_E_CUDA, "server: cudaStreamCreate failed");
     }
+    batch_bind_stream(&s->batch, s->ctx.st);
     S->slots.push_back(s);
+    if ((rc = s->res_pin.ensure(1 << 20)) || (rc = s->cig_pin.ensure(8 << 20)) || (rc = s->hdr_pin.ensure(64))) {
+      ksw2g_server_destroy(S);
+      return rc;
+    }
     S->idle.push_back(s);
   }
   S->sched = std::thread(scheduler, S);
@@ -288,6 +374,7 @@ extern "C" void ksw2g_server_destroy(ksw2g_server_t *S) {
                       &s->batch.sorted, &s->batch.tb_off, &s->batch.res, &s->batch.bts, &s->batch.cigar,
                       &s->batch.counters, &s->batch.llmat, &s->batch.blist, &s->batch.blist_off})
       d->release();
+    cudaStreamSynchronize(s->ctx.st);
     s->res_pin.release(), s->cig_pin.release(), s->hdr_pin.release();
     cudaStreamDestroy(s->ctx.st);
     delete s;
@@ -366,5 +453,13 @@ extern "C" int ksw2g_server_stats(ksw2g_server_t *S, int64_t *admitted, int64_t 
   if (done) *done = S->n_done;
   if (peak_inflight) *peak_inflight = S->peak_inflight;
   if (peak_pool_bytes) *peak_pool_bytes = S->peak_pool;
+  return 0;
+}
+
+extern "C" int ksw2g_server_launch_stats(ksw2g_server_t *S, int64_t *launches, int64_t *max_merged) {
+  if (!S) return report_error(KSW2G_E_ARG, "server: null");
+  std::lock_guard<std::mutex> g(S->mu);
+  if (launches) *launches = S->n_launches;
+  if (max_merged) *max_merged = S->max_group;
   return 0;
 }

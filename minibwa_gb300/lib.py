@@ -110,6 +110,7 @@ def load_library():
         "ksw2g_server_submit_ll": (i64, [vp, i32, i32, vp, i32, i32, i32, vp, u8p, i64, u8p, i64, vp]),
         "ksw2g_server_wait": (i32, [vp, i64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(i64)]),
         "ksw2g_server_stats": (i32, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
+        "ksw2g_server_launch_stats": (i32, [vp, C.POINTER(i64), C.POINTER(i64)]),
         "ksw_extz2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i32, i32, i32, i32, C.POINTER(KswExtz)]),
         "ksw_extd2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i8, i8, i32, i32, i32, i32,
                                  C.POINTER(KswExtz)]),
@@ -424,7 +425,10 @@ class Server:
     def stats(self):
         a, d, p, b = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
         _check(self.L.ksw2g_server_stats(self.h, C.byref(a), C.byref(d), C.byref(p), C.byref(b)))
-        return dict(admitted=a.value, done=d.value, peak_inflight=p.value, peak_pool_bytes=b.value)
+        nl, mg = C.c_int64(), C.c_int64()
+        _check(self.L.ksw2g_server_launch_stats(self.h, C.byref(nl), C.byref(mg)))
+        return dict(admitted=a.value, done=d.value, peak_inflight=p.value, peak_pool_bytes=b.value,
+                    launches=nl.value, max_merged=mg.value)
 
     def close(self):
         if self.h:

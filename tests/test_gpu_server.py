@@ -44,7 +44,7 @@ def _same(kind, a, ca, b, cb):
             assert np.array_equal(ca[a["cigar_off"][i]:a["cigar_off"][i] + k], cb[b["cigar_off"][i]:b["cigar_off"][i] + k])
 
 
-@pytest.mark.parametrize("slots,budget", [(4, 64 << 20), (8, 4 << 30)])
+@pytest.mark.parametrize("slots,budget", [(1, 4 << 30), (4, 64 << 20), (8, 4 << 30)])
 def test_results_same_alone_and_in_the_mix(built, slots, budget):
     from minibwa_gb300 import Context, Server
     reqs = _requests()
@@ -67,7 +67,9 @@ def test_results_same_alone_and_in_the_mix(built, slots, budget):
     st = srv.stats()
     srv.close()
     assert st["done"] == len(reqs) and st["admitted"] == len(reqs)
-    assert st["peak_inflight"] >= 2  # requests overlapped on the device
+    assert st["peak_inflight"] >= 2  # requests overlapped on the device (merged or on separate slots)
+    if slots == 1:
+        assert st["max_merged"] >= 2 and st["launches"] < len(reqs)  # queued requests were merged
     assert st["peak_pool_bytes"] <= budget
     for (kind, p), (res, cig), (r2, c2, lat, que) in zip(reqs, alone, got):
         _same(kind, r2, c2, res, cig)
