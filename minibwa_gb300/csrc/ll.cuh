@@ -212,6 +212,33 @@ ll_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__re
 
 namespace ksw2g {
 
+// Bytes 0 and 1 of x into the low and high halfwords, sign-extended when SIGNED
+// (PTX prmt, default mode: selector bit 3 replicates the selected byte's sign).
+template <bool SIGNED>
+__device__ __forceinline__ uint32_t widen2(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  uint32_t r;
+  if (SIGNED) asm("prmt.b32 %0, %1, 0, 0x9180;" : "=r"(r) : "r"(x));
+  else asm("prmt.b32 %0, %1, 0, 0x4140;" : "=r"(r) : "r"(x));
+  return r;
+#else
+  const uint32_t b0 = x & 0xffu, b1 = (x >> 8) & 0xffu;
+  if (SIGNED) return (uint32_t)(uint16_t)(int16_t)(int8_t)b0 | ((uint32_t)(uint16_t)(int16_t)(int8_t)b1 << 16);
+  return b0 | (b1 << 16);
+#endif
+}
+
+// Word offset, in the DPX kernel's dynamic shared memory, of the per-thread
+// Hmax columns that follow the groups' profiles (16-byte aligned).
+__host__ __device__ inline int ll_dpx_hm_offset(int m, int slen, int T) {
+  const int prof_entries = (128 / T) * (m * slen * T + 2 * T);
+  return ((prof_entries * 2 + 15) / 16) * 4;
+}
+// Dynamic shared memory of one 128-thread block of the DPX kernel.
+inline size_t ll_dpx_smem_bytes(int m, int slen, int T) {
+  return (size_t)ll_dpx_hm_offset(m, slen, T) * 4 + (size_t)128 * slen * 4;
+}
+
 // Two SSE lanes per thread, in the two halfwords of every register, on the DPX
 // 16x2 instructions: thread t of a group of T = LANES/2 threads holds lanes t
 // (low half) and t+T (high half) of one job.  Every step of the reference's
@@ -223,7 +250,7 @@ namespace ksw2g {
 // has checked that no H value can reach 32767 and that 0 <= gape, gapo+gape
 // <= 32767; otherwise the host launches ll_kernel above.
 template <int SIZE, int SLEN>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, SLEN <= 24 ? 4 : (SLEN <= 32 ? 3 : 2))
 ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__restrict__ arena,
               const int8_t *__restrict__ mat_g, int m, int gapo, int gape, ksw2g_ll_result *__restrict__ res,
               uint64_t *__restrict__ blist, const int64_t *__restrict__ blist_off, int *__restrict__ job_counter) {
@@ -233,9 +260,13 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
   const int t = lane & (T - 1);
   const int grp = threadIdx.x / T;
   const unsigned gm = ((1u << T) - 1u) << (lane & ~(T - 1));
+  // Shared memory: the groups' striped profiles, one byte per SSE lane (two per 16-bit
+  // entry: lanes t and t+T), then the best-row copy of H of every thread (Hmax of the
+  // reference) in a thread-interleaved column, which is written only when the maximum grows.
   extern __shared__ uint32_t lld_smem[];
-  const int prof_stride = m * SLEN * T + T;  // +T words staggers the groups over the banks
-  uint32_t *prof = lld_smem + grp * prof_stride;
+  const int prof_stride = m * SLEN * T + 2 * T;  // entries; +2T staggers the groups over the banks
+  uint16_t *prof = (uint16_t *)lld_smem + grp * prof_stride;
+  uint32_t *hm = lld_smem + ll_dpx_hm_offset(m, SLEN, T) + threadIdx.x;  // hm[s * 128]
 
   int shift = 127, mdiff = 0;  // ksw2_ll_sse.c:66-74
   for (int a = 0; a < m * m; ++a) {
@@ -250,7 +281,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
   auto pk = [](int lo, int hi) -> uint32_t { return (uint32_t)(uint16_t)lo | ((uint32_t)(uint16_t)hi << 16); };
   const uint32_t NGOE = pk(-goe, -goe), NGE = pk(-ge, -ge), NSHIFT = pk(-shift, -shift), C255 = pk(255, 255);
 
-  uint32_t H[SLEN], E[SLEN], HM[SLEN];
+  uint32_t H[SLEN], E[SLEN];
   int jid = -1, slen = 0, qlen = 0, tlen = 0, xtra = 0, i = 0, te = -1, gmax = 0, n_b = 0, minsc = 0, endsc = 0;
   const uint8_t *tp = nullptr;
   uint64_t *bl = nullptr;
@@ -281,9 +312,9 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
                 const int k = s + (t + h * T) * slen;
                 const int qc = k >= qlen ? 0 : qp[k];
                 const int v = k >= qlen ? -1 : mat_g[a * m + (qc < m ? qc : m - 1)];  // codes must be < m
-                v2[h] = SIZE == 1 ? ((v + shift) & 0xff) : v;
+                v2[h] = SIZE == 1 ? ((v + shift) & 0xff) : v;  // u8: 0..255; i16: an int8 score
               }
-              prof[(a * SLEN + s) * T + t] = pk(v2[0], v2[1]);
+              prof[(a * SLEN + s) * T + t] = (uint16_t)((v2[0] & 0xff) | ((v2[1] & 0xff) << 8));
             }
           }
         __syncwarp(gm);
@@ -291,7 +322,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
         endsc = (xtra & KSW2G_LL_STOP) ? (xtra & 0xffff) : 0x10000;
         bl = (blist && (xtra & KSW2G_LL_SUBO)) ? blist + blist_off[jid] : nullptr;
 #pragma unroll
-        for (int s = 0; s < SLEN; ++s) H[s] = 0, E[s] = 0, HM[s] = 0;
+        for (int s = 0; s < SLEN; ++s) H[s] = 0, E[s] = 0, hm[s * 128] = 0;
         i = 0, te = -1, gmax = 0, n_b = 0;
       }
     }
@@ -301,7 +332,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
     bool done = i >= tlen;
     if (!done) {
       const int a = tp[i] < m ? tp[i] : m - 1;
-      const uint32_t *S = prof + a * SLEN * T + t;
+      const uint16_t *S = prof + a * SLEN * T + t;
       uint32_t hlast = H[0];
 #pragma unroll
       for (int s = 1; s < SLEN; ++s) hlast = (s == slen - 1) ? H[s] : hlast;
@@ -312,7 +343,8 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
 #pragma unroll
       for (int s = 0; s < SLEN; ++s) {
         if (s < slen) {
-          const uint32_t sc = S[s * T];
+          // widen the entry's two bytes to the two halfwords: zero-extended (u8) or sign-extended (i16)
+          const uint32_t sc = widen2<SIZE == 2>((uint32_t)S[s * T]);
           uint32_t hv;
           if (SIZE == 1) hv = __viaddmax_s16x2(__viaddmin_s16x2(h, sc, C255), NSHIFT, 0u);
           else hv = __vadd2(h, sc);
@@ -350,7 +382,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
       if (imax > gmax) {
         gmax = imax, te = i;
 #pragma unroll
-        for (int s = 0; s < SLEN; ++s) HM[s] = H[s];
+        for (int s = 0; s < SLEN; ++s) hm[s * 128] = H[s];
         if ((SIZE == 1 && gmax + shift >= 255) || gmax >= endsc) done = true;
       }
       ++i;
@@ -368,7 +400,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
           if (s < slen) {
 #pragma unroll
             for (int hf = 0; hf < 2; ++hf) {
-              const uint32_t v = (HM[s] >> (16 * hf)) & 0xffffu;
+              const uint32_t v = (hm[s * 128] >> (16 * hf)) & 0xffffu;
               const uint32_t key = (v << 16) | (uint32_t)(0xffff - (s + (t + hf * T) * slen));
               if (!any || key > best) best = key, any = true;
             }

@@ -11,10 +11,13 @@ typedef void (*ll_fn)(const ksw2g_ll_job *, int, const uint8_t *, const int8_t *
 static const int kSlen[] = {8, 16, 32, 64};
 static const ll_fn kLL[2][4] = {{ll_kernel<1, 8>, ll_kernel<1, 16>, ll_kernel<1, 32>, ll_kernel<1, 64>},
                                 {ll_kernel<2, 8>, ll_kernel<2, 16>, ll_kernel<2, 32>, ll_kernel<2, 64>}};
-static const int kSlenD[] = {8, 16, 24, 32, 48};
-static const ll_fn kLLD[2][5] = {
-    {ll_dpx_kernel<1, 8>, ll_dpx_kernel<1, 16>, ll_dpx_kernel<1, 24>, ll_dpx_kernel<1, 32>, ll_dpx_kernel<1, 48>},
-    {ll_dpx_kernel<2, 8>, ll_dpx_kernel<2, 16>, ll_dpx_kernel<2, 24>, ll_dpx_kernel<2, 32>, ll_dpx_kernel<2, 48>}};
+static const int kSlenD[] = {8, 16, 20, 24, 32, 48};
+static const int kNumSlenD = 6;
+static const ll_fn kLLD[2][kNumSlenD] = {
+    {ll_dpx_kernel<1, 8>, ll_dpx_kernel<1, 16>, ll_dpx_kernel<1, 20>, ll_dpx_kernel<1, 24>, ll_dpx_kernel<1, 32>,
+     ll_dpx_kernel<1, 48>},
+    {ll_dpx_kernel<2, 8>, ll_dpx_kernel<2, 16>, ll_dpx_kernel<2, 20>, ll_dpx_kernel<2, 24>, ll_dpx_kernel<2, 32>,
+     ll_dpx_kernel<2, 48>}};
 
 int ll_slen_cap(int size) { (void)size; return 64; }
 
@@ -29,7 +32,7 @@ bool ll_dpx_exact(int size, const LLLaunch &L) {
 static cudaError_t launch_dpx(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st, bool &done) {
   done = false;
   int si = -1;
-  for (int i = 0; i < 5; ++i)
+  for (int i = 0; i < kNumSlenD; ++i)
     if (slen_max <= kSlenD[i]) {
       si = i;
       break;
@@ -37,7 +40,7 @@ static cudaError_t launch_dpx(int size, int slen_max, const LLLaunch &L, int max
   if (si < 0) return cudaSuccess;
   const ll_fn fn = kLLD[size - 1][si];
   const int T = size == 1 ? 8 : 4, groups = 128 / T;
-  const size_t smem = (size_t)groups * (L.m * kSlenD[si] * T + T) * sizeof(uint32_t);
+  const size_t smem = ll_dpx_smem_bytes(L.m, kSlenD[si], T);
   if (smem > 200 * 1024) return cudaSuccess;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -119,13 +119,13 @@ int emu_ll(int size, int slen_max, int n, const ksw2g_ll_job *jobs, const uint8_
       break;
     }
   if (dpx) {
-    const int sd[] = {8, 16, 24, 32, 48};
-    const ll_fn d1[] = {ll_dpx_kernel<1, 8>, ll_dpx_kernel<1, 16>, ll_dpx_kernel<1, 24>, ll_dpx_kernel<1, 32>,
-                        ll_dpx_kernel<1, 48>};
-    const ll_fn d2[] = {ll_dpx_kernel<2, 8>, ll_dpx_kernel<2, 16>, ll_dpx_kernel<2, 24>, ll_dpx_kernel<2, 32>,
-                        ll_dpx_kernel<2, 48>};
+    const int sd[] = {8, 16, 20, 24, 32, 48};
+    const ll_fn d1[] = {ll_dpx_kernel<1, 8>,  ll_dpx_kernel<1, 16>, ll_dpx_kernel<1, 20>,
+                        ll_dpx_kernel<1, 24>, ll_dpx_kernel<1, 32>, ll_dpx_kernel<1, 48>};
+    const ll_fn d2[] = {ll_dpx_kernel<2, 8>,  ll_dpx_kernel<2, 16>, ll_dpx_kernel<2, 20>,
+                        ll_dpx_kernel<2, 24>, ll_dpx_kernel<2, 32>, ll_dpx_kernel<2, 48>};
     f = nullptr;
-    for (int i = 0; i < 5; ++i)
+    for (int i = 0; i < 6; ++i)
       if (slen_max <= sd[i]) {
         f = size == 1 ? d1[i] : d2[i];
         break;
