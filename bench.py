@@ -329,8 +329,9 @@ def main():
         dp_ms, bt_ms, n_dp, n_bt = batches[0].kernel_ms()
         n_dp = max(1, n_dp // args.steps)
         dp_ms_step = dp_ms / args.steps
-        kernel_note = (f"DP kernel: {n_dp} launches per step, {dp_ms_step:.2f} ms per step "
-                       f"(backtrack {bt_ms / args.steps:.2f} ms), CUDA events around each launch")
+        kernel_note = (f"DP kernel: {n_dp} launches per step, busy {dp_ms_step:.2f} ms per step "
+                       f"(backtrack {bt_ms / args.steps:.2f} ms); CUDA events around each launch, the "
+                       f"union of their intervals (waves alternate between two streams)")
     else:
         dp_ms_step = ms  # branches overlap inside the graph: the whole graph is the timed unit
         kernel_note = "whole graph (DP branches overlap); CUDA events around each graph launch"

@@ -99,9 +99,11 @@ int ksw2g_batch_launches(const ksw2g_batch_t *batch);
 void ksw2g_batch_free(ksw2g_batch_t *batch);
 /* Per-kernel timing of a batch's runs: with timing on, every kernel of a run is
  * bracketed by CUDA events on the launching stream.  ksw2g_batch_kernel_ms
- * waits for the runs and returns the DP-kernel and backtrack-kernel time (sums
- * over all launches since timing was last switched on) and the launch counts.
- * Off by default; not for batches captured in a graph. */
+ * waits for the runs and returns, for the DP kernels and the backtrack kernels
+ * of all runs since timing was last switched on, the time covered by their
+ * launches (launches on the two streams of a run may overlap; overlapping time
+ * counts once) and the launch counts.  Off by default; not for batches captured
+ * in a graph. */
 int ksw2g_batch_set_timing(ksw2g_batch_t *batch, int on);
 int ksw2g_batch_kernel_ms(ksw2g_batch_t *batch, double *dp_ms, double *bt_ms, int *n_dp, int *n_bt);
 

@@ -78,6 +78,11 @@ struct ksw2g_ctx {
   cudaStream_t st = nullptr;
   int nsm = 0;
   int64_t tb_budget = (int64_t)16 << 30;
+  // Waves are cut at tb_budget / wave_div.  With 2, two waves fit the budget at
+  // once, and ksw2g_batch_run alternates them between st and aux so that one
+  // wave's tail overlaps the next wave's start.
+  int wave_div = 2;
+  cudaStream_t aux = nullptr;
   DevBuf tb_pool;       // traceback rows of the running wave
   DevBuf one;           // per-call drop-in scratch (device)
   PinBuf one_h;         // per-call drop-in staging (pinned)
@@ -117,6 +122,7 @@ struct ksw2g_batch {
   std::vector<cudaEvent_t> tev;  // 2 per timed launch
   std::vector<int> tkind;        // 0 DP kernel, 1 backtrack kernel, per timed launch
   int n_timed = 0;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // two-stream runs
 };
 
 
@@ -155,4 +161,10 @@ int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t 
 // Enqueue the DP (+ backtrack) of a prepared extension batch on st, with tb (tb_cap bytes)
 // holding the traceback rows of one wave at a time.
 int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap);
+// The same with the waves alternating between s0 (region tb0) and s1 (region
+// tb1); s1 joins s0's order at the start and s0 waits for s1 at the end.  With
+// s1 null, or fewer than two waves, everything runs on s0 in tb0.
+int ext_run_on2(ksw2g_batch *b, cudaStream_t s0, cudaStream_t s1, uint8_t *tb0, uint8_t *tb1, int64_t tb_cap);
+// Largest wave of a prepared extension batch (bytes, at least 16).
+int64_t ext_max_wave(const ksw2g_batch *b);
 int ll_run_on(ksw2g_batch *b, cudaStream_t st);

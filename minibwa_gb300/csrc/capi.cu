@@ -105,6 +105,10 @@ extern "C" void ksw2g_ctx_destroy(ksw2g_ctx_t *c) {
   if (c->scratch) ksw2g_batch_free(c->scratch);
   for (ksw2g_ctx *sc : c->sub)
     if (sc) ksw2g_ctx_destroy(sc);
+  if (c->aux) {
+    cudaStreamSynchronize(c->aux);
+    cudaStreamDestroy(c->aux);
+  }
   c->tb_pool.release();
   c->one.release();
   c->one_h.release();
@@ -129,6 +133,8 @@ extern "C" void ksw2g_batch_free(ksw2g_batch_t *b) {
                     &b->counters, &b->llmat, &b->blist, &b->blist_off})
     d->release();
   for (cudaEvent_t e : b->tev) cudaEventDestroy(e);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
   delete b;
 }
 extern "C" int ksw2g_batch_launches(const ksw2g_batch_t *b) { return b ? b->launches : 0; }
@@ -142,13 +148,26 @@ extern "C" int ksw2g_batch_set_timing(ksw2g_batch_t *b, int on) {
 
 extern "C" int ksw2g_batch_kernel_ms(ksw2g_batch_t *b, double *dp_ms, double *bt_ms, int *n_dp, int *n_bt) {
   if (!b) return set_err(KSW2G_E_ARG, "null batch");
+  // Launches of a two-stream run overlap: report, per kernel kind, the length of the
+  // union of the launches' intervals (the plain sum when they run one after another).
   double t[2] = {0, 0};
   int c[2] = {0, 0};
+  std::vector<std::pair<double, double>> iv[2];
   for (int i = 0; i < b->n_timed; ++i) {
-    float ms = 0;
+    float a = 0, z = 0;
     CK(cudaEventSynchronize(b->tev[2 * i + 1]));
-    CK(cudaEventElapsedTime(&ms, b->tev[2 * i], b->tev[2 * i + 1]));
-    t[b->tkind[i]] += ms, ++c[b->tkind[i]];
+    CK(cudaEventElapsedTime(&a, b->tev[0], b->tev[2 * i]));
+    CK(cudaEventElapsedTime(&z, b->tev[0], b->tev[2 * i + 1]));
+    iv[b->tkind[i]].push_back({a, z});
+    ++c[b->tkind[i]];
+  }
+  for (int k = 0; k < 2; ++k) {
+    std::sort(iv[k].begin(), iv[k].end());
+    double end = -1e300;
+    for (auto &x : iv[k]) {
+      if (x.first > end) t[k] += x.second - x.first, end = x.second;
+      else if (x.second > end) t[k] += x.second - end, end = x.second;
+    }
   }
   if (dp_ms) *dp_ms = t[0];
   if (bt_ms) *bt_ms = t[1];
@@ -311,6 +330,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     for (int i = 0; i < n; ++i) srt[cnt[(size_t)(maxkey - ((int64_t)ql[i] + tl[i]))]++] = i;
   }
   b->waves.clear();
+  const int64_t wave_cap = std::max<int64_t>(c->tb_budget / std::max(c->wave_div, 1), 16);
   std::vector<int64_t> tbo(n);
   std::vector<int32_t> ord(n);
   int64_t ordp = 0;
@@ -321,7 +341,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     wv.w0 = i;
     wv.any_cig = false;
     int64_t acc = 0;
-    while (i < n && (acc + foot[srt[i]] <= c->tb_budget || i == wv.w0)) tbo[srt[i]] = acc, acc += foot[srt[i]], ++i;
+    while (i < n && (acc + foot[srt[i]] <= wave_cap || i == wv.w0)) tbo[srt[i]] = acc, acc += foot[srt[i]], ++i;
     wv.w1 = i;
     wv.tb_bytes = acc;
     std::fill(bcount.begin(), bcount.end(), 0);
@@ -394,16 +414,37 @@ static cudaError_t timed_end(ksw2g_batch *b, cudaStream_t st) {
   return r;
 }
 
+int64_t ext_max_wave(const ksw2g_batch *b) {
+  int64_t m = 16;
+  for (const Wave &wv : b->waves) m = std::max(m, wv.tb_bytes);
+  return m;
+}
+
 int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap) {
+  return ext_run_on2(b, st, nullptr, tb, nullptr, tb_cap);
+}
+
+int ext_run_on2(ksw2g_batch *b, cudaStream_t s0, cudaStream_t s1, uint8_t *tb0, uint8_t *tb1, int64_t tb_cap) {
   b->launches = 0;
   if (b->n == 0) return 0;
   for (auto &wv : b->waves)
     if (wv.tb_bytes > tb_cap) return set_err(KSW2G_E_CAPACITY, "traceback wave exceeds the pool");
+  const bool two = s1 && tb1 && b->waves.size() >= 2;
+  if (two && !b->ev_fork) {
+    CK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+  }
+  cudaStream_t st = s0;
+  uint8_t *tb = tb0;
   int *cnt = b->counters.as<int>();
   unsigned long long *cursor = (unsigned long long *)cnt;  // bytes 0..7
   int *err = cnt + 2;                                      // bytes 8..11
   int *jc = cnt + 4;                                       // per-bin job counters
-  CK(cudaMemsetAsync(b->counters.p, 0, 16 + sizeof(int) * (size_t)b->n_counters, st));
+  CK(cudaMemsetAsync(b->counters.p, 0, 16 + sizeof(int) * (size_t)b->n_counters, s0));
+  if (two) {
+    CK(cudaEventRecord(b->ev_fork, s0));
+    CK(cudaStreamWaitEvent(s1, b->ev_fork, 0));
+  }
   const ksw2g_job *dj = b->jobs.as<ksw2g_job>();
   ksw2g_ext_result *dr = b->res.as<ksw2g_ext_result>();
   ksw2g_bt *db = b->bts.as<ksw2g_bt>();
@@ -411,7 +452,10 @@ int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap) {
   const int32_t *dord = b->order.as<int32_t>();
   const int32_t *dsrt = b->sorted.as<int32_t>();
   int ci = 0;
-  for (auto &wv : b->waves) {
+  for (size_t w = 0; w < b->waves.size(); ++w) {
+    const Wave &wv = b->waves[w];
+    st = two && (w & 1) ? s1 : s0;
+    tb = two && (w & 1) ? tb1 : tb0;
     for (auto &bn : wv.bins) {
       ExtLaunch L{dj, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr, db, tb, dto,
                   jc + ci++};
@@ -428,15 +472,25 @@ int ext_run_on(ksw2g_batch *b, cudaStream_t st, uint8_t *tb, int64_t tb_cap) {
       ++b->launches;
     }
   }
+  if (two) {
+    CK(cudaEventRecord(b->ev_join, s1));
+    CK(cudaStreamWaitEvent(s0, b->ev_join, 0));
+  }
   return 0;
 }
 
 static int ext_run(ksw2g_ctx *c, ksw2g_batch *b) {
   CK(cudaSetDevice(c->device));
-  int64_t maxtb = 0;
-  for (auto &wv : b->waves) maxtb = std::max(maxtb, wv.tb_bytes);
+  const int64_t maxtb = ext_max_wave(b), al = (maxtb + 255) & ~(int64_t)255;
   int rc;
-  if ((rc = c->tb_pool.ensure((size_t)std::max<int64_t>(maxtb, 16)))) return rc;
+  if (b->waves.size() >= 2 && 2 * maxtb <= c->tb_budget + 512 && c->wave_div >= 2) {
+    if (!c->aux && cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking) != cudaSuccess)
+      return set_err(KSW2G_E_CUDA, "cudaStreamCreate failed");
+    if ((rc = c->tb_pool.ensure((size_t)(2 * al)))) return rc;
+    uint8_t *tb = c->tb_pool.as<uint8_t>();
+    return ext_run_on2(b, c->st, c->aux, tb, tb + al, maxtb);
+  }
+  if ((rc = c->tb_pool.ensure((size_t)maxtb))) return rc;
   return ext_run_on(b, c->st, c->tb_pool.as<uint8_t>(), (int64_t)c->tb_pool.cap);
 }
 
@@ -486,6 +540,7 @@ static int sub_ctx(ksw2g_ctx *c, int i, ksw2g_ctx **out) {
     c->sub[i]->scratch = new ksw2g_batch;
   }
   c->sub[i]->tb_budget = std::max<int64_t>(c->tb_budget / 2, 1 << 20);
+  c->sub[i]->wave_div = 1;  // each sub-context runs one stream; the two alternate chunks
   *out = c->sub[i];
   return 0;
 }

@@ -16,16 +16,19 @@ __device__ __forceinline__ void band_pad(int r, int qlen, int tlen, int w, int &
   off_end = (en & ~15) + 15;
 }
 
-// One walk over the traceback.  WRITE == false counts CIGAR operations;
-// WRITE == true stores them in final order at out[0..n).
-template <bool WRITE>
-__device__ int bt_walk(const uint8_t *__restrict__ tb, int ncol16, int qlen, int tlen, int w, int i0, int j0,
-                       int rev, int n_total, uint32_t *__restrict__ out) {
+// One walk over the traceback from (i0, j0).  The CIGAR runs are produced last
+// op first; run k (counting from the walk's start) is stored at scratch[-1-k].
+// scratch is the end of the job's own traceback region: the walk reads every
+// row at most once, in decreasing order, and after k runs it has left at least
+// k rows of n_col_*16 >= 32 bytes behind it, so the runs only overwrite rows it
+// has already passed.  Returns the number of runs.
+__device__ int bt_walk(const uint8_t *tb, int ncol16, int qlen, int tlen, int w, int i0, int j0,
+                       uint32_t *scratch) {
   int i = i0, j = j0, state = 0, n = 0, last_op = -1;
   uint32_t run = 0;
   auto push = [&](int op, int len) {
     if (n == 0 || op != last_op) {
-      if (WRITE && n > 0) out[rev ? n - 1 : n_total - n] = run << 4 | (uint32_t)last_op;
+      if (n > 0) scratch[-n] = run << 4 | (uint32_t)last_op;
       ++n, last_op = op, run = (uint32_t)len;
     } else run += (uint32_t)len;
   };
@@ -35,7 +38,8 @@ __device__ int bt_walk(const uint8_t *__restrict__ tb, int ncol16, int qlen, int
     band_pad(r, qlen, tlen, w, off, off_end);
     if (i < off) force = 2;
     if (i > off_end) force = 1;
-    const unsigned t = force < 0 ? __ldg(tb + (size_t)r * ncol16 + (i - off)) : 0u;
+    // a plain load: rows behind the walk are overwritten by its output
+    const unsigned t = force < 0 ? tb[(size_t)r * ncol16 + (i - off)] : 0u;
     if (state == 0) state = t & 7;
     else if (!(t >> (state + 2) & 1)) state = 0;
     if (state == 0) state = t & 7;
@@ -46,13 +50,15 @@ __device__ int bt_walk(const uint8_t *__restrict__ tb, int ncol16, int qlen, int
   }
   if (i >= 0) push(2, i + 1);
   if (j >= 0) push(1, j + 1);
-  if (WRITE && n > 0) out[rev ? n - 1 : n_total - n] = run << 4 | (uint32_t)last_op;
+  if (n > 0) scratch[-n] = run << 4 | (uint32_t)last_op;
   return n;
 }
 
-// One thread per job; jobs order[0..n_jobs) (all jobs when order is null).
+// One thread per job; jobs order[0..n_jobs) (all jobs when order is null).  The
+// walk runs once; its runs are then copied to an exactly sized range of the
+// CIGAR arena, reversed into final order unless KSW_EZ_REV_CIGAR (ksw2.h:168-170).
 __global__ void ext_bt_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ order, int n_jobs,
-                              const ksw2g_bt *__restrict__ bts, const uint8_t *__restrict__ tb_pool,
+                              const ksw2g_bt *__restrict__ bts, uint8_t *tb_pool,
                               const int64_t *__restrict__ tb_off, ksw2g_ext_result *__restrict__ res,
                               uint32_t *__restrict__ cigar_out, unsigned long long *__restrict__ cursor,
                               long long cigar_cap, int *__restrict__ err) {
@@ -70,8 +76,10 @@ __global__ void ext_bt_kernel(const ksw2g_job *__restrict__ jobs, const int32_t 
   int nc = J.qlen < J.tlen ? J.qlen : J.tlen;
   nc = ((nc < w + 1 ? nc : w + 1) + 15) / 16 + 1;
   const int rev = (J.flag & KSW2G_REV_CIGAR) ? 1 : 0;
-  const uint8_t *tb = tb_pool + tb_off[jid];
-  const int n = bt_walk<false>(tb, nc * 16, J.qlen, J.tlen, w, b.i0, b.j0, rev, 0, nullptr);
+  uint8_t *tb = tb_pool + tb_off[jid];
+  // the end of row i0+j0: 16-byte aligned (rows are n_col_*16 bytes, regions 16-byte aligned)
+  uint32_t *scratch = (uint32_t *)(tb + (size_t)(b.i0 + b.j0 + 1) * (nc * 16));
+  const int n = bt_walk(tb, nc * 16, J.qlen, J.tlen, w, b.i0, b.j0, scratch);
   const unsigned long long o = atomicAdd(cursor, (unsigned long long)n);
   if ((long long)(o + n) > cigar_cap) {  // arena too small: report, write nothing
     atomicOr(err, 1);
@@ -79,7 +87,12 @@ __global__ void ext_bt_kernel(const ksw2g_job *__restrict__ jobs, const int32_t 
     res[jid].cigar_off = -1;
     return;
   }
-  bt_walk<true>(tb, nc * 16, J.qlen, J.tlen, w, b.i0, b.j0, rev, n, cigar_out + o);
+  uint32_t *out = cigar_out + o;
+  // scratch[-1] is the last op of the final CIGAR; scratch[-n] the first
+  if (rev)
+    for (int k = 0; k < n; ++k) out[k] = scratch[-1 - k];
+  else
+    for (int k = 0; k < n; ++k) out[k] = scratch[k - n];
   res[jid].n_cigar = n;
   res[jid].cigar_off = (int64_t)o;
 }

@@ -35,7 +35,7 @@ int ext_shape_for(int n_col) {
 }
 
 cudaError_t launch_ext_bt(const ksw2g_job *jobs, const int32_t *order, int n_jobs, const ksw2g_bt *bts,
-                          const uint8_t *tb_pool, const int64_t *tb_off, ksw2g_ext_result *res, uint32_t *cigar_out,
+                          uint8_t *tb_pool, const int64_t *tb_off, ksw2g_ext_result *res, uint32_t *cigar_out,
                           unsigned long long *cursor, long long cigar_cap, int *err, cudaStream_t st) {
   if (n_jobs <= 0) return cudaSuccess;
   const int bs = 128;

@@ -37,7 +37,7 @@ struct ExtLaunch {
 cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,
                           int max_blocks, cudaStream_t st);
 cudaError_t launch_ext_bt(const ksw2g_job *jobs, const int32_t *order, int n_jobs, const ksw2g_bt *bts,
-                          const uint8_t *tb_pool,
+                          uint8_t *tb_pool,
                           const int64_t *tb_off, ksw2g_ext_result *res, uint32_t *cigar_out,
                           unsigned long long *cursor, long long cigar_cap, int *err, cudaStream_t st);
 cudaError_t launch_pack(int n, const uint8_t *raw, const int64_t *raw_off, const int32_t *len, uint8_t *arena,

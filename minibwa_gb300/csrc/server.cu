@@ -347,6 +347,7 @@ extern "C" int ksw2g_server_create(int device, int n_slots, int64_t tb_budget, k
       return report_error(KSW2G_E_CUDA, "server: cudaStreamCreate failed");
     }
     batch_bind_stream(&s->batch, s->ctx.st);
+    s->ctx.wave_div = 1;  // a slot runs its waves on one stream in its own pool range
     S->slots.push_back(s);
     if ((rc = s->res_pin.ensure(1 << 20)) || (rc = s->cig_pin.ensure(8 << 20)) || (rc = s->hdr_pin.ensure(64))) {
       ksw2g_server_destroy(S);

@@ -12,10 +12,11 @@ def _cigars(res, cig):
     return [cig[o:o + n].tolist() for o, n in zip(res["cigar_off"], res["n_cigar"])]
 
 
-def test_mixed_graph_matches_plain_batches(built):
+@pytest.mark.parametrize("budget", [None, 48 << 20])  # 48 MiB: several waves, run on two streams
+def test_mixed_graph_matches_plain_batches(built, budget):
     from minibwa_gb300 import Context, ExtBatch, Graph, LLBatch, synth
     long_, short, resc = synth.config2_long(60), synth.config2_short(3000), synth.config3(2000)
-    ctx = Context(0)
+    ctx = Context(0, tb_budget=budget)
     want_l = ctx.ext_batch(long_.dual, 5, long_.mat, long_.q, long_.e, long_.q2, long_.e2, long_.jobs, long_.qbuf,
                            long_.tbuf)
     want_s = ctx.ext_batch(short.dual, 5, short.mat, short.q, short.e, short.q2, short.e2, short.jobs, short.qbuf,
