@@ -282,6 +282,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
   const uint32_t NGOE = pk(-goe, -goe), NGE = pk(-ge, -ge), NSHIFT = pk(-shift, -shift), C255 = pk(255, 255);
 
   uint32_t H[SLEN], E[SLEN];
+  uint32_t hl = 0;  // H[slen-1], the segment the next row's one-lane shift reads
   int jid = -1, slen = 0, qlen = 0, tlen = 0, xtra = 0, i = 0, te = -1, gmax = 0, n_b = 0, minsc = 0, endsc = 0;
   const uint8_t *tp = nullptr;
   uint64_t *bl = nullptr;
@@ -323,6 +324,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
         bl = (blist && (xtra & KSW2G_LL_SUBO)) ? blist + blist_off[jid] : nullptr;
 #pragma unroll
         for (int s = 0; s < SLEN; ++s) H[s] = 0, E[s] = 0, hm[s * 128] = 0;
+        hl = 0;
         i = 0, te = -1, gmax = 0, n_b = 0;
       }
     }
@@ -333,11 +335,8 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
     if (!done) {
       const int a = tp[i] < m ? tp[i] : m - 1;
       const uint16_t *S = prof + a * SLEN * T + t;
-      uint32_t hlast = H[0];
-#pragma unroll
-      for (int s = 1; s < SLEN; ++s) hlast = (s == slen - 1) ? H[s] : hlast;
       // one-lane shift of the last segment (ksw2_ll_sse.c:146-147): lane l <- lane l-1, lane 0 <- 0
-      const uint32_t up = __shfl_up_sync(gm, hlast, 1, T), wrap = __shfl_sync(gm, hlast, T - 1, T);
+      const uint32_t up = __shfl_up_sync(gm, hl, 1, T), wrap = __shfl_sync(gm, hl, T - 1, T);
       uint32_t h = t ? up : (wrap << 16);
       uint32_t f = 0, mx = 0;
 #pragma unroll
@@ -352,6 +351,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
           mx = __vmaxs2(mx, hv);
           h = H[s];
           H[s] = hv;
+          hl = hv;  // the last segment processed is slen-1
           const uint32_t tt = __viaddmax_s16x2(hv, NGOE, 0u);
           E[s] = __viaddmax_s16x2(E[s], NGE, tt);
           f = __viaddmax_s16x2(f, NGE, tt);
@@ -366,6 +366,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
           if (s < slen && !fin) {
             const uint32_t hv = __vmaxs2(H[s], f);
             H[s] = hv;
+            if (s == slen - 1) hl = hv;
             const uint32_t hh = __viaddmax_s16x2(hv, NGOE, 0u);
             f = __viaddmax_s16x2(f, NGE, 0u);
             fin = __all_sync(gm, (__vmaxs2(f, hh) ^ hh) == 0u);  // f <= hh in every lane
