@@ -212,27 +212,37 @@ ll_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__re
 
 namespace ksw2g {
 
-// Bytes 0 and 1 of x into the low and high halfwords, sign-extended when SIGNED
-// (PTX prmt, default mode: selector bit 3 replicates the selected byte's sign).
-template <bool SIGNED>
+// Bytes 2H and 2H+1 of x into the low and high halfwords, sign-extended when
+// SIGNED (PTX prmt, default mode: selector bit 3 replicates the selected byte's sign).
+template <bool SIGNED, int H>
 __device__ __forceinline__ uint32_t widen2(uint32_t x) {
 #if defined(__CUDA_ARCH__)
   uint32_t r;
-  if (SIGNED) asm("prmt.b32 %0, %1, 0, 0x9180;" : "=r"(r) : "r"(x));
-  else asm("prmt.b32 %0, %1, 0, 0x4140;" : "=r"(r) : "r"(x));
+  if (SIGNED && H == 0) asm("prmt.b32 %0, %1, 0, 0x9180;" : "=r"(r) : "r"(x));
+  else if (SIGNED) asm("prmt.b32 %0, %1, 0, 0xb3a2;" : "=r"(r) : "r"(x));
+  else if (H == 0) asm("prmt.b32 %0, %1, 0, 0x4140;" : "=r"(r) : "r"(x));
+  else asm("prmt.b32 %0, %1, 0, 0x4342;" : "=r"(r) : "r"(x));
   return r;
 #else
-  const uint32_t b0 = x & 0xffu, b1 = (x >> 8) & 0xffu;
+  const uint32_t b0 = (x >> (16 * H)) & 0xffu, b1 = (x >> (16 * H + 8)) & 0xffu;
   if (SIGNED) return (uint32_t)(uint16_t)(int16_t)(int8_t)b0 | ((uint32_t)(uint16_t)(int16_t)(int8_t)b1 << 16);
   return b0 | (b1 << 16);
 #endif
 }
 
-// Word offset, in the DPX kernel's dynamic shared memory, of the per-thread
-// Hmax columns that follow the groups' profiles (16-byte aligned).
+// Shared-memory layout of the DPX kernel.  Each thread's profile row (one residue, all
+// its segments, two lane bytes per segment) is contiguous and padded to SP segments,
+// SP = 8 (mod 16), so a 16-byte load brings 8 segments and the rows of the threads of
+// a quarter-warp start on different banks; a group's rows are followed by padding that
+// puts the next group's on the other half of the banks.  The per-thread Hmax columns
+// follow all the profiles.
+__host__ __device__ constexpr int ll_dpx_sp(int slen) { return ((slen + 7) / 16) * 16 + 8; }
+__host__ __device__ inline int ll_dpx_group_words(int m, int slen, int T) {
+  const int w = m * T * ll_dpx_sp(slen) / 2;
+  return w + (16 - w % 32 + 32) % 32;
+}
 __host__ __device__ inline int ll_dpx_hm_offset(int m, int slen, int T) {
-  const int prof_entries = (128 / T) * (m * slen * T + 2 * T);
-  return ((prof_entries * 2 + 15) / 16) * 4;
+  return (128 / T) * ll_dpx_group_words(m, slen, T);
 }
 // Dynamic shared memory of one 128-thread block of the DPX kernel.
 inline size_t ll_dpx_smem_bytes(int m, int slen, int T) {
@@ -264,8 +274,8 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
   // entry: lanes t and t+T), then the best-row copy of H of every thread (Hmax of the
   // reference) in a thread-interleaved column, which is written only when the maximum grows.
   extern __shared__ uint32_t lld_smem[];
-  const int prof_stride = m * SLEN * T + 2 * T;  // entries; +2T staggers the groups over the banks
-  uint16_t *prof = (uint16_t *)lld_smem + grp * prof_stride;
+  constexpr int SP = ll_dpx_sp(SLEN);
+  uint16_t *prof = (uint16_t *)(lld_smem + grp * ll_dpx_group_words(m, SLEN, T));
   uint32_t *hm = lld_smem + ll_dpx_hm_offset(m, SLEN, T) + threadIdx.x;  // hm[s * 128]
 
   int shift = 127, mdiff = 0;  // ksw2_ll_sse.c:66-74
@@ -315,7 +325,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
                 const int v = k >= qlen ? -1 : mat_g[a * m + (qc < m ? qc : m - 1)];  // codes must be < m
                 v2[h] = SIZE == 1 ? ((v + shift) & 0xff) : v;  // u8: 0..255; i16: an int8 score
               }
-              prof[(a * SLEN + s) * T + t] = (uint16_t)((v2[0] & 0xff) | ((v2[1] & 0xff) << 8));
+              prof[(a * T + t) * SP + s] = (uint16_t)((v2[0] & 0xff) | ((v2[1] & 0xff) << 8));
             }
           }
         __syncwarp(gm);
@@ -334,16 +344,19 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
     bool done = i >= tlen;
     if (!done) {
       const int a = tp[i] < m ? tp[i] : m - 1;
-      const uint16_t *S = prof + a * SLEN * T + t;
+      const uint4 *S4 = (const uint4 *)(prof + (a * T + t) * SP);  // 8 segments per 16-byte load
       // one-lane shift of the last segment (ksw2_ll_sse.c:146-147): lane l <- lane l-1, lane 0 <- 0
       const uint32_t up = __shfl_up_sync(gm, hl, 1, T), wrap = __shfl_sync(gm, hl, T - 1, T);
       uint32_t h = t ? up : (wrap << 16);
       uint32_t f = 0, mx = 0;
+      uint4 q8 = make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int s = 0; s < SLEN; ++s) {
+        if ((s & 7) == 0 && s < slen) q8 = S4[s >> 3];
         if (s < slen) {
-          // widen the entry's two bytes to the two halfwords: zero-extended (u8) or sign-extended (i16)
-          const uint32_t sc = widen2<SIZE == 2>((uint32_t)S[s * T]);
+          // widen the segment's two bytes to the two halfwords: zero-extended (u8) or sign-extended (i16)
+          const uint32_t qw = (s & 7) < 2 ? q8.x : (s & 7) < 4 ? q8.y : (s & 7) < 6 ? q8.z : q8.w;
+          const uint32_t sc = (s & 1) ? widen2<SIZE == 2, 1>(qw) : widen2<SIZE == 2, 0>(qw);
           uint32_t hv;
           if (SIZE == 1) hv = __viaddmax_s16x2(__viaddmin_s16x2(h, sc, C255), NSHIFT, 0u);
           else hv = __vadd2(h, sc);

@@ -30,6 +30,11 @@
 #define __restrict__
 #define __shared__
 
+struct uint4 {
+  uint32_t x, y, z, w;
+};
+inline uint4 make_uint4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) { return uint4{x, y, z, w}; }
+
 struct emu_dim3 {
   unsigned x = 0, y = 0, z = 0;
 };

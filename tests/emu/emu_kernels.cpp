@@ -22,8 +22,8 @@ LaneState g_lane_state[1024];
 #include "../../minibwa_gb300/csrc/shapes.h"
 
 namespace ksw2g {
-int16_t ll_smem[1 << 20];
-uint32_t lld_smem[1 << 20];
+alignas(16) int16_t ll_smem[1 << 20];
+alignas(16) uint32_t lld_smem[1 << 20];
 }
 
 using namespace ksw2g;
