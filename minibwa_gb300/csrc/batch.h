@@ -112,6 +112,9 @@ struct ksw2g_batch {
   ksw2g_ext_params P;
   int ll_m = 0, ll_gapo = 0, ll_gape = 0, ll_size = 1, ll_slen = 0, ll_qlen_max = 0, ll_mat_max = 0, ll_force = 0;
   DevBuf raw, rawmeta, arena, jobs, order, sorted, tb_off, res, bts, cigar, counters, llmat, blist, blist_off;
+  DevBuf wide;            // block scratch of wide-band jobs: two halves of wide_blocks x wide_stride
+  int64_t wide_stride = 0;
+  int wide_blocks = 0;
   int64_t cigar_cap = 0;
   int n_counters = 0;
   std::vector<Wave> waves;
@@ -129,7 +132,7 @@ struct ksw2g_batch {
 // Make every device buffer of the batch grow in stream order on st.
 inline void batch_bind_stream(ksw2g_batch *b, cudaStream_t st) {
   for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts,
-                    &b->cigar, &b->counters, &b->llmat, &b->blist, &b->blist_off})
+                    &b->cigar, &b->counters, &b->llmat, &b->blist, &b->blist_off, &b->wide})
     d->st = st;
 }
 

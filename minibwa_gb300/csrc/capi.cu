@@ -29,6 +29,7 @@ cudaError_t launch_ext_dp_d2(int mode, int shape, const ksw2g_ext_params &P, con
                              cudaStream_t st);
 cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,
                           int max_blocks, cudaStream_t st) {
+  if (shape == kWideShape) return launch_ext_wide(P, L, st);
   return dual ? launch_ext_dp_d2(mode, shape, P, L, max_blocks, st)
               : launch_ext_dp_z2(mode, shape, P, L, max_blocks, st);
 }
@@ -130,7 +131,7 @@ extern "C" int ksw2g_ctx_set_tb_budget(ksw2g_ctx_t *c, int64_t bytes) {
 extern "C" void ksw2g_batch_free(ksw2g_batch_t *b) {
   if (!b) return;
   for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts, &b->cigar,
-                    &b->counters, &b->llmat, &b->blist, &b->blist_off})
+                    &b->counters, &b->llmat, &b->blist, &b->blist_off, &b->wide})
     d->release();
   for (cudaEvent_t e : b->tev) cudaEventDestroy(e);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
@@ -285,7 +286,8 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   std::vector<int32_t> ql(n), tl(n);
   std::vector<int> shape(n), mode(n);
   std::vector<int64_t> foot(n);
-  int64_t cig = 0;
+  int64_t cig = 0, wide_max = 0;
+  int n_wide = 0;
   for (int i = 0; i < n; ++i) {
     const ksw2g_job_t &J = jobs[i];
     if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
@@ -297,9 +299,8 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     mode[i] = ext_mode(J.flag);
     const bool live = J.qlen > 0 && J.tlen > 0 && !b->P.skip_all;
     const int nc = live ? ext_ncol(J.qlen, J.tlen, J.w) : 1;
-    shape[i] = ext_shape_pick(dual, mode[i], nc);
-    if (shape[i] < 0)
-      return set_err(KSW2G_E_BAND, "job %d: band of %d 16-byte blocks exceeds the widest kernel shape", i, nc);
+    shape[i] = ext_shape_or_wide(ext_shape_pick(dual, mode[i], nc));
+    if (shape[i] == kWideShape) ++n_wide, wide_max = std::max(wide_max, ext_wide_scratch(J.qlen, J.tlen));
     foot[i] = (live && mode[i] != 0) ? (((int64_t)(J.qlen + J.tlen - 1) * nc * 16 + 15) & ~(int64_t)15) : 0;
     if (foot[i] > c->tb_budget)
       return set_err(KSW2G_E_CAPACITY, "job %d: traceback needs %lld bytes, budget %lld", i, (long long)foot[i],
@@ -334,7 +335,8 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   std::vector<int64_t> tbo(n);
   std::vector<int32_t> ord(n);
   int64_t ordp = 0;
-  const int nbins = 3 * kNumExtShapes;
+  const int nshp = kNumExtShapes + 1;  // the instantiated shapes and the block-wide kernel
+  const int nbins = 3 * nshp;
   std::vector<int32_t> bcount(nbins), bpos(nbins);
   for (int i = 0; i < n;) {
     Wave wv;
@@ -345,16 +347,16 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     wv.w1 = i;
     wv.tb_bytes = acc;
     std::fill(bcount.begin(), bcount.end(), 0);
-    for (int k = wv.w0; k < wv.w1; ++k) ++bcount[mode[srt[k]] * kNumExtShapes + shape[srt[k]]];
+    for (int k = wv.w0; k < wv.w1; ++k) ++bcount[mode[srt[k]] * nshp + shape[srt[k]]];
     for (int bi = 0; bi < nbins; ++bi) {
       bpos[bi] = (int32_t)ordp;
       if (bcount[bi]) {
-        wv.bins.push_back(Bin{bi / kNumExtShapes, bi % kNumExtShapes, ordp, bcount[bi]});
-        wv.any_cig |= bi / kNumExtShapes != 0;
+        wv.bins.push_back(Bin{bi / nshp, bi % nshp, ordp, bcount[bi]});
+        wv.any_cig |= bi / nshp != 0;
       }
       ordp += bcount[bi];
     }
-    for (int k = wv.w0; k < wv.w1; ++k) ord[bpos[mode[srt[k]] * kNumExtShapes + shape[srt[k]]]++] = srt[k];
+    for (int k = wv.w0; k < wv.w1; ++k) ord[bpos[mode[srt[k]] * nshp + shape[srt[k]]]++] = srt[k];
     b->waves.push_back(wv);
   }
   b->n_counters = 0;
@@ -366,6 +368,14 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   if ((rc = b->res.ensure(sizeof(ksw2g_ext_result) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->bts.ensure(sizeof(ksw2g_bt) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->counters.ensure(16 + sizeof(int) * (size_t)std::max(b->n_counters, 1)))) return rc;
+  // block scratch of the wide-band jobs: one area per resident block, in two halves for two-stream runs
+  b->wide_blocks = 0, b->wide_stride = 0;
+  if (n_wide) {
+    if (!c->nsm) c->nsm = num_sms(c->device);
+    b->wide_blocks = std::min(n_wide, std::max(c->nsm, 1) * 2);
+    b->wide_stride = wide_max;
+    if ((rc = b->wide.ensure((size_t)(2 * b->wide_blocks) * (size_t)wide_max))) return rc;
+  }
   b->cigar_cap = std::max<int64_t>(cig, 16);
   if ((rc = b->cigar.ensure(sizeof(uint32_t) * (size_t)b->cigar_cap))) return rc;
   if (n) {
@@ -459,6 +469,9 @@ int ext_run_on2(ksw2g_batch *b, cudaStream_t s0, cudaStream_t s1, uint8_t *tb0, 
     for (auto &bn : wv.bins) {
       ExtLaunch L{dj, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr, db, tb, dto,
                   jc + ci++};
+      if (bn.shape == kWideShape)  // each stream of a two-stream run has its own half of the scratch
+        L.wide_scratch = b->wide.as<uint8_t>() + (size_t)(st == s0 ? 0 : 1) * b->wide_blocks * b->wide_stride,
+        L.wide_stride = b->wide_stride, L.wide_blocks = b->wide_blocks;
       CK(timed_begin(b, 0, st));
       CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, st));
       CK(timed_end(b, st));
@@ -722,11 +735,7 @@ static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen
   ksw2g_ctx *c = thread_ctx();
   const int mode = ext_mode(flag);
   const int nc = ext_ncol(qlen, tlen, w);
-  const int shape = ext_shape_pick(dual, mode, nc);
-  if (shape < 0) {
-    fprintf(stderr, "[ksw2gpu] fatal: band of %d blocks exceeds the widest kernel shape\n", nc);
-    abort();
-  }
+  const int shape = ext_shape_or_wide(ext_shape_pick(dual, mode, nc));
   const int64_t ncig = mode ? (int64_t)qlen + tlen + 1 : 0;
   const int64_t foot = mode ? (int64_t)(qlen + tlen - 1) * nc * 16 : 0;
   const size_t o_job = 32, o_tbo = o_job + 48, o_bt = o_tbo + 16, o_res = o_bt + 16;
@@ -734,7 +743,9 @@ static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen
   const size_t o_arena = (o_cig + ncig * 4 + 15) & ~(size_t)15;
   const size_t arena_bytes = slot_bytes(qlen) + slot_bytes(tlen);
   const size_t o_tb = (o_arena + arena_bytes + 255) & ~(size_t)255;
-  const size_t total = o_tb + foot + 16;
+  const int64_t wide = shape == kWideShape ? ext_wide_scratch(qlen, tlen) : 0;  // block scratch of a wide band
+  const size_t o_wide = (o_tb + foot + 255) & ~(size_t)255;
+  const size_t total = o_wide + wide + 16;
   if (c->one.ensure(total) || c->one_h.ensure(o_tb)) {
     fprintf(stderr, "[ksw2gpu] fatal: %s\n", tl_err.c_str());
     abort();
@@ -754,6 +765,7 @@ static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen
   DIE_ON(cudaMemcpyAsync(d + o_arena, h + o_arena, arena_bytes, cudaMemcpyHostToDevice, c->st));
   ExtLaunch L{(const ksw2g_job *)(d + o_job), nullptr, 1, d + o_arena, (ksw2g_ext_result *)(d + o_res),
               (ksw2g_bt *)(d + o_bt), d + o_tb, (const int64_t *)(d + o_tbo), (int *)(d + 16)};
+  if (wide) L.wide_scratch = d + o_wide, L.wide_stride = wide, L.wide_blocks = 1;
   DIE_ON(launch_ext_dp(dual, mode, shape, P, L, 1, c->st));
   if (mode)
     DIE_ON(launch_ext_bt((const ksw2g_job *)(d + o_job), nullptr, 1, (const ksw2g_bt *)(d + o_bt), d + o_tb,

@@ -80,8 +80,11 @@ __device__ __forceinline__ uint32_t ld_tw(const uint8_t *tp, int p, int tlen) {
 
 // VAR: 0 = extz2 (affine), 1 = extd2 (dual affine)
 // MODE: 0 = score only, 1 = left-aligned gaps with traceback, 2 = right-aligned gaps with traceback
+#ifndef KSW2G_EXT_MINB4
+#define KSW2G_EXT_MINB4 4  // resident blocks per SM asked of shapes with K <= 4
+#endif
 template <int VAR, int MODE, int G, int K>
-__global__ void __launch_bounds__(128, (K <= 4 ? 4 : (K <= 5 ? 3 : 2)))
+__global__ void __launch_bounds__(128, (K <= 4 ? KSW2G_EXT_MINB4 : (K <= 5 ? 3 : 2)))
 ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ order, int n_jobs,
               const uint8_t *__restrict__ arena, const ksw2g_ext_params P, ksw2g_ext_result *__restrict__ res,
               ksw2g_bt *__restrict__ bts, uint8_t *__restrict__ tb_pool, const int64_t *__restrict__ tb_off,

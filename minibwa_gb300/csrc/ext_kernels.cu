@@ -9,7 +9,8 @@
 #define KSW2G_EXT_VAR 0
 #endif
 #if KSW2G_EXT_VAR == 0
-#include "ext_bt.cuh"  // the backtrack and packing kernels live in the extz2 half only
+#include "ext_bt.cuh"    // the backtrack and packing kernels live in the extz2 half only
+#include "ext_wide.cuh"  // and so does the block-wide kernel (both variants, runtime dual)
 #endif
 
 namespace ksw2g {
@@ -51,6 +52,17 @@ cudaError_t launch_pack(int n, const uint8_t *raw, const int64_t *raw_off, const
   int blocks = (int)(((int64_t)n * 32 + bs - 1) / bs);
   if (blocks > 65535 * 8) blocks = 65535 * 8;
   pack_seqs_kernel<<<blocks, bs, 0, st>>>(n, raw, raw_off, len, arena, dst_off);
+  return cudaGetLastError();
+}
+
+int64_t ext_wide_scratch(int qlen, int tlen) { return (ext_wide_scratch_bytes(qlen, tlen) + 255) & ~(int64_t)255; }
+
+cudaError_t launch_ext_wide(const ksw2g_ext_params &P, const ExtLaunch &L, cudaStream_t st) {
+  if (L.n_jobs <= 0) return cudaSuccess;
+  if (!L.wide_scratch || L.wide_blocks <= 0) return cudaErrorInvalidValue;
+  const int blocks = L.n_jobs < L.wide_blocks ? L.n_jobs : L.wide_blocks;
+  ext_wide_kernel<<<blocks, kWideThreads, 0, st>>>(L.jobs, L.order, L.n_jobs, L.arena, P, L.res, L.bts, L.tb_pool,
+                                                   L.tb_off, L.job_counter, L.wide_scratch, L.wide_stride);
   return cudaGetLastError();
 }
 

@@ -31,7 +31,17 @@ struct ExtLaunch {
   uint8_t *tb_pool;
   const int64_t *tb_off;
   int *job_counter;
+  // wide-band bins only: wide_blocks per-block scratch areas of wide_stride bytes
+  uint8_t *wide_scratch = nullptr;
+  int64_t wide_stride = 0;
+  int wide_blocks = 0;
 };
+// Bands wider than the widest thread-group shape run on the block-wide kernel
+// (ext_wide.cuh); bins and launches use this virtual shape index for them.
+constexpr int kWideShape = KSW2G_NUM_SHAPES;
+inline int ext_shape_or_wide(int s) { return s < 0 ? kWideShape : s; }
+cudaError_t launch_ext_wide(const ksw2g_ext_params &P, const ExtLaunch &L, cudaStream_t st);
+int64_t ext_wide_scratch(int qlen, int tlen);
 
 // Launch the DP kernel of (dual, mode, shape) as a persistent grid.
 cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,

@@ -208,6 +208,179 @@ ll_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__re
   }
 }
 
+
+// Queries of more segments than the register-resident kernels hold: the same
+// one-lane-per-thread recurrences, with the striped profile, H, E and the
+// best-row copy of H in shared memory (int16 entries, [segment][lane]), one job
+// per block of LANES threads and dynamic segment loops.  slen_cap is the
+// number of segments the block's shared memory was sized for.
+template <int SIZE>
+__global__ void __launch_bounds__(16)
+ll_wide_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__restrict__ arena,
+          const int8_t *__restrict__ mat_g, int m, int gapo, int gape, ksw2g_ll_result *__restrict__ res,
+          uint64_t *__restrict__ blist, const int64_t *__restrict__ blist_off, int *__restrict__ job_counter,
+          int slen_cap) {
+  constexpr int LANES = SIZE == 1 ? 16 : 8;
+  const int l = threadIdx.x;
+  const unsigned gm = (1u << LANES) - 1u;
+  extern __shared__ int16_t llw_smem[];
+  int16_t *prof = llw_smem;                           // [m][slen_cap][LANES]
+  int16_t *Hs = prof + (size_t)m * slen_cap * LANES;  // [slen_cap][LANES]
+  int16_t *Es = Hs + (size_t)slen_cap * LANES;
+  int16_t *HMs = Es + (size_t)slen_cap * LANES;
+
+  // scoring constants (ksw2_ll_sse.c:66-74)
+  int shift = 127, mdiff = 0;
+  for (int a = 0; a < m * m; ++a) {
+    const int v = mat_g[a];
+    if (v < (int)(int8_t)(uint8_t)shift) shift = (uint8_t)v;
+    if (v > (int)(int8_t)(uint8_t)mdiff) mdiff = (uint8_t)v;
+  }
+  const int qmax = mdiff;
+  shift = (256 - shift) & 0xff;
+  const int goe = SIZE == 1 ? ((gapo + gape) & 0xff) : (int)(int16_t)(gapo + gape);
+  const int ge = SIZE == 1 ? (gape & 0xff) : (int)(int16_t)gape;
+
+  int jid = -1, slen = 0, qlen = 0, tlen = 0, xtra = 0, i = 0, te = -1, gmax = 0, n_b = 0, minsc = 0, endsc = 0;
+  const uint8_t *tp = nullptr;
+  uint64_t *bl = nullptr;
+  bool active = false, need = true;
+
+  // saturating lane ops (s2n-lite.h / SSE semantics)
+  auto adds = [&](int a, int b) -> int {
+    if (SIZE == 1) { const int s = a + b; return s > 255 ? 255 : s; }
+    const int s = a + b; return s > 32767 ? 32767 : s < -32768 ? -32768 : s;
+  };
+  auto subsu = [&](int a, int b) -> int {  // unsigned saturating subtract on the lane width
+    if (SIZE == 1) return a > b ? a - b : 0;
+    const unsigned x = (uint16_t)a, y = (uint16_t)b;
+    return (int)(int16_t)(uint16_t)(x > y ? x - y : 0u);
+  };
+  auto vmax = [&](int a, int b) -> int { return a > b ? a : b; };  // max_epu8 on 0..255 / max_epi16
+
+  for (;;) {
+    if (need) {
+      int j = 0;
+      if (l == 0) j = atomicAdd(job_counter, 1);
+      j = __shfl_sync(gm, j, 0, LANES);
+      need = false;
+      active = j < n_jobs;
+      if (active) {
+        jid = j;
+        const ksw2g_ll_job J = jobs[jid];
+        qlen = J.qlen, tlen = J.tlen, xtra = J.xtra;
+        slen = (qlen + LANES - 1) / LANES;
+        tp = arena + J.toff;
+        const uint8_t *qp = arena + J.qoff;
+        // striped profile: lane l of segment s scores query position s + l*slen
+        __syncwarp(gm);
+        for (int a = 0; a < m; ++a)
+          for (int s = 0; s < slen; ++s) {
+            const int k = s + l * slen;
+            const int qc = k >= qlen ? 0 : qp[k];
+            const int v = k >= qlen ? -1 : mat_g[a * m + (qc < m ? qc : m - 1)];  // codes must be < m
+            prof[(a * slen_cap + s) * LANES + l] = (int16_t)(SIZE == 1 ? ((v + shift) & 0xff) : v);
+          }
+        __syncwarp(gm);
+        minsc = (xtra & KSW2G_LL_SUBO) ? (xtra & 0xffff) : 0x10000;
+        endsc = (xtra & KSW2G_LL_STOP) ? (xtra & 0xffff) : 0x10000;
+        bl = (blist && (xtra & KSW2G_LL_SUBO)) ? blist + blist_off[jid] : nullptr;
+        for (int s = 0; s < slen; ++s) Hs[s * LANES + l] = 0, Es[s * LANES + l] = 0, HMs[s * LANES + l] = 0;
+        i = 0, te = -1, gmax = 0, n_b = 0;
+        if (tlen <= 0) {
+          // no rows: fall through to the result with gmax = 0
+        }
+      }
+    }
+    if (!active) break;  // one job per block: active is uniform
+
+
+    bool done = i >= tlen;
+    if (!done) {
+      // ---- target row i (ksw2_ll_sse.c:142-201) ----
+      const int a = tp[i] < m ? tp[i] : m - 1;  // codes must be < m; clamp keeps the read inside the profile
+      const int16_t *S = prof + a * slen_cap * LANES + l;
+      int hlast = slen > 0 ? Hs[(slen - 1) * LANES + l] : 0;
+      int h = __shfl_up_sync(gm, hlast, 1, LANES);
+      if (l == 0) h = 0;
+      int f = 0, mx = 0;
+      for (int s = 0; s < slen; ++s) {
+        const int sc = S[s * LANES];
+        int hv;
+        if (SIZE == 1) hv = subsu(adds(h, sc & 0xff), shift);
+        else hv = adds(h, sc);
+        const int ev = Es[s * LANES + l];
+        hv = vmax(hv, ev);
+        hv = vmax(hv, f);
+        mx = vmax(mx, hv);
+        h = Hs[s * LANES + l];  // H(i-1, s): diagonal predecessor of segment s+1
+        Hs[s * LANES + l] = (int16_t)hv;
+        Es[s * LANES + l] = (int16_t)vmax(subsu(ev, ge), subsu(hv, goe));
+        f = vmax(subsu(f, ge), subsu(hv, goe));
+      }
+      // lazy-F (ksw2_ll_sse.c:175-185 / 287-297)
+      bool fin = false;
+      for (int kk = 0; kk < 16 && !fin; ++kk) {
+        int fs = __shfl_up_sync(gm, f, 1, LANES);
+        f = l == 0 ? 0 : fs;
+        for (int s = 0; s < slen && !fin; ++s) {
+          const int hv = vmax(Hs[s * LANES + l], f);
+          Hs[s * LANES + l] = (int16_t)hv;
+          const int hh = subsu(hv, goe);
+          f = subsu(f, ge);
+          const bool ok = SIZE == 1 ? (f <= hh) : !(f > hh);
+          fin = __all_sync(gm, ok);
+        }
+      }
+      int imax = mx;
+#pragma unroll
+      for (int off = LANES / 2; off > 0; off >>= 1) imax = vmax(imax, __shfl_xor_sync(gm, imax, off, LANES));
+      if (imax >= minsc && bl != nullptr && l == 0) {  // second-best bookkeeping (ksw2_ll_sse.c:188-193)
+        if (n_b == 0 || (int32_t)bl[n_b - 1] + 1 != i) bl[n_b++] = (uint64_t)imax << 32 | (uint32_t)i;
+        else if ((int)(bl[n_b - 1] >> 32) < imax) bl[n_b - 1] = (uint64_t)imax << 32 | (uint32_t)i;
+      }
+      if (imax >= minsc && bl != nullptr) n_b = __shfl_sync(gm, n_b, 0, LANES);
+      if (imax > gmax) {
+        gmax = imax, te = i;
+        for (int s = 0; s < slen; ++s) HMs[s * LANES + l] = Hs[s * LANES + l];
+        if ((SIZE == 1 && gmax + shift >= 255) || gmax >= endsc) done = true;
+      }
+      ++i;
+      if (i >= tlen) done = true;
+    }
+    if (done) {
+      // ---- result (ksw2_ll_sse.c:202-219 / 314-330) ----
+      ksw2g_ll_result o;
+      o.score = SIZE == 1 ? (gmax + shift < 255 ? gmax : 255) : gmax;
+      o.te = te, o.qe = -1, o.score2 = -1, o.te2 = -1, o.rows = i;
+      if (SIZE == 2 || o.score != 255) {
+        // max over Hmax in memory order, ties to the smallest query index
+        uint32_t best = 0;
+        bool any = false;
+        for (int s = 0; s < slen; ++s) {
+          const int hmv = HMs[s * LANES + l];
+          const uint32_t v = SIZE == 1 ? (uint32_t)hmv : (uint32_t)(uint16_t)hmv;
+          const uint32_t key = (v << 16) | (uint32_t)(0xffff - (s + l * slen));
+          if (!any || key > best) best = key, any = true;
+        }
+#pragma unroll
+        for (int off = LANES / 2; off > 0; off >>= 1) best = max(best, __shfl_xor_sync(gm, best, off, LANES));
+        if (slen > 0) o.qe = 0xffff - (int)(best & 0xffff);
+        if (bl != nullptr && l == 0 && n_b > 0) {
+          const int c = qmax > 0 ? (o.score + qmax - 1) / qmax : 0;
+          const int low = te - c, high = te + c;
+          for (int b = 0; b < n_b; ++b) {
+            const int e = (int32_t)bl[b];
+            if ((e < low || e > high) && (int)(bl[b] >> 32) > o.score2) o.score2 = (int)(bl[b] >> 32), o.te2 = e;
+          }
+        }
+      }
+      if (l == 0) res[jid] = o;
+      need = true;
+    }
+  }
+}
+
 }  // namespace ksw2g
 
 namespace ksw2g {

@@ -19,7 +19,50 @@ static const ll_fn kLLD[2][kNumSlenD] = {
     {ll_dpx_kernel<2, 8>, ll_dpx_kernel<2, 16>, ll_dpx_kernel<2, 20>, ll_dpx_kernel<2, 24>, ll_dpx_kernel<2, 32>,
      ll_dpx_kernel<2, 48>}};
 
-int ll_slen_cap(int size) { (void)size; return 64; }
+// Segments of the longest query: the register-resident kernels hold 64; the
+// shared-memory kernel holds as many as fit its block's shared memory.
+static int wide_smem_cap() {
+  static int cap = 0;
+  if (!cap) {
+    int d = 0, v = 0;
+    cudaGetDevice(&d);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, d) != cudaSuccess || v <= 0) v = 48 * 1024;
+    cap = v;
+  }
+  return cap;
+}
+static size_t wide_smem_bytes(int size, int m, int slen) {
+  const int lanes = size == 1 ? 16 : 8;
+  return (size_t)(m + 3) * slen * lanes * sizeof(int16_t);
+}
+int ll_slen_cap(int size) {
+  int s = 64;
+  while (wide_smem_bytes(size, 16, s * 2) <= (size_t)wide_smem_cap()) s *= 2;
+  while (wide_smem_bytes(size, 16, s + 64) <= (size_t)wide_smem_cap()) s += 64;
+  return s;
+}
+
+static cudaError_t launch_wide(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st) {
+  typedef void (*wide_fn)(const ksw2g_ll_job *, int, const uint8_t *, const int8_t *, int, int, int,
+                          ksw2g_ll_result *, uint64_t *, const int64_t *, int *, int);
+  const wide_fn fn = size == 1 ? ll_wide_kernel<1> : ll_wide_kernel<2>;
+  const size_t smem = wide_smem_bytes(size, L.m, slen_max);
+  if (smem > (size_t)wide_smem_cap()) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int lanes = size == 1 ? 16 : 8;
+  int occ = 0, sms = 0, d = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, lanes, smem);
+  cudaGetDevice(&d);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+  int blocks = L.n_jobs;
+  const int cap = sms * (occ > 0 ? occ : 1);
+  if (blocks > cap) blocks = cap;
+  if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
+  fn<<<blocks, lanes, smem, st>>>(L.jobs, L.n_jobs, L.arena, L.mat, L.m, L.gapo, L.gape, L.res, L.blist,
+                                  L.blist_off, L.job_counter, slen_max);
+  return cudaGetLastError();
+}
 
 bool ll_dpx_exact(int size, const LLLaunch &L) {
   if (size == 1) return true;
@@ -67,13 +110,14 @@ cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks,
     cudaError_t e = launch_dpx(size, slen_max, L, max_blocks, st, done);
     if (e != cudaSuccess || done) return e;
   }
+  if (size != 1 && size != 2) return cudaErrorInvalidValue;
   int si = -1;
   for (int i = 0; i < 4; ++i)
     if (slen_max <= kSlen[i]) {
       si = i;
       break;
     }
-  if (si < 0 || (size != 1 && size != 2)) return cudaErrorInvalidValue;
+  if (si < 0) return launch_wide(size, slen_max, L, max_blocks, st);
   const ll_fn fn = kLL[size - 1][si];
   const int lanes = size == 1 ? 16 : 8, groups = 128 / lanes;
   const size_t smem = (size_t)groups * (L.m * kSlen[si] * lanes + 8) * sizeof(int16_t);

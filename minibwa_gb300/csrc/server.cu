@@ -373,7 +373,7 @@ extern "C" void ksw2g_server_destroy(ksw2g_server_t *S) {
     cudaStreamSynchronize(s->ctx.st);
     for (DevBuf *d : {&s->batch.raw, &s->batch.rawmeta, &s->batch.arena, &s->batch.jobs, &s->batch.order,
                       &s->batch.sorted, &s->batch.tb_off, &s->batch.res, &s->batch.bts, &s->batch.cigar,
-                      &s->batch.counters, &s->batch.llmat, &s->batch.blist, &s->batch.blist_off})
+                      &s->batch.counters, &s->batch.llmat, &s->batch.blist, &s->batch.blist_off, &s->batch.wide})
       d->release();
     cudaStreamSynchronize(s->ctx.st);
     s->res_pin.release(), s->cig_pin.release(), s->hdr_pin.release();

@@ -29,6 +29,7 @@
 #define __launch_bounds__(...)
 #define __restrict__
 #define __shared__
+#define KSW2G_EMU 1
 
 struct uint4 {
   uint32_t x, y, z, w;
@@ -85,6 +86,7 @@ struct Warp {
 };
 
 extern Warp *g_warps;  // one per warp of the emulated block
+extern Barrier *g_block;  // all threads of the emulated block (__syncthreads)
 
 // last collective of each emulated thread, for the watchdog of run_block
 struct LaneState {
@@ -175,6 +177,7 @@ inline unsigned __reduce_max_sync(unsigned mask, unsigned v) { return (unsigned)
 inline int __all_sync(unsigned mask, int pred) { return __ballot_sync(mask, pred) == (mask & emu::warp().present); }
 inline int __any_sync(unsigned mask, int pred) { return __ballot_sync(mask, pred) != 0; }
 inline void __syncwarp(unsigned mask = 0xffffffffu) { (void)__ballot_sync(mask, 1); }
+inline void __syncthreads() { emu::g_block->arrive(); }
 
 inline uint32_t __byte_perm(uint32_t x, uint32_t y, uint32_t s) {
   uint8_t b[8];

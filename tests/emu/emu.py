@@ -28,7 +28,8 @@ def build():
                                                         os.listdir(os.path.join(ROOT, "minibwa_gb300", "csrc"))]
     if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return
-    subprocess.check_call(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-w", "-o", LIB] + src)
+    subprocess.check_call(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-w",
+                           "-DKSW2G_WIDE_THREADS=64", "-o", LIB] + src)
 
 
 _L = None
@@ -105,13 +106,16 @@ def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=N
     mat = np.ascontiguousarray(mat, np.int8)
     L.emu_derive_params(int(dual), m, mat.ctypes.data, q, e, q2, e2, P.ctypes.data)
     mode = 0 if flag & 1 else (2 if flag & 2 else 1)
+    wide = L.emu_num_shapes()  # index of the block-wide kernel
     need = max(shape_for(ncol(len(a), len(b), w)) for a, b in zip(qs, ts))
+    if need < 0:
+        need = wide
     if shape is None:
         shape = need
-    if L.emu_shape_words(shape) < L.emu_shape_words(need):
+    if shape != wide and (need == wide or L.emu_shape_words(shape) < L.emu_shape_words(need)):
         raise ValueError("shape too small for the band")
     if threads is None:  # one thread group per emulated warp
-        threads = L.emu_shape_threads(shape)
+        threads = L.emu_shape_threads(shape) if shape != wide else 0
     foot = [((len(a) + len(b) - 1) * ncol(len(a), len(b), w) * 16 + 15) & ~15 if mode else 0 for a, b in zip(qs, ts)]
     tb_off = np.concatenate([[0], np.cumsum(foot)[:-1]]).astype(np.int64)
     tb = np.zeros(max(sum(foot), 16), np.uint8)

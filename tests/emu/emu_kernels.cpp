@@ -12,11 +12,13 @@ thread_local emu_dim3 threadIdx, blockIdx;
 emu_dim3 blockDim, gridDim;
 namespace emu {
 Warp *g_warps = nullptr;
+Barrier *g_block = nullptr;
 LaneState g_lane_state[1024];
 }
 
 #include "../../minibwa_gb300/csrc/ext_bt.cuh"
 #include "../../minibwa_gb300/csrc/ext_dp.cuh"
+#include "../../minibwa_gb300/csrc/ext_wide.cuh"
 #include "../../minibwa_gb300/csrc/host_common.h"
 #include "../../minibwa_gb300/csrc/ll.cuh"
 #include "../../minibwa_gb300/csrc/shapes.h"
@@ -24,6 +26,7 @@ LaneState g_lane_state[1024];
 namespace ksw2g {
 alignas(16) int16_t ll_smem[1 << 20];
 alignas(16) uint32_t lld_smem[1 << 20];
+alignas(16) int16_t llw_smem[1 << 22];
 }
 
 using namespace ksw2g;
@@ -38,6 +41,9 @@ static void run_block(int nthreads, F f) {
     warps[w].present = n == 32 ? 0xffffffffu : ((1u << n) - 1u);
   }
   emu::g_warps = warps.data();
+  emu::Barrier block_bar;
+  block_bar.need = nthreads;
+  emu::g_block = &block_bar;
   std::vector<std::thread> th;
   for (int t = 0; t < nthreads; ++t)
     th.emplace_back([=] {
@@ -84,11 +90,21 @@ void emu_derive_params(int dual, int m, const int8_t *mat, int q, int e, int q2,
 int emu_ext(int dual, int mode, int shape, const ksw2g_ext_params *P, int n, const ksw2g_job *jobs,
             const uint8_t *arena, ksw2g_ext_result *res, ksw2g_bt *bts, uint8_t *tb_pool, const int64_t *tb_off,
             uint32_t *cigar, long long cap, int threads) {
-  if (shape < 0 || shape >= KSW2G_NUM_SHAPES) return -1;
+  if (shape < 0 || shape > KSW2G_NUM_SHAPES) return -1;
   int counter = 0;
-  const ext_fn f = kTab[shape][dual][mode];
   const ksw2g_ext_params Pc = *P;
-  run_block(threads, [&] { f(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter); });
+  if (shape == KSW2G_NUM_SHAPES) {  // the block-wide kernel, one emulated block
+    int64_t stride = 0;
+    for (int j = 0; j < n; ++j) stride = std::max(stride, ext_wide_scratch_bytes(jobs[j].qlen, jobs[j].tlen));
+    std::vector<uint8_t> scratch((size_t)stride + 256);
+    uint8_t *sp = (uint8_t *)(((uintptr_t)scratch.data() + 255) & ~(uintptr_t)255);
+    run_block(kWideThreads, [&] {
+      ext_wide_kernel(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter, sp, stride);
+    });
+  } else {
+    const ext_fn f = kTab[shape][dual][mode];
+    run_block(threads, [&] { f(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter); });
+  }
   if (mode != 0) {
     unsigned long long cursor = 0;
     int err = 0;
@@ -131,6 +147,15 @@ int emu_ll(int size, int slen_max, int n, const ksw2g_ll_job *jobs, const uint8_
         break;
       }
     threads = (size == 1 ? 8 : 4) * (threads / (size == 1 ? 16 : 8));
+  }
+  if (!f && !dpx && slen_max > 64) {  // long queries: the shared-memory kernel, one job per LANES threads
+    const int lanes = size == 1 ? 16 : 8;
+    if ((size_t)(m + 3) * slen_max * lanes > sizeof(llw_smem) / sizeof(int16_t)) return -3;
+    run_block(lanes, [&] {
+      if (size == 1) ll_wide_kernel<1>(jobs, n, arena, mat, m, gapo, gape, res, blist, blist_off, &counter, slen_max);
+      else ll_wide_kernel<2>(jobs, n, arena, mat, m, gapo, gape, res, blist, blist_off, &counter, slen_max);
+    });
+    return 0;
   }
   if (!f) return -1;
   run_block(threads, [&] { f(jobs, n, arena, mat, m, gapo, gape, res, blist, blist_off, &counter); });

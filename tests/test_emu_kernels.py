@@ -93,3 +93,48 @@ def test_emulated_dpx_ll_kernel_matches_golden(emu, golden):
         assert {f: int(r[f]) for f in LL_FIELDS} == c["out"], (i, c["size"], c["xtra"])
         n += 1
     assert n > 200
+
+
+def test_emulated_long_query_ll_kernel(emu):
+    """Queries beyond the 64 register-resident segments run on the shared-memory kernel."""
+    from oracle import oracle as O
+    from minibwa_gb300 import synth
+    from minibwa_gb300.lib import gen_nt4_mat
+    for size, ql, xtra, mat, go, ge in ((2, 1200, 0, None, 12, 2), (1, 1500, 0x40000 | 19, gen_nt4_mat(1, 4, 0, 1), 6, 1)):
+        r = synth.ll_jobs(6, qlen=ql, tlen_lo=ql, tlen_hi=ql + 600, plant=0.7, size=size, xtra=xtra, mat=mat, gapo=go,
+                          gape=ge, seed=ql)
+        qs = [r.qbuf[o:o + n] for o, n in zip(r.jobs["qoff"], r.jobs["qlen"])]
+        ts = [r.tbuf[o:o + n] for o, n in zip(r.jobs["toff"], r.jobs["tlen"])]
+        got = emu.ll(size, 5, r.mat, r.gapo, r.gape, qs, ts, xtra)
+        want = O.ll_batch("orc", size, 5, r.mat, r.gapo, r.gape, r.jobs, r.qbuf, r.tbuf, 4)
+        for f in ("score", "te", "qe", "score2", "te2"):
+            assert np.array_equal(got[f], want[f]), (size, f, got[f], want[f])
+
+
+def test_emulated_block_wide_kernel(emu):
+    """Bands wider than the widest thread group (here w=-1 on ~1.2 kb pairs: 76+ blocks) run
+    on the block-wide kernel; every flag family against the oracle."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(5)
+    for flag in (0x40, 0x00, 0xc2, 0x41, 0x08, 0x18, 0x04):
+        for dual in (0, 1):
+            qs, ts = [], []
+            for _ in range(2):
+                q = rng.integers(0, 4, int(rng.integers(1100, 1400))).astype(np.uint8)
+                t = q.copy()
+                sub = rng.random(len(t)) < 0.03
+                t[sub] = rng.integers(0, 5, sub.sum())
+                t = np.concatenate([t[:300], rng.integers(0, 4, 7).astype(np.uint8), t[300:],
+                                    rng.integers(0, 4, int(rng.integers(0, 200))).astype(np.uint8)])
+                qs.append(q), ts.append(t)
+            mat = np.array([2 if i // 5 == i % 5 else -8 for i in range(25)], np.int8)
+            mat[20:25] = -1
+            mat[4::5] = -1
+            q2, e2 = (24, 1) if dual else (12, 2)
+            res, cig = emu.ext(dual, 5, mat, 12, 2, q2, e2, qs, ts, -1, 100, 10, flag)
+            for k in range(len(qs)):
+                exp, _ = O.extz(dual, qs[k], ts[k], 5, mat, 12, 2, q2, e2, -1, 100, 10, flag)
+                got = {f: int(res[f][k]) for f in EXT_FIELDS if f in exp}
+                for f in got:
+                    assert got[f] == exp[f], (flag, dual, k, f, got[f], exp[f])
+                assert cig[k] == exp["cigar"], (flag, dual, k)

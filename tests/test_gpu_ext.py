@@ -240,3 +240,39 @@ def test_one_shot_chunked_equals_resident(built):
     n = res["n_cigar"][live].astype(np.int64)
     k = np.argsort(o, kind="stable")
     assert (o[k][1:] >= o[k][:-1] + n[k][:-1]).all() and o[k][-1] + n[k][-1] <= len(cig)
+
+
+def _wide_pairs(n, lo, hi, w, flag, dual, seed):
+    from minibwa_gb300 import synth
+    spec = dict(synth.SPEC_LONG, clip_lo=lo, clip_hi=hi)
+    p = synth.ext_pairs(n, spec, w, 400, 10, flag, dual, seed=seed)
+    return p
+
+
+def test_wide_bands_block_kernel(ctx):
+    """Bands wider than the widest thread group (long reads' end extension with w up to
+    bw_long): batched alone, mixed with narrow pairs in one batch, and over many waves."""
+    from minibwa_gb300 import Context
+    for flag in (0x40, 0x00, 0xc2, 0x08, 0x41):
+        for dual in (0, 1):
+            _batch_vs_oracle(ctx, _wide_pairs(6, 1500, 4000, -1, flag, dual, seed=flag + dual))
+    mixed = _wide_pairs(40, 300, 3000, 1200, 0x40, 1, seed=3)   # narrow and wide jobs in one batch
+    _batch_vs_oracle(ctx, mixed)
+    c = Context(0, tb_budget=64 << 20)                           # many waves, two streams
+    try:
+        _batch_vs_oracle(c, _wide_pairs(12, 1500, 3000, 2500, 0x40, 1, seed=9))
+    finally:
+        c.close()
+
+
+def test_wide_band_per_call(built):
+    import minibwa_gb300.lib as K
+    p = _wide_pairs(3, 2000, 3000, 3000, 0x40, 1, seed=21)
+    for i in range(len(p)):
+        q, t = p.query(i), p.target(i)
+        ez = K.ksw_extd2_sse(q, t, 5, p.mat, p.q, p.e, p.q2, p.e2, 3000, 400, 10, 0x40)
+        exp, _ = O.extz(1, q, t, 5, p.mat, p.q, p.e, p.q2, p.e2, 3000, 400, 10, 0x40)
+        got = ez.fields()
+        for f in EXT_FIELDS + ["cigar"]:
+            assert got[f] == exp[f], (i, f)
+        K.free_extz(ez)

@@ -108,3 +108,25 @@ def test_both_kernel_families(ctx, family, monkeypatch):
                           mat=gen_nt4_mat(1, 4, 0, 1) if size == 1 else None, gapo=6 if size == 1 else 12,
                           gape=1 if size == 1 else 2)
         _batch(ctx, r)
+
+
+def test_long_queries_shared_memory_kernel(ctx):
+    """Queries beyond 64 segments (align.c's inversion check allows up to max_gap = 5000 nt)
+    run on the shared-memory kernel; batched and per call."""
+    from minibwa_gb300 import synth
+    from minibwa_gb300.lib import gen_nt4_mat
+    import minibwa_gb300.lib as K
+    for size, ql, xtra in ((2, 600, 0), (2, 2000, 0), (2, 5000, 0), (1, 1100, 0x40000 | 19), (1, 3000, 0x40000 | 19)):
+        mat = gen_nt4_mat(1, 4, 0, 1) if size == 1 else None
+        r = synth.ll_jobs(40, qlen=ql, tlen_lo=ql // 2, tlen_hi=ql * 2, plant=0.6, size=size, xtra=xtra, mat=mat,
+                          gapo=6 if size == 1 else 12, gape=1 if size == 1 else 2, seed=ql + size)
+        _batch(ctx, r)
+    r = synth.ll_jobs(3, qlen=3000, tlen_lo=2000, tlen_hi=4000, plant=1.0, seed=3)
+    for k in range(len(r)):
+        q = r.qbuf[r.jobs["qoff"][k]:r.jobs["qoff"][k] + r.jobs["qlen"][k]]
+        t = r.tbuf[r.jobs["toff"][k]:r.jobs["toff"][k] + r.jobs["tlen"][k]]
+        qp = K.ksw_ll_qinit(2, q, 5, r.mat)
+        s, qe, te = K.ksw_ll_i16(qp, t, r.gapo, r.gape)
+        K.ll_free(qp)
+        want, _ = O.ll(2, q, t, 5, r.mat, r.gapo, r.gape, 0)
+        assert (s, qe, te) == (want["score"], want["qe"], want["te"])
