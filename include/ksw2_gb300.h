@@ -23,7 +23,7 @@ extern "C" {
 #define KSW2G_OK           0
 #define KSW2G_E_CUDA      -1  /* a CUDA call failed */
 #define KSW2G_E_ARG       -2  /* invalid argument */
-#define KSW2G_E_BAND      -3  /* band too wide for the instantiated kernels */
+#define KSW2G_E_BAND      -3  /* band or query too long for the kernels (no-alloc path, very long ll queries) */
 #define KSW2G_E_NOMEM     -4  /* device or pinned allocation failed */
 #define KSW2G_E_CAPACITY  -5  /* caller's output buffer too small */
 #define KSW2G_E_UNSUPPORTED -6 /* e.g. GENERIC_SC with m > 16 */
