@@ -844,8 +844,8 @@ int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t 
     blo[i] = nbl;
     if (J.xtra & KSW_LL_SUBO) nbl += J.tlen;
   }
-  if (slen > ll_slen_cap(size))
-    return set_err(KSW2G_E_BAND, "ll query of %d segments exceeds the kernel's %d", slen, ll_slen_cap(size));
+  if (slen > ll_slen_cap(size, m))
+    return set_err(KSW2G_E_BAND, "ll query of %d segments exceeds the kernel's %d", slen, ll_slen_cap(size, m));
   b->ll_slen = slen;
   b->ll_qlen_max = 0;
   for (int i = 0; i < n; ++i) b->ll_qlen_max = std::max(b->ll_qlen_max, (int)jobs[i].qlen);
@@ -956,7 +956,7 @@ static ksw_llrst_t ll_one(void *q_, int tlen, const uint8_t *target, int gapo, i
   const int m = h->m, qlen = h->qlen, size = want_size;
   const int lanes = size == 1 ? 16 : 8;
   const int slen = (qlen + lanes - 1) / lanes;
-  if (slen > ll_slen_cap(size)) {
+  if (slen > ll_slen_cap(size, m)) {
     fprintf(stderr, "[ksw2gpu] fatal: ksw_ll query of %d nt exceeds the kernel limit\n", qlen);
     abort();
   }

@@ -74,7 +74,8 @@ struct LLLaunch {
 // force: 0 automatic, 1 one lane per thread, 2 DPX (only where exact).
 cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st, int force = 0);
 bool ll_dpx_exact(int size, const LLLaunch &L);
-int ll_slen_cap(int size);
+// Longest ksw_ll query, in segments, the kernels take for an alphabet of m.
+int ll_slen_cap(int size, int m);
 
 int num_sms(int device);
 

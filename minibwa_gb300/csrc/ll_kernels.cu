@@ -35,11 +35,10 @@ static size_t wide_smem_bytes(int size, int m, int slen) {
   const int lanes = size == 1 ? 16 : 8;
   return (size_t)(m + 3) * slen * lanes * sizeof(int16_t);
 }
-int ll_slen_cap(int size) {
-  int s = 64;
-  while (wide_smem_bytes(size, 16, s * 2) <= (size_t)wide_smem_cap()) s *= 2;
-  while (wide_smem_bytes(size, 16, s + 64) <= (size_t)wide_smem_cap()) s += 64;
-  return s;
+int ll_slen_cap(int size, int m) {
+  const size_t per = wide_smem_bytes(size, m, 1);  // bytes per segment
+  const int s = (int)((size_t)wide_smem_cap() / (per ? per : 1));
+  return s > 64 ? s : 64;
 }
 
 static cudaError_t launch_wide(int size, int slen_max, const LLLaunch &L, int max_blocks, cudaStream_t st) {
