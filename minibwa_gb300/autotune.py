@@ -49,9 +49,14 @@ def _time_batch(ctx, b, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def tune_ext(ctx, pairs, sample=4096, reps=3, min_class=64, seed=1):
+def tune_ext(ctx, pairs, sample=32768, reps=3, min_class=64, seed=1):
     """Tune the shape of every n_col_ class of `pairs` (a synth.Pairs or anything with the same
-    fields).  Installs the winners and returns {(dual, mode, ncol): (G, K, ms_per_pair_by_shape)}."""
+    fields).  Installs the winners and returns {(dual, mode, ncol): (G, K, ms_per_pair_by_shape)}.
+
+    The sample must fill the GPU the way the real batch does: on GB300 a 4,096-pair sample of
+    150 nt pairs favours groups of 8 threads, while full batches of them run 30% faster in
+    groups of 4, because a small sample leaves most SMs idle and rewards spreading each pair
+    over more threads."""
     L = load_library()
     shp = shapes()
     jobs = pairs.jobs

@@ -39,12 +39,16 @@ static const int kMaxPrefCol = 512;
 static int g_pref[2][3][kMaxPrefCol + 1];
 static std::mutex g_pref_mu;
 
+static bool shape_holds(int s, int n_col) {
+  return s >= 0 && s < kNumExtShapes && kExtShapes[s].G * kExtShapes[s].K >= 4 * n_col;
+}
+
 int ext_shape_pick(int dual, int mode, int n_col) {
   const int fit = ext_shape_for(n_col);
   if (fit < 0) return -1;
   if (n_col >= 0 && n_col <= kMaxPrefCol) {
     const int p = g_pref[dual & 1][mode][n_col] - 1;
-    if (p >= fit && p < kNumExtShapes) return p;
+    if (shape_holds(p, n_col)) return p;
   }
   return fit;
 }
