@@ -188,8 +188,12 @@ int ksw2g_server_stats(ksw2g_server_t *server, int64_t *admitted, int64_t *done,
 					   int64_t *peak_pool_bytes);
 /* Launches issued and the most requests merged into one launch.  Queued
  * requests of the head request's kind and scoring scheme are merged into its
- * launch while they fit the pool (at most 65,536 jobs per launch). */
+ * launch while they fit the pool and the merge limit. */
 int ksw2g_server_launch_stats(ksw2g_server_t *server, int64_t *launches, int64_t *max_merged);
+/* Most jobs one merged launch may hold (default 8,192; 1 turns merging off).
+ * Smaller launches finish sooner, larger ones fill the GPU: a latency /
+ * throughput knob. */
+int ksw2g_server_set_merge(ksw2g_server_t *server, int max_jobs);
 
 /* Measured 32-bit integer instruction throughput of the device (lane-ops per
  * second), the denominator of the DP kernels' integer-pipe roofline. */

@@ -111,6 +111,7 @@ def load_library():
         "ksw2g_server_wait": (i32, [vp, i64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(i64)]),
         "ksw2g_server_stats": (i32, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
         "ksw2g_server_launch_stats": (i32, [vp, C.POINTER(i64), C.POINTER(i64)]),
+        "ksw2g_server_set_merge": (i32, [vp, i32]),
         "ksw_extz2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i32, i32, i32, i32, C.POINTER(KswExtz)]),
         "ksw_extd2_sse": (None, [vp, i32, u8p, i32, u8p, i8, vp, i8, i8, i8, i8, i32, i32, i32, i32,
                                  C.POINTER(KswExtz)]),
@@ -394,11 +395,13 @@ class Server:
     """Continuous-batching serving engine (ksw2g_server_t): requests admitted by traceback
     footprint against a fixed device budget, run concurrently on `slots` streams."""
 
-    def __init__(self, device=0, slots=8, tb_budget=40 << 30):
+    def __init__(self, device=0, slots=8, tb_budget=40 << 30, max_merge=None):
         self.L = load_library()
         h = C.c_void_p()
         _check(self.L.ksw2g_server_create(device, slots, int(tb_budget), C.byref(h)))
         self.h = h
+        if max_merge is not None:
+            _check(self.L.ksw2g_server_set_merge(self.h, int(max_merge)))
 
     def submit_ext(self, dual, m, mat, q, e, q2, e2, jobs, qbuf, tbuf):
         jobs = np.ascontiguousarray(jobs, EXT_JOB)

@@ -195,10 +195,10 @@ def pct(a, q):
 
 
 def sweep(duration=3.0, fracs=(0.1, 0.25, 0.5, 0.8, 1.0), slots=8, budget=40 << 30, percall_threads=16,
-          percall_deadline=4.0, check=True, log=sys.stderr):
+          percall_deadline=4.0, check=True, log=sys.stderr, max_merge=None):
     from .lib import Context, Server
     sets = JobSets()
-    srv = Server(0, slots=slots, tb_budget=budget)
+    srv = Server(0, slots=slots, tb_budget=budget, max_merge=max_merge)
     warm = Trace(sets, 20000, None, seed=1)
     run_server(srv, sets, warm)
     # peak: everything queued at time 0
@@ -255,9 +255,10 @@ def main(argv=None):
     ap.add_argument("--budget-gb", type=float, default=40)
     ap.add_argument("--percall-threads", type=int, default=16)
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--max-merge", type=int, default=None, help="jobs per merged launch (1: no merging)")
     a = ap.parse_args(argv)
     out = sweep(a.duration, tuple(float(x) for x in a.fracs.split(",")), a.slots, int(a.budget_gb * (1 << 30)),
-                a.percall_threads, check=not a.no_check)
+                a.percall_threads, check=not a.no_check, max_merge=a.max_merge)
     print(json.dumps(out))
 
 
