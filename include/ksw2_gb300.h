@@ -107,6 +107,37 @@ void ksw2g_batch_free(ksw2g_batch_t *batch);
 int ksw2g_batch_set_timing(ksw2g_batch_t *batch, int on);
 int ksw2g_batch_kernel_ms(ksw2g_batch_t *batch, double *dp_ms, double *bt_ms, int *n_dp, int *n_bt);
 
+/* ---- a 2-bit reference resident on the device ----
+ * minibwa's l2b layout (l2bit.h:18-32): base i of the concatenated contigs is
+ * the 2-bit field at bits 2*(i%32) of pac[i/32]; contig k spans
+ * [ctg_off[k], ctg_off[k]+ctg_len[k]); ambi holds n_ambi sorted, disjoint
+ * [st, en) pairs (same coordinate) that read as N.  Extension and ksw_ll
+ * batches can then name their targets as windows (contig tid[k], start
+ * jobs[k].toff, length jobs[k].tlen) decoded on the device as l2b_getseq does
+ * (l2bit.c:52-77), with per-job flags: */
+#define KSW2G_REF_REVERSE 1  /* reversed in place (mb_seq_rev, align.c:643-644) */
+#define KSW2G_REF_C2T     2  /* l2b_meth_convert(L2B_METH_C2T) (l2bit.c:79-90) */
+#define KSW2G_REF_G2A     4  /* l2b_meth_convert(L2B_METH_G2A) */
+typedef struct ksw2g_ref ksw2g_ref_t;
+int ksw2g_ref_create(ksw2g_ctx_t *ctx, int64_t n_ctg, const uint64_t *ctg_off, const uint64_t *ctg_len,
+					 const uint64_t *pac, int64_t n_pac, int64_t n_ambi, const uint64_t *ambi, ksw2g_ref_t **ref);
+void ksw2g_ref_destroy(ksw2g_ref_t *ref);
+/* One window decoded on the device into host bytes (windows must lie inside their contig). */
+int ksw2g_ref_getseq(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int64_t tid, int64_t st, int64_t len, int flags,
+					 uint8_t *seq);
+/* ksw2g_ext_batch / ksw2g_ext_prepare / ksw2g_ll_batch with reference targets:
+ * only the queries travel from the host; tflags may be NULL. */
+int ksw2g_ext_batch_ref(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int dual, int8_t m, const int8_t *mat, int8_t q,
+						int8_t e, int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs, const int32_t *tid,
+						const int32_t *tflags, const uint8_t *qbuf, int64_t qbuf_len, ksw2g_ext_result_t *res,
+						uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used);
+int ksw2g_ext_prepare_ref(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int dual, int8_t m, const int8_t *mat, int8_t q,
+						  int8_t e, int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs, const int32_t *tid,
+						  const int32_t *tflags, const uint8_t *qbuf, int64_t qbuf_len, ksw2g_batch_t **batch);
+int ksw2g_ll_batch_ref(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int size, int m, const int8_t *mat, int gapo,
+					   int gape, int n_jobs, const ksw2g_ll_job_t *jobs, const int32_t *tid, const int32_t *tflags,
+					   const uint8_t *qbuf, int64_t qbuf_len, ksw2g_ll_result_t *res);
+
 /* ---- CUDA graphs: one launch runs several prepared batches concurrently ----
  * Captures the kernels of n prepared batches (extension or ll) into one CUDA
  * graph.  Each batch is a branch of the graph, so the batches run

@@ -21,6 +21,7 @@ from .lib import (  # noqa: F401
     KSW_LL_SUBO,
     Context,
     Graph,
+    Reference,
     Server,
     ExtBatch,
     LLBatch,

@@ -57,6 +57,7 @@ def build(verbose=False, force=False):
         ("noalloc.cu", "noalloc.o", []),
         ("server.cu", "server.o", []),
         ("graph.cu", "graph.o", []),
+        ("ref.cu", "ref.o", []),
     ]
     hdrs = _headers()
     procs, objs = [], []

@@ -112,6 +112,7 @@ struct ksw2g_batch {
   ksw2g_ext_params P;
   int ll_m = 0, ll_gapo = 0, ll_gape = 0, ll_size = 1, ll_slen = 0, ll_qlen_max = 0, ll_mat_max = 0, ll_force = 0;
   DevBuf raw, rawmeta, arena, jobs, order, sorted, tb_off, res, bts, cigar, counters, llmat, blist, blist_off;
+  DevBuf refmeta;         // per-job reference windows of a batch whose targets come from the device reference
   DevBuf wide;            // block scratch of wide-band jobs: two halves of wide_blocks x wide_stride
   int64_t wide_stride = 0;
   int wide_blocks = 0;
@@ -132,7 +133,7 @@ struct ksw2g_batch {
 // Make every device buffer of the batch grow in stream order on st.
 inline void batch_bind_stream(ksw2g_batch *b, cudaStream_t st) {
   for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts,
-                    &b->cigar, &b->counters, &b->llmat, &b->blist, &b->blist_off, &b->wide})
+                    &b->cigar, &b->counters, &b->llmat, &b->blist, &b->blist_off, &b->wide, &b->refmeta})
     d->st = st;
 }
 
@@ -148,10 +149,25 @@ struct SeqSeg {
   const uint8_t *tbuf;
   int64_t tlen;
 };
+// Targets read from a device-resident reference instead of host buffers: job
+// k's target is the window [toff, toff+tlen) of contig tid[k], decoded with
+// flags[k] (KSW2G_REF_*; flags may be null).  Used with a single segment whose
+// tbuf is unused.
+struct ksw2g_ref;
+struct RefTargets {
+  const ksw2g_ref *ref;
+  const int32_t *tid;
+  const int32_t *flags;
+};
 int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
-                     int8_t q2, int8_t e2, int nseg, const SeqSeg *segs);
+                     int8_t q2, int8_t e2, int nseg, const SeqSeg *segs, const RefTargets *rt = nullptr);
 int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape, int nseg,
-                    const SeqSeg *segs);
+                    const SeqSeg *segs, const RefTargets *rt = nullptr);
+namespace ksw2g {
+cudaError_t launch_ref_gather(int n, const int32_t *tid, const int64_t *st, const int32_t *len, const int32_t *flags,
+                              const int64_t *dst_off, uint8_t *arena, const ksw2g_ref *R, cudaStream_t stream);
+int ref_check_window(const ksw2g_ref *R, int64_t tid, int64_t st, int64_t len);
+}  // namespace ksw2g
 
 // Upload + pack the sequences and build the device job table and the wave plan
 // (synchronous on c->st, so the host buffers may be reused on return).

@@ -186,9 +186,9 @@ extern "C" int ksw2g_batch_kernel_ms(ksw2g_batch_t *b, double *dp_ms, double *bt
 // qoff/toff index the concatenation of the segments' query / target buffers.
 int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, const int32_t *qlen,
                            const int64_t *toff, const int32_t *tlen, int nseg, const SeqSeg *segs,
-                           std::vector<int64_t> &qpad, std::vector<int64_t> &tpad) {
+                           std::vector<int64_t> &qpad, std::vector<int64_t> &tpad, const RefTargets *rt) {
   int64_t qbuf_len = 0, tbuf_len = 0;
-  for (int k = 0; k < nseg; ++k) qbuf_len += segs[k].qlen, tbuf_len += segs[k].tlen;
+  for (int k = 0; k < nseg; ++k) qbuf_len += segs[k].qlen, tbuf_len += rt ? 0 : segs[k].tlen;
   qpad.resize(n), tpad.resize(n);
   int64_t a = 0;
   for (int i = 0; i < n; ++i) {
@@ -199,31 +199,49 @@ int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, co
   int rc;
   if ((rc = b->arena.ensure(arena_bytes))) return rc;
   if ((rc = b->raw.ensure(qbuf_len + tbuf_len + 16))) return rc;
-  // metadata: raw offsets (2n int64), lengths (2n int32), dst offsets (2n int64)
-  const size_t meta = (size_t)2 * n * (8 + 4 + 8);
+  // metadata of the packed sequences (queries, then targets unless they come from the
+  // device reference): raw offsets (int64), lengths (int32), arena offsets (int64)
+  const int npack = rt ? n : 2 * n;
+  const size_t o_ln = (size_t)8 * npack, o_dof = (o_ln + (size_t)4 * npack + 7) & ~(size_t)7;
+  const size_t meta = o_dof + (size_t)8 * npack;
   if ((rc = b->rawmeta.ensure(meta))) return rc;
   std::vector<uint8_t> hm(meta);
   int64_t *ro = (int64_t *)hm.data();
-  int32_t *ln = (int32_t *)(ro + 2 * n);
-  int64_t *dof = (int64_t *)(ln + 2 * n);
+  int32_t *ln = (int32_t *)(hm.data() + o_ln);
+  int64_t *dof = (int64_t *)(hm.data() + o_dof);
   for (int i = 0; i < n; ++i) {
     ro[i] = qoff[i], ln[i] = qlen[i], dof[i] = qpad[i];
-    ro[n + i] = qbuf_len + toff[i], ln[n + i] = tlen[i], dof[n + i] = tpad[i];
+    if (!rt) ro[n + i] = qbuf_len + toff[i], ln[n + i] = tlen[i], dof[n + i] = tpad[i];
   }
   uint8_t *raw = b->raw.as<uint8_t>();
   {
     int64_t qa = 0, ta = qbuf_len;
     for (int k = 0; k < nseg; ++k) {
       if (segs[k].qlen) CK(cudaMemcpyAsync(raw + qa, segs[k].qbuf, segs[k].qlen, cudaMemcpyHostToDevice, c->st));
-      if (segs[k].tlen) CK(cudaMemcpyAsync(raw + ta, segs[k].tbuf, segs[k].tlen, cudaMemcpyHostToDevice, c->st));
-      qa += segs[k].qlen, ta += segs[k].tlen;
+      if (!rt && segs[k].tlen) CK(cudaMemcpyAsync(raw + ta, segs[k].tbuf, segs[k].tlen, cudaMemcpyHostToDevice, c->st));
+      qa += segs[k].qlen, ta += rt ? 0 : segs[k].tlen;
     }
   }
   CK(cudaMemcpyAsync(b->rawmeta.p, hm.data(), meta, cudaMemcpyHostToDevice, c->st));
   const int64_t *dro = b->rawmeta.as<int64_t>();
-  const int32_t *dln = (const int32_t *)(dro + 2 * n);
-  const int64_t *ddof = (const int64_t *)(dln + 2 * n);
-  CK(launch_pack(2 * n, raw, dro, dln, b->arena.as<uint8_t>(), ddof, c->st));
+  const int32_t *dln = (const int32_t *)(b->rawmeta.as<uint8_t>() + o_ln);
+  const int64_t *ddof = (const int64_t *)(b->rawmeta.as<uint8_t>() + o_dof);
+  CK(launch_pack(npack, raw, dro, dln, b->arena.as<uint8_t>(), ddof, c->st));
+  if (rt) {  // targets: windows of the device reference, decoded into their arena slots
+    // layout: start (int64), arena offset (int64), contig (int32), length (int32), flags (int32)
+    const size_t rm = (size_t)n * (8 + 8 + 4 + 4 + 4);
+    if ((rc = b->refmeta.ensure(rm))) return rc;
+    std::vector<uint8_t> h(rm);
+    int64_t *hst = (int64_t *)h.data(), *hdst = hst + n;
+    int32_t *htid = (int32_t *)(hdst + n), *hlen = htid + n, *hfl = hlen + n;
+    for (int i = 0; i < n; ++i)
+      hst[i] = toff[i], hdst[i] = tpad[i], htid[i] = rt->tid[i], hlen[i] = tlen[i],
+      hfl[i] = rt->flags ? rt->flags[i] : 0;
+    CK(cudaMemcpyAsync(b->refmeta.p, h.data(), rm, cudaMemcpyHostToDevice, c->st));
+    const int64_t *dst = b->refmeta.as<int64_t>(), *ddst = dst + n;
+    const int32_t *dtid = (const int32_t *)(ddst + n), *dlen = dtid + n, *dfl = dlen + n;
+    CK(launch_ref_gather(n, dtid, dst, dlen, dfl, ddst, b->arena.as<uint8_t>(), rt->ref, c->st));
+  }
   // the H2D source buffers may be reused by the caller after return
   CK(cudaStreamSynchronize(c->st));
   return 0;
@@ -271,7 +289,9 @@ int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
 }
 
 int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
-                     int8_t q2, int8_t e2, int nseg, const SeqSeg *segs) {
+                     int8_t q2, int8_t e2, int nseg, const SeqSeg *segs, const RefTargets *rt) {
+  if (rt && (nseg != 1 || !rt->ref || (segs[0].n > 0 && !rt->tid)))
+    return set_err(KSW2G_E_ARG, "reference targets need one segment and a contig id per job");
   std::vector<ksw2g_job_t> flat;
   const ksw2g_job_t *jobs = nullptr;
   int n = 0;
@@ -295,8 +315,9 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   for (int i = 0; i < n; ++i) {
     const ksw2g_job_t &J = jobs[i];
     if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
-        J.toff + J.tlen > tbuf_len)
+        (!rt && J.toff + J.tlen > tbuf_len))
       return set_err(KSW2G_E_ARG, "job %d: sequence out of buffer bounds", i);
+    if (rt && ref_check_window(rt->ref, rt->tid[i], J.toff, J.tlen)) return KSW2G_E_ARG;
     if ((J.flag & KSW_EZ_GENERIC_SC) && m > 16)
       return set_err(KSW2G_E_UNSUPPORTED, "job %d: GENERIC_SC needs m <= 16 on the device (m=%d)", i, m);
     qo[i] = J.qoff, to[i] = J.toff, ql[i] = J.qlen, tl[i] = J.tlen;
@@ -312,7 +333,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     if (mode[i] != 0) cig += J.qlen + J.tlen + 1;
   }
   std::vector<int64_t> qpad, tpad;
-  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad);
+  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad, rt);
   if (rc) return rc;
   // device job table
   std::vector<ksw2g_job> dj(n);
@@ -659,6 +680,56 @@ extern "C" int ksw2g_ext_batch(ksw2g_ctx_t *c, int dual, int8_t m, const int8_t 
   return ksw2g_ext_fetch(c, c->scratch, res, cigar, cigar_cap, cigar_used);
 }
 
+int ll_run(ksw2g_ctx *c, ksw2g_batch *b);
+
+// ---- batches whose targets are windows of a device-resident reference
+extern "C" int ksw2g_ext_prepare_ref(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int dual, int8_t m, const int8_t *mat,
+                                     int8_t q, int8_t e, int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs,
+                                     const int32_t *tid, const int32_t *tflags, const uint8_t *qbuf,
+                                     int64_t qbuf_len, ksw2g_batch_t **out) {
+  if (!c || !out || !ref) return set_err(KSW2G_E_ARG, "null ctx/ref/out");
+  ksw2g_batch *b = new ksw2g_batch;
+  const SeqSeg seg{jobs, n_jobs, qbuf, qbuf_len, nullptr, 0};
+  const RefTargets rt{ref, tid, tflags};
+  int rc = ext_prepare_segs(c, b, dual, m, mat, q, e, q2, e2, 1, &seg, &rt);
+  if (rc) {
+    ksw2g_batch_free(b);
+    return rc;
+  }
+  *out = b;
+  return 0;
+}
+
+extern "C" int ksw2g_ext_batch_ref(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int dual, int8_t m, const int8_t *mat,
+                                   int8_t q, int8_t e, int8_t q2, int8_t e2, int n_jobs, const ksw2g_job_t *jobs,
+                                   const int32_t *tid, const int32_t *tflags, const uint8_t *qbuf, int64_t qbuf_len,
+                                   ksw2g_ext_result_t *res, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used) {
+  if (!c || !ref) return set_err(KSW2G_E_ARG, "null ctx/ref");
+  CK(cudaSetDevice(c->device));
+  if (!c->scratch) c->scratch = new ksw2g_batch;
+  const SeqSeg seg{jobs, n_jobs, qbuf, qbuf_len, nullptr, 0};
+  const RefTargets rt{ref, tid, tflags};
+  int rc = ext_prepare_segs(c, c->scratch, dual, m, mat, q, e, q2, e2, 1, &seg, &rt);
+  if (rc) return rc;
+  if ((rc = ext_run(c, c->scratch))) return rc;
+  return ksw2g_ext_fetch(c, c->scratch, res, cigar, cigar_cap, cigar_used);
+}
+
+extern "C" int ksw2g_ll_batch_ref(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int size, int m, const int8_t *mat, int gapo,
+                                  int gape, int n_jobs, const ksw2g_ll_job_t *jobs, const int32_t *tid,
+                                  const int32_t *tflags, const uint8_t *qbuf, int64_t qbuf_len,
+                                  ksw2g_ll_result_t *res) {
+  if (!c || !ref) return set_err(KSW2G_E_ARG, "null ctx/ref");
+  CK(cudaSetDevice(c->device));
+  if (!c->scratch) c->scratch = new ksw2g_batch;
+  const SeqSeg seg{jobs, n_jobs, qbuf, qbuf_len, nullptr, 0};
+  const RefTargets rt{ref, tid, tflags};
+  int rc = ll_prepare_segs(c, c->scratch, size, m, mat, gapo, gape, 1, &seg, &rt);
+  if (rc) return rc;
+  if ((rc = ll_run(c, c->scratch))) return rc;
+  return ksw2g_ll_fetch(c, c->scratch, res);
+}
+
 extern "C" int ksw2g_ext_num_shapes(void) { return kNumExtShapes; }
 extern "C" int ksw2g_ext_shape_info(int shape, int *g, int *k) {
   if (shape < 0 || shape >= kNumExtShapes) return set_err(KSW2G_E_ARG, "bad shape");
@@ -817,7 +888,9 @@ int ll_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t 
 }
 
 int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t *mat, int gapo, int gape, int nseg,
-                    const SeqSeg *segs) {
+                    const SeqSeg *segs, const RefTargets *rt) {
+  if (rt && (nseg != 1 || !rt->ref || (segs[0].n > 0 && !rt->tid)))
+    return set_err(KSW2G_E_ARG, "reference targets need one segment and a contig id per job");
   std::vector<ksw2g_ll_job_t> flat;
   const ksw2g_ll_job_t *jobs = nullptr;
   int n = 0;
@@ -841,8 +914,9 @@ int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t 
   for (int i = 0; i < n; ++i) {
     const ksw2g_ll_job_t &J = jobs[i];
     if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
-        J.toff + J.tlen > tbuf_len)
+        (!rt && J.toff + J.tlen > tbuf_len))
       return set_err(KSW2G_E_ARG, "ll job %d: sequence out of buffer bounds", i);
+    if (rt && ref_check_window(rt->ref, rt->tid[i], J.toff, J.tlen)) return KSW2G_E_ARG;
     qo[i] = J.qoff, to[i] = J.toff, ql[i] = J.qlen, tl[i] = J.tlen;
     slen = std::max(slen, (J.qlen + lanes - 1) / lanes);
     blo[i] = nbl;
@@ -856,7 +930,7 @@ int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t 
   b->ll_mat_max = mat[0];
   for (int a = 1; a < m * m; ++a) b->ll_mat_max = std::max(b->ll_mat_max, (int)mat[a]);
   std::vector<int64_t> qpad, tpad;
-  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad);
+  int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad, rt);
   if (rc) return rc;
   std::vector<ksw2g_ll_job> dj(n);
   for (int i = 0; i < n; ++i) dj[i] = ksw2g_ll_job{qpad[i], tpad[i], jobs[i].qlen, jobs[i].tlen, jobs[i].xtra, 0};

@@ -100,6 +100,14 @@ def load_library():
         "ksw2g_batch_set_timing": (i32, [vp, i32]),
         "ksw2g_batch_kernel_ms": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(i32),
                                         C.POINTER(i32)]),
+        "ksw2g_ref_create": (i32, [vp, i64, vp, vp, vp, i64, i64, vp, C.POINTER(vp)]),
+        "ksw2g_ref_destroy": (None, [vp]),
+        "ksw2g_ref_getseq": (i32, [vp, vp, i64, i64, i64, i32, u8p]),
+        "ksw2g_ext_batch_ref": (i32, [vp, vp, i32, i8, vp, i8, i8, i8, i8, i32, vp, vp, vp, u8p, i64, vp, vp, i64,
+                                      C.POINTER(i64)]),
+        "ksw2g_ext_prepare_ref": (i32, [vp, vp, i32, i8, vp, i8, i8, i8, i8, i32, vp, vp, vp, u8p, i64,
+                                        C.POINTER(vp)]),
+        "ksw2g_ll_batch_ref": (i32, [vp, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp, u8p, i64, vp]),
         "ksw2g_graph_create": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
         "ksw2g_graph_launch": (i32, [vp, vp]),
         "ksw2g_graph_launches": (i32, [vp]),
@@ -345,6 +353,63 @@ class LLBatch(_Batch):
         res = res if res is not None else np.zeros(self.n, LL_RESULT)
         _check(self.L.ksw2g_ll_fetch(self.ctx.h, self.h, _ptr(res)))
         return res
+
+
+class Reference:
+    """A 2-bit reference resident on the device (ksw2g_ref_t), from l2b arrays: pac (uint64, 32
+    bases each), contig offsets and lengths, and (n, 2) [st, en) runs of N."""
+
+    def __init__(self, ctx, pac, ctg_off, ctg_len, ambi):
+        self.L, self.ctx = ctx.L, ctx
+        self._pac = np.ascontiguousarray(pac, np.uint64)
+        self._off = np.ascontiguousarray(ctg_off, np.uint64)
+        self._len = np.ascontiguousarray(ctg_len, np.uint64)
+        self._amb = np.ascontiguousarray(ambi, np.uint64).reshape(-1)
+        self.h = C.c_void_p()
+        _check(self.L.ksw2g_ref_create(ctx.h, len(self._off), _ptr(self._off), _ptr(self._len), _ptr(self._pac),
+                                       len(self._pac), len(self._amb) // 2, _ptr(self._amb) if len(self._amb) else None,
+                                       C.byref(self.h)))
+
+    def getseq(self, tid, st, length, flags=0):
+        out = np.zeros(max(int(length), 1), np.uint8)
+        _check(self.L.ksw2g_ref_getseq(self.ctx.h, self.h, int(tid), int(st), int(length), int(flags), _ptr(out)))
+        return out[:int(length)]
+
+    def ext_batch(self, dual, m, mat, q, e, q2, e2, jobs, tid, tflags, qbuf):
+        """Extension jobs whose targets are windows (jobs['toff'], jobs['tlen'] of contig tid)."""
+        jobs = np.ascontiguousarray(jobs, EXT_JOB)
+        tid = np.ascontiguousarray(tid, np.int32)
+        tflags = None if tflags is None else np.ascontiguousarray(tflags, np.int32)
+        qbuf, mat = _u8(qbuf), np.ascontiguousarray(mat, np.int8)
+        res = np.zeros(len(jobs), EXT_RESULT)
+        cap = int((jobs["qlen"].astype(np.int64) + jobs["tlen"] + 1).sum()) + 16
+        cig = np.zeros(cap, np.uint32)
+        used = C.c_int64()
+        _check(self.L.ksw2g_ext_batch_ref(self.ctx.h, self.h, int(dual), m, _ptr(mat), q, e, q2, e2, len(jobs),
+                                          _ptr(jobs), _ptr(tid), _ptr(tflags), _ptr(qbuf), len(qbuf), _ptr(res),
+                                          _ptr(cig), cap, C.byref(used)))
+        return res, cig[:used.value]
+
+    def ll_batch(self, size, m, mat, gapo, gape, jobs, tid, tflags, qbuf):
+        jobs = np.ascontiguousarray(jobs, LL_JOB)
+        tid = np.ascontiguousarray(tid, np.int32)
+        tflags = None if tflags is None else np.ascontiguousarray(tflags, np.int32)
+        qbuf, mat = _u8(qbuf), np.ascontiguousarray(mat, np.int8)
+        res = np.zeros(len(jobs), LL_RESULT)
+        _check(self.L.ksw2g_ll_batch_ref(self.ctx.h, self.h, size, m, _ptr(mat), gapo, gape, len(jobs), _ptr(jobs),
+                                         _ptr(tid), _ptr(tflags), _ptr(qbuf), len(qbuf), _ptr(res)))
+        return res
+
+    def close(self):
+        if self.h:
+            self.L.ksw2g_ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Graph:

@@ -189,3 +189,80 @@ def config3_pe(n=200000, seed=SEED + 5):
     from .lib import KSW_LL_SUBO
     mat = gen_nt4_mat(1, 4, 0, 1)
     return ll_jobs(n, size=1, xtra=KSW_LL_SUBO | 19, mat=mat, gapo=6, gape=1, seed=seed, name="cfg3-ll-u8-pe")
+
+
+class Reference2b:
+    """A synthetic reference in minibwa's l2b layout: 2-bit packed bases (32 per uint64, base i
+    at bits 2*(i%32)), contigs back to back, and sorted [st, en) runs of N.  N positions hold a
+    random 2-bit base in pac, as l2b_import stores them."""
+
+    def __init__(self, ctg_len, n_runs=20, run_max=200, seed=SEED + 50):
+        rng = np.random.default_rng(seed)
+        self.ctg_len = np.asarray(ctg_len, np.uint64)
+        self.ctg_off = np.concatenate([[0], np.cumsum(self.ctg_len)[:-1]]).astype(np.uint64)
+        tot = int(self.ctg_len.sum())
+        self.bases = rng.integers(0, 4, tot).astype(np.uint8)
+        starts = np.sort(rng.choice(max(tot - run_max, 1), n_runs, replace=False)) if n_runs else np.zeros(0, int)
+        runs = []
+        for st in starts:
+            en = int(st) + int(rng.integers(1, run_max + 1))
+            if runs and st <= runs[-1][1]:
+                runs[-1][1] = max(runs[-1][1], en)
+            else:
+                runs.append([int(st), en])
+        self.ambi = np.array(runs, np.uint64).reshape(-1, 2)
+        n_pac = (tot + 31) // 32
+        pac = np.zeros(n_pac * 32, np.uint64)
+        pac[:tot] = self.bases
+        pac = pac.reshape(n_pac, 32) << (2 * np.arange(32, dtype=np.uint64))
+        self.pac = np.bitwise_or.reduce(pac, axis=1).astype(np.uint64)
+
+    def window(self, tid, st, length, flags=0):
+        """The decoded window, computed here with numpy (an independent cross-check)."""
+        g0 = int(self.ctg_off[tid]) + int(st)
+        w = self.bases[g0:g0 + length].copy()
+        for s0, e0 in self.ambi:
+            s1, e1 = max(int(s0), g0), min(int(e0), g0 + length)
+            if s1 < e1:
+                w[s1 - g0:e1 - g0] = 4
+        if flags & 2:
+            w[w == 1] = 3
+        elif flags & 4:
+            w[w == 2] = 0
+        return w[::-1].copy() if flags & 1 else w
+
+
+def ref_pairs(ref, n, qlen_lo=100, qlen_hi=300, flank=50, w=100, dual=True, flag=KSW_EZ_EXTZ_ONLY, flags=None,
+              seed=SEED + 51):
+    """Extension jobs whose targets are windows of `ref`: the query is the window (as the job's
+    flags decode it) with 2% substitutions and 0.5% indels, the window `flank` bases longer.
+    Returns (Pairs with host target bytes, contig ids, window flags)."""
+    rng = np.random.default_rng(seed)
+    jobs = np.zeros(n, EXT_JOB)
+    tids = np.zeros(n, np.int32)
+    tfl = np.zeros(n, np.int32) if flags is None else np.asarray(flags, np.int32)
+    qparts, tparts = [], []
+    for i in range(n):
+        ql = int(rng.integers(qlen_lo, qlen_hi + 1))
+        k = int(rng.integers(0, len(ref.ctg_len)))
+        tl = min(ql + flank, int(ref.ctg_len[k]))
+        st = int(rng.integers(0, int(ref.ctg_len[k]) - tl + 1))
+        t = ref.window(k, st, tl, int(tfl[i]))
+        q = t[:min(ql, tl)].copy()
+        sub = rng.random(len(q)) < 0.02
+        q[sub] = rng.integers(0, 4, int(sub.sum()))
+        if rng.random() < 0.3 and len(q) > 20:
+            p = int(rng.integers(5, len(q) - 5))
+            q = np.concatenate([q[:p], q[p + int(rng.integers(1, 4)):]])
+        jobs[i]["qlen"], jobs[i]["tlen"], jobs[i]["toff"] = len(q), tl, st
+        tids[i] = k
+        qparts.append(q), tparts.append(t)
+    jobs["qoff"] = np.concatenate([[0], np.cumsum([len(x) for x in qparts])[:-1]])
+    jobs["w"], jobs["zdrop"], jobs["end_bonus"], jobs["flag"] = w, 100, 10, flag
+    mat = gen_nt4_mat(2, 8, 0, 1)
+    q2, e2 = (24, 1) if dual else (12, 2)
+    host = jobs.copy()
+    host["toff"] = np.concatenate([[0], np.cumsum([len(x) for x in tparts])[:-1]])
+    pairs = Pairs(host, np.concatenate(qparts), np.concatenate(tparts), dual, mat, 12, 2, q2, e2, "ref-windows")
+    pairs.ref_toff = jobs["toff"].copy()
+    return pairs, tids, tfl

@@ -681,3 +681,30 @@ void orc_gen_nt4_mat(int8_t *mat, int8_t a, int8_t b, int8_t b_ts, int8_t b_ambi
 	if (mt == 1) mat[1 * m + 3] = a;
 	else if (mt == 2) mat[2 * m + 0] = a;
 }
+
+/* l2b_getseq (l2bit.c:52-77) on the l2b arrays, then l2b_meth_convert (l2bit.c:79-90) and
+ * the callers' in-place reversal (mb_seq_rev); flags: 1 reverse, 2 C2T, 4 G2A.  The window
+ * [st, st+len) must lie inside contig tid. */
+void orc_l2b_getseq(const uint64_t *pac, const uint64_t *ctg_off, int64_t n_ambi, const uint64_t *ambi, int64_t tid,
+					int64_t st, int64_t len, int flags, uint8_t *seq)
+{
+	uint64_t g0 = ctg_off[tid] + (uint64_t)st, i;
+	int64_t a, p;
+	for (i = 0; i < (uint64_t)len; ++i) {
+		uint64_t g = g0 + i;
+		seq[i] = (uint8_t)(pac[g >> 5] >> ((g & 31) << 1) & 3);
+	}
+	for (a = 0; a < n_ambi; ++a) { /* N runs overlapping the window */
+		uint64_t s = ambi[2 * a] > g0 ? ambi[2 * a] : g0;
+		uint64_t e = ambi[2 * a + 1] < g0 + (uint64_t)len ? ambi[2 * a + 1] : g0 + (uint64_t)len;
+		for (i = s; i < e; ++i) seq[i - g0] = 4;
+	}
+	if (flags & 2) { for (p = 0; p < len; ++p) if (seq[p] == 1) seq[p] = 3; }
+	else if (flags & 4) { for (p = 0; p < len; ++p) if (seq[p] == 2) seq[p] = 0; }
+	if (flags & 1) {
+		for (p = 0; p < len / 2; ++p) {
+			uint8_t t = seq[p];
+			seq[p] = seq[len - 1 - p], seq[len - 1 - p] = t;
+		}
+	}
+}

@@ -95,6 +95,9 @@ void orc_ll_batch(int size, int n_jobs, const orc_job_t *jobs, const uint8_t *qb
 				  int m, const int8_t *mat, int gapo, int gape, int xtra, orc_llrst_t *res, int nthreads,
 				  int64_t *cells);
 
+void orc_l2b_getseq(const uint64_t *pac, const uint64_t *ctg_off, int64_t n_ambi, const uint64_t *ambi, int64_t tid,
+					int64_t st, int64_t len, int flags, uint8_t *seq);
+
 #ifdef __cplusplus
 }
 #endif

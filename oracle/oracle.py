@@ -89,6 +89,8 @@ def _load(path, prefix):
         L.orc_ll_i16_core.argtypes = [vp, i32, vp, i32, i32, i32]
         L.orc_ll_rows.restype = i32
         L.orc_ll_rows.argtypes = [vp]
+        L.orc_l2b_getseq.restype = None
+        L.orc_l2b_getseq.argtypes = [vp, vp, i64, vp, i64, i64, i64, i32, vp]
     _libs[path] = L
     return L
 
@@ -179,3 +181,16 @@ def ll(size, query, target, m, mat, gapo, gape, xtra):
     libc.free.argtypes = [C.c_void_p]
     libc.free(qp)
     return dict(score=r.score, te=r.te, qe=r.qe, score2=r.score2, te2=r.te2), rows
+
+
+def l2b_getseq(ref, tid, st, length, flags=0):
+    """A window of a 2-bit reference (an object with pac, ctg_off and ambi arrays, ambi as
+    (n, 2) [st, en) rows), decoded as the reference's l2b_getseq / l2b_meth_convert / mb_seq_rev
+    sequence; flags 1 reverse, 2 C2T, 4 G2A."""
+    L = oracle_lib()
+    out = np.zeros(max(int(length), 1), np.uint8)
+    amb = np.ascontiguousarray(ref.ambi, np.uint64).reshape(-1)
+    L.orc_l2b_getseq(_p(np.ascontiguousarray(ref.pac, np.uint64)), _p(np.ascontiguousarray(ref.ctg_off, np.uint64)),
+                     len(amb) // 2, _p(amb) if len(amb) else None, int(tid), int(st), int(length), int(flags),
+                     _p(out))
+    return out[:int(length)]
