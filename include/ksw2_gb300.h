@@ -138,6 +138,42 @@ int ksw2g_ll_batch_ref(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int size, int m
 					   int gape, int n_jobs, const ksw2g_ll_job_t *jobs, const int32_t *tid, const int32_t *tflags,
 					   const uint8_t *qbuf, int64_t qbuf_len, ksw2g_ll_result_t *res);
 
+/* ---- mate rescue over the resident reference (pe.c:209-372) ----
+ * One candidate is one (read, window) pair of mb_matesw_core: the window
+ * [ts, te) on contig tid computed from the insert-size statistics and clamped
+ * to the contig (pe.c:336-339), the read in the orientation aligned
+ * (seq[is_rev]), the window's methylation mode (l2b_meth_rev applied when
+ * is_rev: 0 none, 1 C2T, 2 G2A) and min_sc already divided by a.  Per
+ * candidate the call runs mb_ungap (7-mer Hough votes along diagonals), the
+ * narrowing and thresholds of pe.c:347-353, ksw_ll with the matrix scaled by a
+ * (u8 or i16 by pe.c:263's rule) and, when ksw_ll's score passes, ksw_extz2 on
+ * the reversed prefixes ending at ksw_ll's end (pe.c:283-290).  The windows are
+ * decoded on the device; only the reads travel from the host. */
+typedef struct {
+	int32_t a, b, b_ts, b_ambi, q, e;      /* mb_opt_t scores, unscaled */
+	int32_t bw, zdrop, end_bonus, min_len, min_dp_max;
+} ksw2g_rescue_opt_t;
+
+typedef struct {
+	int64_t qoff;                        /* read in qbuf */
+	int64_t ts, te;                      /* candidate window on contig tid */
+	int32_t qlen, tid, meth, min_sc, rev, pad;
+} ksw2g_rescue_job_t;
+
+typedef struct {
+	int32_t max_ug, max_i, n_good, n_kmer; /* mb_ungap's return value and outputs */
+	int64_t ts2, te2;                      /* the window ksw_ll ran on */
+	int32_t ll_done, ll_score, ll_te, ll_qe, ll_score2, ll_te2;
+	int32_t ext_done, rescued;             /* extz2 ran; the hit passed pe.c:291 */
+	int32_t qs, qe, dp_max2, pad;          /* hit on the read, flipped when rev (pe.c:364-368) */
+	int64_t ts, te;                        /* hit on the contig */
+	ksw2g_ext_result_t ext;                /* extz2 result; CIGAR at cigar[ext.cigar_off] */
+} ksw2g_rescue_result_t;
+
+int ksw2g_rescue_batch(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, const ksw2g_rescue_opt_t *opt, int n_jobs,
+					   const ksw2g_rescue_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+					   ksw2g_rescue_result_t *res, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used);
+
 /* ---- CUDA graphs: one launch runs several prepared batches concurrently ----
  * Captures the kernels of n prepared batches (extension or ll) into one CUDA
  * graph.  Each batch is a branch of the graph, so the batches run

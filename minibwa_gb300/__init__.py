@@ -10,6 +10,9 @@ from .lib import (  # noqa: F401
     EXT_RESULT,
     LL_JOB,
     LL_RESULT,
+    RESCUE_JOB,
+    RESCUE_OPT,
+    RESCUE_RESULT,
     KSW_EZ_APPROX_DROP,
     KSW_EZ_APPROX_MAX,
     KSW_EZ_EXTZ_ONLY,

@@ -58,6 +58,7 @@ def build(verbose=False, force=False):
         ("server.cu", "server.o", []),
         ("graph.cu", "graph.o", []),
         ("ref.cu", "ref.o", []),
+        ("rescue.cu", "rescue.o", []),
     ]
     hdrs = _headers()
     procs, objs = [], []

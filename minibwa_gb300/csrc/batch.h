@@ -86,6 +86,8 @@ struct ksw2g_ctx {
   DevBuf tb_pool;       // traceback rows of the running wave
   DevBuf one;           // per-call drop-in scratch (device)
   PinBuf one_h;         // per-call drop-in staging (pinned)
+  DevBuf rs_q, rs_t, rs_meta, rs_res, rs_hist;  // mate-rescue prefilter: reads, windows, records, votes
+  PinBuf rs_h;                                  // mate-rescue staging (pinned)
   ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
   // two sub-contexts (own stream and traceback pool, half the budget each) that the
   // one-shot extension call alternates between, so the host prepares one chunk

@@ -117,6 +117,8 @@ extern "C" void ksw2g_ctx_destroy(ksw2g_ctx_t *c) {
   c->tb_pool.release();
   c->one.release();
   c->one_h.release();
+  for (DevBuf *d : {&c->rs_q, &c->rs_t, &c->rs_meta, &c->rs_res, &c->rs_hist}) d->release();
+  c->rs_h.release();
   cudaStreamDestroy(c->st);
   delete c;
 }

@@ -28,10 +28,12 @@ namespace ksw2g {
 constexpr int kWideThreads = KSW2G_WIDE_THREADS;  // a multiple of 32
 
 // block-shared variables (the host emulation of the kernels shares them as statics)
+#ifndef KSW2G_BLOCK_SHARED
 #ifdef KSW2G_EMU
 #define KSW2G_BLOCK_SHARED static
 #else
 #define KSW2G_BLOCK_SHARED __shared__
+#endif
 #endif
 
 // Bytes of one block's scratch for a pair (the 16 bytes of slack after every

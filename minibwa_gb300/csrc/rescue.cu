@@ -1,0 +1,244 @@
+// rescue.cu -- pe.c's mate rescue on the device: the 7-mer Hough prefilter
+// (mb_ungap, pe.c:209-247), the window narrowing and thresholds of
+// mb_matesw_core (pe.c:347-353), then ksw_ll and the reverse extension of
+// mb_matesw_align (pe.c:249-300) as batches over the resident reference.
+//
+// The caller computes each candidate window from the insert-size statistics as
+// pe.c:336-339 does and passes the read in the orientation pe.c aligns
+// (seq[is_rev]) with the window's methylation mode.  Stage 1 decodes the
+// windows on the device (plain l2b_getseq: pe.c converts bases only inside
+// mb_ungap and through the scoring matrix) and votes the read's 7-mers along
+// diagonals, one block per candidate: the query's table of last positions
+// (4^7 uint16, the reference's direct table) is built in shared memory in the
+// reference's sequential order, so the last occurrence wins as it does there;
+// the target's votes are parallel atomic adds into a diagonal histogram in
+// shared memory (global memory for windows too long for it).  Stage 2 runs
+// ksw_ll on the narrowed windows (u8 or i16 by pe.c:263's rule, matrix scaled by
+// a), stage 3 extends the reversed prefixes ending at ksw_ll's end with extz2
+// (EXTZ_ONLY | RIGHT | REV_CIGAR, plus GENERIC_SC for methylation modes).
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/ksw2.h"
+#include "../../include/ksw2_gb300.h"
+#include "batch.h"
+#include "host_common.h"
+#include "launch.h"
+#include "ungap.cuh"
+
+using namespace ksw2g;
+
+namespace {
+
+// ksw_gen_nt4_mat (ksw2.h:199-219) with its int8 arguments
+void gen_nt4(int8_t *mat, int8_t a, int8_t b, int8_t b_ts, int8_t b_ambi, int mt) {
+  const int m = 5;
+  a = a < 0 ? -a : a;
+  b = b > 0 ? -b : b;
+  b_ambi = b_ambi > 0 ? -b_ambi : b_ambi;
+  for (int i = 0; i < m - 1; ++i) {
+    for (int j = 0; j < m - 1; ++j) mat[i * m + j] = i == j ? a : b;
+    mat[i * m + m - 1] = b_ambi;
+  }
+  for (int j = 0; j < m; ++j) mat[(m - 1) * m + j] = b_ambi;
+  if (b_ts != 0 && b_ts != b) {  // compared after b is made negative, as there
+    b_ts = b_ts > 0 ? -b_ts : b_ts;
+    mat[0 * m + 2] = mat[1 * m + 3] = mat[2 * m + 0] = mat[3 * m + 1] = b_ts;
+  }
+  if (mt == 1) mat[1 * m + 3] = a;
+  else if (mt == 2) mat[2 * m + 0] = a;
+}
+
+inline int64_t al16(int64_t x) { return (x + 15) & ~(int64_t)15; }
+
+}  // namespace
+
+extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const ksw2g_rescue_opt_t *opt, int n,
+                                  const ksw2g_rescue_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
+                                  ksw2g_rescue_result_t *res, uint32_t *cigar, int64_t cigar_cap,
+                                  int64_t *cigar_used) {
+  if (!c || !ref || !opt || n < 0 || qbuf_len < 0 || (n > 0 && (!jobs || !res || !qbuf)))
+    return report_error(KSW2G_E_ARG, "rescue: bad arguments");
+  if (opt->a <= 0) return report_error(KSW2G_E_ARG, "rescue: the match score must be positive");
+  if (cigar_used) *cigar_used = 0;
+  if (n == 0) return 0;
+  if (cudaSetDevice(c->device) != cudaSuccess) return report_error(KSW2G_E_CUDA, "rescue: bad device");
+  const ksw2g_rescue_opt_t &o = *opt;
+  int rc;
+  for (int i = 0; i < n; ++i) {
+    const ksw2g_rescue_job_t &J = jobs[i];
+    if (J.qlen < 0 || J.qoff < 0 || J.qoff + J.qlen > qbuf_len || J.te < J.ts || J.te - J.ts > INT32_MAX / 2 ||
+        J.meth < 0 || J.meth > 2)
+      return report_error(KSW2G_E_ARG, "rescue: candidate out of bounds");
+    if ((rc = ref_check_window(ref, J.tid, J.ts, J.te - J.ts))) return rc;
+  }
+  // ---- stage 1: the windows decoded on the device, then mb_ungap's votes
+  // device records: st int64[n] | dst int64[n] | tid, len, flags int32[n] | UngapJob[n] | counter
+  const int64_t o_dst = 8 * (int64_t)n, o_tid = 16 * (int64_t)n, o_len = 20 * (int64_t)n, o_fl = 24 * (int64_t)n;
+  const int64_t o_uj = al16(28 * (int64_t)n), o_cnt = o_uj + (int64_t)sizeof(UngapJob) * n, meta = o_cnt + 16;
+  const int64_t o_ur = al16(meta);
+  if ((rc = c->rs_h.ensure((size_t)(o_ur + (int64_t)sizeof(UngapRes) * n)))) return rc;
+  uint8_t *hm = (uint8_t *)c->rs_h.p;
+  int64_t tarena = 0;
+  int tmax = 1;
+  for (int i = 0; i < n; ++i) {
+    const ksw2g_rescue_job_t &J = jobs[i];
+    const int len = (int)(J.te - J.ts);
+    ((int64_t *)hm)[i] = J.ts;
+    ((int64_t *)(hm + o_dst))[i] = tarena + 32;
+    ((int32_t *)(hm + o_tid))[i] = J.tid;
+    ((int32_t *)(hm + o_len))[i] = len;
+    ((int32_t *)(hm + o_fl))[i] = 0;
+    ((UngapJob *)(hm + o_uj))[i] = UngapJob{J.qoff, tarena + 32, J.qlen, len, J.meth, 0};
+    tarena += slot_bytes(len);
+    tmax = std::max(tmax, len);
+  }
+  memset(hm + o_cnt, 0, 16);
+  if (!c->nsm) c->nsm = num_sms(c->device);
+  const int blocks = std::min(n, c->nsm * 8);
+  const bool shared_hist = kUngapTable + (size_t)tmax * 4 <= kUngapSmemMax;
+  const size_t smem = shared_hist ? kUngapTable + (size_t)tmax * 4 : kUngapTable;
+  if ((rc = c->rs_q.ensure((size_t)qbuf_len + 16)) || (rc = c->rs_t.ensure((size_t)tarena + 64)) ||
+      (rc = c->rs_meta.ensure((size_t)meta)) || (rc = c->rs_res.ensure(sizeof(UngapRes) * (size_t)n)) ||
+      (!shared_hist && (rc = c->rs_hist.ensure((size_t)blocks * tmax * 4))))
+    return rc;
+  cudaStream_t st = c->st;
+  uint8_t *dm = c->rs_meta.as<uint8_t>();
+  if ((qbuf_len && cudaMemcpyAsync(c->rs_q.p, qbuf, (size_t)qbuf_len, cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+      cudaMemcpyAsync(dm, hm, (size_t)meta, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return report_error(KSW2G_E_CUDA, "rescue: upload failed");
+  if (launch_ref_gather(n, (const int32_t *)(dm + o_tid), (const int64_t *)dm, (const int32_t *)(dm + o_len),
+                        (const int32_t *)(dm + o_fl), (const int64_t *)(dm + o_dst), c->rs_t.as<uint8_t>(), ref,
+                        st) != cudaSuccess)
+    return report_error(KSW2G_E_CUDA, "rescue: window gather failed");
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(ungap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return report_error(KSW2G_E_CUDA, "rescue: shared memory attribute");
+  ungap_kernel<<<blocks, kUngapThreads, smem, st>>>(
+      n, (const UngapJob *)(dm + o_uj), c->rs_q.as<uint8_t>(), c->rs_t.as<uint8_t>(), c->rs_res.as<UngapRes>(),
+      (int *)(dm + o_cnt), shared_hist ? nullptr : c->rs_hist.as<int32_t>(), shared_hist ? 0 : (int64_t)tmax);
+  const UngapRes *ur = (const UngapRes *)(hm + o_ur);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync((void *)ur, c->rs_res.p, sizeof(UngapRes) * (size_t)n, cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return report_error(KSW2G_E_CUDA, "rescue: prefilter failed");
+
+  // ---- stage 2: narrowing and thresholds (pe.c:347-353), then ksw_ll per (size, methylation) group
+  const int b_mm = (o.b + o.a - 1) / o.a, b_ts = (o.b_ts + o.a - 1) / o.a, b_ambi = (o.b_ambi + o.a - 1) / o.a;
+  const int gapo = (o.q + o.a - 1) / o.a, gape = (o.e + o.a - 1) / o.a;
+  std::vector<int> ll_size(n, 0);
+  for (int i = 0; i < n; ++i) {
+    const ksw2g_rescue_job_t &J = jobs[i];
+    ksw2g_rescue_result_t &R = res[i];
+    memset(&R, 0, sizeof R);
+    R.ext.cigar_off = -1;
+    R.max_ug = ur[i].max, R.max_i = ur[i].max_i, R.n_good = ur[i].n_good, R.n_kmer = ur[i].n_kmer;
+    int64_t ts2 = J.ts, te2 = J.te;
+    if (R.max_ug >= 10 && R.max_ug >= J.qlen >> 1 && R.n_good == 1) {
+      ts2 = J.ts + R.max_i - J.qlen / 2;
+      te2 = ts2 + (int64_t)J.qlen * 2;
+      if (ts2 < J.ts) ts2 = J.ts;
+      if (te2 > J.te) te2 = J.te;
+    }
+    R.ts2 = ts2, R.te2 = te2;
+    if (!(R.max_ug >= 10 || R.max_ug >= R.n_kmer * 0.33)) continue;
+    const int64_t tl2 = te2 - ts2, max_sc = J.qlen < tl2 ? J.qlen : tl2;
+    if (max_sc >= 32767) continue;  // mb_matesw_align returns before ksw_ll
+    ll_size[i] = max_sc < 255 - b_mm ? 1 : 2;
+  }
+  for (int size = 1; size <= 2; ++size)
+    for (int mt = 0; mt <= 2; ++mt) {
+      std::vector<int> idx;
+      for (int i = 0; i < n; ++i)
+        if (ll_size[i] == size && jobs[i].meth == mt) idx.push_back(i);
+      if (idx.empty()) continue;
+      int8_t mat[25];
+      gen_nt4(mat, 1, (int8_t)b_mm, (int8_t)b_ts, (int8_t)b_ambi, mt);
+      std::vector<ksw2g_ll_job_t> lj(idx.size());
+      std::vector<int32_t> tids(idx.size());
+      for (size_t k = 0; k < idx.size(); ++k) {
+        const int i = idx[k];
+        lj[k] = ksw2g_ll_job_t{jobs[i].qoff, res[i].ts2, jobs[i].qlen, (int32_t)(res[i].te2 - res[i].ts2),
+                               KSW_LL_SUBO | o.min_len, 0};
+        tids[k] = jobs[i].tid;
+      }
+      std::vector<ksw2g_ll_result_t> lr(idx.size());
+      if ((rc = ksw2g_ll_batch_ref(c, ref, size, 5, mat, gapo, gape, (int)idx.size(), lj.data(), tids.data(),
+                                   nullptr, qbuf, qbuf_len, lr.data())))
+        return rc;
+      for (size_t k = 0; k < idx.size(); ++k) {
+        ksw2g_rescue_result_t &R = res[idx[k]];
+        R.ll_done = 1, R.ll_score = lr[k].score, R.ll_te = lr[k].te, R.ll_qe = lr[k].qe;
+        R.ll_score2 = lr[k].score2, R.ll_te2 = lr[k].te2;
+      }
+    }
+
+  // ---- stage 3: extz2 on the reversed prefixes ending at ksw_ll's end (pe.c:283-300)
+  int64_t used = 0;
+  for (int mt = 0; mt <= 2; ++mt) {
+    std::vector<int> idx;
+    for (int i = 0; i < n; ++i) {
+      const ksw2g_rescue_result_t &R = res[i];
+      if (R.ll_done && jobs[i].meth == mt && R.ll_score >= o.min_dp_max && R.ll_score >= jobs[i].min_sc)
+        idx.push_back(i);
+    }
+    if (idx.empty()) continue;
+    int8_t mat[25];
+    gen_nt4(mat, (int8_t)o.a, (int8_t)o.b, (int8_t)o.b_ts, (int8_t)o.b_ambi, mt);
+    const int flag = KSW_EZ_EXTZ_ONLY | KSW_EZ_RIGHT | KSW_EZ_REV_CIGAR | (mt ? KSW_EZ_GENERIC_SC : 0);
+    std::vector<ksw2g_job_t> ej(idx.size());
+    std::vector<int32_t> tids(idx.size()), tfl(idx.size(), KSW2G_REF_REVERSE);
+    std::vector<uint8_t> rq;
+    int64_t cap = 16;
+    for (size_t k = 0; k < idx.size(); ++k) {
+      const int i = idx[k];
+      const int qe = res[i].ll_qe + 1, te = res[i].ll_te + 1;
+      const int64_t qo = (int64_t)rq.size();
+      for (int p = qe - 1; p >= 0; --p) rq.push_back(qbuf[jobs[i].qoff + p]);  // mb_seq_rev(qe, qseq)
+      ej[k] = ksw2g_job_t{qo, res[i].ts2, qe, te, o.bw, o.zdrop, o.end_bonus, flag};
+      tids[k] = jobs[i].tid;
+      cap += (int64_t)qe + te + 1;
+    }
+    std::vector<ksw2g_ext_result_t> er(idx.size());
+    std::vector<uint32_t> cg((size_t)cap);
+    int64_t u = 0;
+    if ((rc = ksw2g_ext_batch_ref(c, ref, 0, 5, mat, (int8_t)o.q, (int8_t)o.e, (int8_t)o.q, (int8_t)o.e,
+                                  (int)idx.size(), ej.data(), tids.data(), tfl.data(), rq.data(), (int64_t)rq.size(),
+                                  er.data(), cg.data(), cap, &u)))
+      return rc;
+    for (size_t k = 0; k < idx.size(); ++k) {
+      const int i = idx[k];
+      ksw2g_rescue_result_t &R = res[i];
+      const ksw2g_ext_result_t &E = er[k];
+      R.ext_done = 1;
+      R.ext = E;
+      R.ext.cigar_off = -1;
+      if (E.n_cigar > 0 && cigar) {
+        if (used + E.n_cigar > cigar_cap) return report_error(KSW2G_E_CAPACITY, "rescue: CIGAR buffer too small");
+        memcpy(cigar + used, cg.data() + E.cigar_off, sizeof(uint32_t) * (size_t)E.n_cigar);
+        R.ext.cigar_off = used;
+        used += E.n_cigar;
+      }
+      if (E.n_cigar > 0 && E.max >= o.min_dp_max * o.a) {  // the hit of pe.c:291-304 and 361-368
+        const int qe = ej[k].qlen, te = ej[k].tlen;
+        int qs = qe - (E.reach_end ? qe : E.max_q + 1), qe2 = qe;
+        R.rescued = 1;
+        R.ts = res[i].ts2 + te - (E.reach_end ? E.mqe_t + 1 : E.max_t + 1);
+        R.te = res[i].ts2 + te;
+        const int32_t d2 = (int32_t)((double)E.max / R.ll_score * R.ll_score2 + .499);
+        R.dp_max2 = d2 < 0 ? 0 : d2;
+        if (jobs[i].rev) {
+          const int t = qs;
+          qs = jobs[i].qlen - qe2, qe2 = jobs[i].qlen - t;
+        }
+        R.qs = qs, R.qe = qe2;
+      }
+    }
+  }
+  if (cigar_used) *cigar_used = used;
+  return 0;
+}

@@ -35,6 +35,17 @@ LL_JOB = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "
 LL_RESULT = np.dtype([("score", "<i4"), ("te", "<i4"), ("qe", "<i4"), ("score2", "<i4"),
                       ("te2", "<i4"), ("rows", "<i4")])
 assert EXT_JOB.itemsize == 40 and EXT_RESULT.itemsize == 64 and LL_JOB.itemsize == 32 and LL_RESULT.itemsize == 24
+RESCUE_OPT = np.dtype([(k, "<i4") for k in ("a", "b", "b_ts", "b_ambi", "q", "e", "bw", "zdrop", "end_bonus",
+                                            "min_len", "min_dp_max")])
+RESCUE_JOB = np.dtype([("qoff", "<i8"), ("ts", "<i8"), ("te", "<i8"), ("qlen", "<i4"), ("tid", "<i4"),
+                       ("meth", "<i4"), ("min_sc", "<i4"), ("rev", "<i4"), ("pad", "<i4")])
+RESCUE_RESULT = np.dtype([("max_ug", "<i4"), ("max_i", "<i4"), ("n_good", "<i4"), ("n_kmer", "<i4"),
+                          ("ts2", "<i8"), ("te2", "<i8"),
+                          ("ll_done", "<i4"), ("ll_score", "<i4"), ("ll_te", "<i4"), ("ll_qe", "<i4"),
+                          ("ll_score2", "<i4"), ("ll_te2", "<i4"), ("ext_done", "<i4"), ("rescued", "<i4"),
+                          ("qs", "<i4"), ("qe", "<i4"), ("dp_max2", "<i4"), ("pad", "<i4"),
+                          ("ts", "<i8"), ("te", "<i8"), ("ext", EXT_RESULT)])
+assert RESCUE_OPT.itemsize == 44 and RESCUE_JOB.itemsize == 48 and RESCUE_RESULT.itemsize == 160
 
 
 class KswExtz(C.Structure):
@@ -108,6 +119,7 @@ def load_library():
         "ksw2g_ext_prepare_ref": (i32, [vp, vp, i32, i8, vp, i8, i8, i8, i8, i32, vp, vp, vp, u8p, i64,
                                         C.POINTER(vp)]),
         "ksw2g_ll_batch_ref": (i32, [vp, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp, u8p, i64, vp]),
+        "ksw2g_rescue_batch": (i32, [vp, vp, vp, i32, vp, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_graph_create": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
         "ksw2g_graph_launch": (i32, [vp, vp]),
         "ksw2g_graph_launches": (i32, [vp]),
@@ -399,6 +411,25 @@ class Reference:
         _check(self.L.ksw2g_ll_batch_ref(self.ctx.h, self.h, size, m, _ptr(mat), gapo, gape, len(jobs), _ptr(jobs),
                                          _ptr(tid), _ptr(tflags), _ptr(qbuf), len(qbuf), _ptr(res)))
         return res
+
+    def rescue_batch(self, opt, jobs, qbuf):
+        """Mate rescue of candidate windows (ksw2g_rescue_batch): opt is a dict or RESCUE_OPT
+        record of mb_opt_t scores, jobs a RESCUE_JOB array.  Returns (results, cigar words)."""
+        if isinstance(opt, dict):
+            o = np.zeros(1, RESCUE_OPT)
+            for k, v in opt.items():
+                o[k] = v
+            opt = o
+        opt = np.ascontiguousarray(opt, RESCUE_OPT)
+        jobs = np.ascontiguousarray(jobs, RESCUE_JOB)
+        qbuf = _u8(qbuf)
+        res = np.zeros(len(jobs), RESCUE_RESULT)
+        cap = int((jobs["qlen"].astype(np.int64) + jobs["te"] - jobs["ts"] + 1).sum()) + 16
+        cig = np.zeros(cap, np.uint32)
+        used = C.c_int64()
+        _check(self.L.ksw2g_rescue_batch(self.ctx.h, self.h, _ptr(opt), len(jobs), _ptr(jobs), _ptr(qbuf), len(qbuf),
+                                         _ptr(res), _ptr(cig), cap, C.byref(used)))
+        return res, cig[:used.value]
 
     def close(self):
         if self.h:

@@ -18,7 +18,7 @@ import os
 
 import numpy as np
 
-from .lib import EXT_JOB, LL_JOB, KSW_EZ_EXTZ_ONLY, gen_nt4_mat
+from .lib import EXT_JOB, LL_JOB, RESCUE_JOB, KSW_EZ_EXTZ_ONLY, gen_nt4_mat
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 SEED = 11
@@ -196,12 +196,21 @@ class Reference2b:
     at bits 2*(i%32)), contigs back to back, and sorted [st, en) runs of N.  N positions hold a
     random 2-bit base in pac, as l2b_import stores them."""
 
-    def __init__(self, ctg_len, n_runs=20, run_max=200, seed=SEED + 50):
+    def __init__(self, ctg_len, n_runs=20, run_max=200, seed=SEED + 50, n_repeats=0):
         rng = np.random.default_rng(seed)
         self.ctg_len = np.asarray(ctg_len, np.uint64)
         self.ctg_off = np.concatenate([[0], np.cumsum(self.ctg_len)[:-1]]).astype(np.uint64)
         tot = int(self.ctg_len.sum())
         self.bases = rng.integers(0, 4, tot).astype(np.uint8)
+        for _ in range(n_repeats):  # near-tandem copies (1% substitutions) 100-700 bases downstream
+            ln = int(rng.integers(100, 400))
+            src = int(rng.integers(0, max(tot - ln - 800, 1)))
+            dst = src + ln + int(rng.integers(0, 400))
+            if dst + ln <= tot:
+                cp = self.bases[src:src + ln].copy()
+                s = rng.random(ln) < 0.01
+                cp[s] = rng.integers(0, 4, int(s.sum()))
+                self.bases[dst:dst + ln] = cp
         starts = np.sort(rng.choice(max(tot - run_max, 1), n_runs, replace=False)) if n_runs else np.zeros(0, int)
         runs = []
         for st in starts:
@@ -266,3 +275,110 @@ def ref_pairs(ref, n, qlen_lo=100, qlen_hi=300, flank=50, w=100, dual=True, flag
     pairs = Pairs(host, np.concatenate(qparts), np.concatenate(tparts), dual, mat, 12, 2, q2, e2, "ref-windows")
     pairs.ref_toff = jobs["toff"].copy()
     return pairs, tids, tfl
+
+
+# minibwa's short-read defaults (options.c mb_opt_init / the "sr" preset)
+RESCUE_OPT_SR = dict(a=2, b=8, b_ts=0, b_ambi=1, q=12, e=2, bw=100, zdrop=80, end_bonus=10, min_len=19,
+                     min_dp_max=30)
+
+
+def _revcomp(x):
+    x = np.asarray(x, np.uint8)[::-1]
+    return np.where(x < 4, 3 - x, x).astype(np.uint8)
+
+
+class RescueCases:
+    """Mate-rescue candidates over a Reference2b: for each, an anchor hit (contig, ts, te, rev,
+    r0), one permitted orientation dir with insert bounds [lo, hi], the mate as sequenced and
+    its reverse complement (seq[0], seq[1]) and the library's methylation mode mt0.  window()
+    gives the candidate window and the read orientation of pe.c:330-339; jobs/qbuf are the
+    device call's inputs (the read in the orientation pe.c aligns, mt after l2b_meth_rev)."""
+
+    def __init__(self, ref, n, qlen_lo=100, qlen_hi=250, lo=50, hi=800, p_random=0.2, p_meth=0.25,
+                 p_edge=0.05, sub=0.02, indel=0.005, min_sc_hi=40, seed=SEED + 52):
+        rng = np.random.default_rng(seed)
+        self.ref, self.cases = ref, []
+        parts, jobs = [], []
+        off = 0
+        while len(self.cases) < n:
+            k = int(rng.integers(0, len(ref.ctg_len)))
+            clen = int(ref.ctg_len[k])
+            qlen = int(rng.integers(qlen_lo, qlen_hi + 1))
+            l0 = int(rng.integers(qlen_lo, qlen_hi + 1))
+            if clen < 3 * (hi + qlen + l0):
+                continue
+            if rng.random() < p_edge:
+                h_ts = int(rng.integers(0, 2 * hi)) if rng.random() < 0.5 else int(rng.integers(clen - 2 * hi, clen - l0))
+            else:
+                h_ts = int(rng.integers(0, clen - l0))
+            h_te, h_rev, r0, d = h_ts + l0, int(rng.integers(0, 2)), int(rng.integers(0, 2)), int(rng.integers(0, 4))
+            mt0 = int(rng.integers(1, 3)) if rng.random() < p_meth else 0
+            ts, te, is_rev = rescue_window(d, lo, hi, h_ts, h_te, h_rev, r0, qlen, clen)
+            if te - ts <= qlen:
+                continue
+            mt = meth_rev(mt0) if is_rev else mt0
+            if rng.random() < p_random:
+                m = rng.integers(0, 4, qlen).astype(np.uint8)
+            else:
+                ms = int(rng.integers(ts, te - qlen + 1))
+                m = ref.window(k, ms, qlen).copy()
+                m = _mutate(rng, m, sub, indel)
+                if mt:
+                    conv = rng.random(len(m)) < 0.9
+                    if mt == 1:
+                        m[(m == 1) & conv] = 3
+                    else:
+                        m[(m == 2) & conv] = 0
+            # the window follows the read's final length, as pe.c computes it from len
+            ts, te, is_rev = rescue_window(d, lo, hi, h_ts, h_te, h_rev, r0, len(m), clen)
+            if te - ts <= len(m):
+                continue
+            seq = [None, None]
+            seq[is_rev] = m
+            seq[1 - is_rev] = _revcomp(m)
+            min_sc = int(rng.integers(0, min_sc_hi + 1))
+            self.cases.append(dict(tid=k, h_ts=h_ts, h_te=h_te, h_rev=h_rev, r0=r0, dir=d, lo=lo, hi=hi, mt0=mt0,
+                                   seq=seq, min_sc=min_sc, ts=ts, te=te, is_rev=is_rev, mt=mt))
+            j = np.zeros(1, RESCUE_JOB)
+            j["qoff"], j["ts"], j["te"], j["qlen"], j["tid"] = off, ts, te, len(m), k
+            j["meth"], j["min_sc"], j["rev"] = mt, min_sc, is_rev
+            jobs.append(j), parts.append(m)
+            off += len(m)
+        self.jobs = np.concatenate(jobs)
+        self.qbuf = np.concatenate(parts)
+
+
+def rescue_window(dir, lo, hi, h_ts, h_te, h_rev, r0, qlen, ctg_len):
+    """The candidate window [ts, te) and read orientation of one orientation dir
+    (pe.c:330-339)."""
+    pos5 = h_te if h_rev else h_ts
+    is_rev = int((dir >> 1) != (dir & 1)) ^ h_rev
+    if (dir >> 1) != (dir & 1):
+        is_larger = (dir >> 1) ^ is_rev
+    else:
+        is_larger = (dir >> 1) ^ r0 ^ h_rev
+    ts = (pos5 + lo if is_larger else pos5 - hi) - (0 if not is_rev else qlen)
+    te = (pos5 + hi if is_larger else pos5 - lo) + (qlen if not is_rev else 0)
+    return max(ts, 0), min(te, int(ctg_len)), is_rev
+
+
+def meth_rev(mt):
+    """l2b_meth_rev (l2bit.h:63-66)."""
+    return 0 if mt == 0 else 2 if mt == 1 else 1
+
+
+def _mutate(rng, m, sub, indel):
+    m = m.copy()
+    s = rng.random(len(m)) < sub
+    m[s] = rng.integers(0, 4, int(s.sum()))
+    out, i = [], 0
+    while i < len(m):
+        u = rng.random()
+        if u < indel / 2:
+            i += int(rng.integers(1, 4))
+            continue
+        if u < indel:
+            out.extend(rng.integers(0, 4, int(rng.integers(1, 4))).tolist())
+        out.append(int(m[i]))
+        i += 1
+    return np.array(out, np.uint8)

@@ -708,3 +708,46 @@ void orc_l2b_getseq(const uint64_t *pac, const uint64_t *ctg_off, int64_t n_ambi
 		}
 	}
 }
+
+/* mb_ungap (pe.c:209-247): the 7-mer Hough transform that pe.c's mate rescue runs before
+ * ksw_ll.  Every k-mer of the query (bases after the methylation table of mt: 0 none, 1 C2T,
+ * 2 G2A) records the last query position where it ends; every k-mer of the target that the
+ * query holds votes for the diagonal i - h[x].  Returns the top vote count; *max_i is its
+ * first diagonal, *n_good the diagonals with more than half of it, *n_kmer the distinct
+ * query k-mers. */
+int orc_ungap(int qlen, const uint8_t *qseq, int tlen, const uint8_t *tseq, int kmer, int mt, int *max_i,
+			  int *n_good, int *n_kmer)
+{
+	static const uint8_t c2t[4] = {0, 3, 2, 3}, g2a[4] = {0, 1, 0, 3};
+	int i, l, cap = 1 << kmer * 2, mask = cap - 1, max;
+	int32_t *a;
+	uint16_t *h, x;
+	*max_i = -1, *n_good = *n_kmer = 0;
+	if (qlen >= 65535) return 0;
+	a = (int32_t *)calloc(tlen > 0 ? tlen : 1, sizeof(int32_t));
+	h = (uint16_t *)calloc(cap, sizeof(uint16_t));
+	for (i = l = 0, x = 0; i < qlen; ++i) {
+		if (qseq[i] < 4) {
+			uint8_t c = mt == 1 ? c2t[qseq[i]] : mt == 2 ? g2a[qseq[i]] : qseq[i];
+			x = (uint16_t)((x << 2 | c) & mask);
+			if (++l >= kmer) {
+				if (h[x] == 0) ++*n_kmer;
+				h[x] = (uint16_t)i;
+			}
+		} else x = 0, l = 0;
+	}
+	for (i = l = 0, x = 0; i < tlen; ++i) {
+		if (tseq[i] < 4) {
+			uint8_t c = mt == 1 ? c2t[tseq[i]] : mt == 2 ? g2a[tseq[i]] : tseq[i];
+			x = (uint16_t)((x << 2 | c) & mask);
+			if (++l >= kmer && h[x] > 0 && i >= h[x]) ++a[i - h[x]];
+		} else x = 0, l = 0;
+	}
+	for (i = 0, max = 0; i < tlen; ++i)
+		if (max < a[i]) max = a[i], *max_i = i;
+	for (i = 0, *n_good = 0; i < tlen; ++i)
+		if (a[i] > max >> 1) ++*n_good;
+	free(h);
+	free(a);
+	return max;
+}

@@ -98,6 +98,9 @@ void orc_ll_batch(int size, int n_jobs, const orc_job_t *jobs, const uint8_t *qb
 void orc_l2b_getseq(const uint64_t *pac, const uint64_t *ctg_off, int64_t n_ambi, const uint64_t *ambi, int64_t tid,
 					int64_t st, int64_t len, int flags, uint8_t *seq);
 
+int orc_ungap(int qlen, const uint8_t *qseq, int tlen, const uint8_t *tseq, int kmer, int mt, int *max_i,
+			  int *n_good, int *n_kmer);
+
 #ifdef __cplusplus
 }
 #endif

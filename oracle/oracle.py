@@ -3,6 +3,7 @@
   liboracle.so        scalar C restatement of the reference (ksw2_oracle.c), builds anywhere
   _ref/libksw2ref.so  the reference's own ksw2 SSE sources, built here from the reference
                       tree when it is present (never on a machine without it)
+  _ref/libmbpe.so     the reference's mate rescue (pe.c) behind ref_pe.c, same conditions
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use this module,
 and only as the checker / the timed CPU baseline -- never as a product code path.
@@ -17,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_TREE = os.environ.get("KSW2_REF_TREE", "/root/reference")
 LIB_ORACLE = os.path.join(HERE, "liboracle.so")
 LIB_REF = os.path.join(HERE, "_ref", "libksw2ref.so")
+LIB_MBPE = os.path.join(HERE, "_ref", "libmbpe.so")
 
 ORC_JOB = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"),
                     ("w", "<i4"), ("zdrop", "<i4"), ("end_bonus", "<i4"), ("flag", "<i4")])
@@ -91,6 +93,8 @@ def _load(path, prefix):
         L.orc_ll_rows.argtypes = [vp]
         L.orc_l2b_getseq.restype = None
         L.orc_l2b_getseq.argtypes = [vp, vp, i64, vp, i64, i64, i64, i32, vp]
+        L.orc_ungap.restype = i32
+        L.orc_ungap.argtypes = [i32, vp, i32, vp, i32, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
     _libs[path] = L
     return L
 
@@ -99,6 +103,27 @@ def oracle_lib():
     if not os.path.exists(LIB_ORACLE):
         build(ref=False)
     return _load(LIB_ORACLE, "orc_")
+
+
+def have_ref_pe():
+    return os.path.exists(LIB_MBPE)
+
+
+def refpe_lib():
+    if not have_ref_pe():
+        raise RuntimeError("reference rescue build not available (oracle/_ref)")
+    if LIB_MBPE not in _libs:
+        L = C.CDLL(LIB_MBPE)
+        vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
+        L.refpe_ungap.restype = i32
+        L.refpe_ungap.argtypes = [i32, vp, i32, vp, i32, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
+        L.refpe_matesw.restype = i32
+        L.refpe_matesw.argtypes = [i64, vp, vp, vp, i64, i64, vp, vp, i32, i32, i32, i64, i64, i64, i32, i32, i32,
+                                   vp, vp, i32, i32, vp, vp, i32]
+        L.refpe_getseq.restype = i64
+        L.refpe_getseq.argtypes = [i64, vp, vp, vp, i64, i64, vp, i64, i64, i64, vp]
+        _libs[LIB_MBPE] = L
+    return _libs[LIB_MBPE]
 
 
 def ref_lib():
@@ -194,3 +219,156 @@ def l2b_getseq(ref, tid, st, length, flags=0):
                      len(amb) // 2, _p(amb) if len(amb) else None, int(tid), int(st), int(length), int(flags),
                      _p(out))
     return out[:int(length)]
+
+
+def ungap(query, target, kmer=7, mt=0):
+    """mb_ungap (pe.c:209-247); returns (max, max_i, n_good, n_kmer)."""
+    L = oracle_lib()
+    q = np.ascontiguousarray(query, np.uint8)
+    t = np.ascontiguousarray(target, np.uint8)
+    mi, ng, nk = C.c_int(), C.c_int(), C.c_int()
+    mx = L.orc_ungap(len(q), _p(q) if len(q) else None, len(t), _p(t) if len(t) else None, kmer, mt, C.byref(mi),
+                     C.byref(ng), C.byref(nk))
+    return mx, mi.value, ng.value, nk.value
+
+
+def ref_ungap(query, target, kmer=7, mt=0):
+    """The reference's own mb_ungap (through _ref/libmbpe.so)."""
+    L = refpe_lib()
+    q = np.ascontiguousarray(query, np.uint8)
+    t = np.ascontiguousarray(target, np.uint8)
+    mi, ng, nk = C.c_int(), C.c_int(), C.c_int()
+    mx = L.refpe_ungap(len(q), _p(q) if len(q) else None, len(t), _p(t) if len(t) else None, kmer, mt, C.byref(mi),
+                       C.byref(ng), C.byref(nk))
+    return mx, mi.value, ng.value, nk.value
+
+
+def _l2b_args(ref):
+    off = np.ascontiguousarray(ref.ctg_off, np.uint64)
+    ln = np.ascontiguousarray(ref.ctg_len, np.uint64)
+    pac = np.ascontiguousarray(ref.pac, np.uint64)
+    amb = np.ascontiguousarray(ref.ambi, np.uint64).reshape(-1)
+    return (off, ln, pac, amb), (len(off), _p(off), _p(ln), _p(pac), len(pac), len(amb) // 2,
+                                 _p(amb) if len(amb) else None)
+
+
+def ref_getseq(ref, tid, st, en):
+    """The reference's own l2b_getseq (l2bit.c:52-77) on [st, en) of contig tid."""
+    L = refpe_lib()
+    keep, args = _l2b_args(ref)
+    out = np.zeros(max(int(en) - int(st), 1), np.uint8)
+    n = L.refpe_getseq(*args, int(tid), int(st), int(en), _p(out))
+    return out[:max(int(n), 0)]
+
+
+RESCUE_SC = ("a", "b", "b_ts", "b_ambi", "q", "e", "bw", "zdrop", "end_bonus", "min_len", "min_dp_max")
+HIT_FIELDS = ("rescued", "ts", "te", "qs", "qe", "rev", "dp_max", "dp_max2", "score", "subsc", "n_cigar")
+
+
+def ref_matesw(ref, opt, dir, lo, hi, tid, h_ts, h_te, h_rev, r0, seq_fwd, seq_rc, mt0, min_sc):
+    """The reference's own mb_matesw_core for one permitted orientation (pe.c:323-377), with
+    mb_update_extra left out; returns None (no hit) or the hit's fields and CIGAR."""
+    L = refpe_lib()
+    sc = np.array([opt[k] for k in RESCUE_SC], np.int32)
+    keep, args = _l2b_args(ref)
+    f = np.ascontiguousarray(seq_fwd, np.uint8).copy()
+    r = np.ascontiguousarray(seq_rc, np.uint8).copy()
+    out = np.zeros(11, np.int64)
+    cig = np.zeros(len(f) * 2 + 16, np.uint32)
+    rc = L.refpe_matesw(*args, _p(sc), dir, lo, hi, tid, h_ts, h_te, h_rev, r0, len(f), _p(f), _p(r), mt0, min_sc, _p(out),
+                        _p(cig), len(cig))
+    if rc != 0:
+        raise RuntimeError("CIGAR buffer too small")
+    if out[10] == 0 and out[0] == 0:
+        return None
+    d = {k: int(v) for k, v in zip(HIT_FIELDS, out)}
+    d["cigar"] = [int(x) for x in cig[:d["n_cigar"]]]
+    return d
+
+
+def rescue_window(dir, lo, hi, h_ts, h_te, h_rev, r0, qlen, ctg_len):
+    """The candidate window and read orientation of one orientation dir (pe.c:330-339)."""
+    pos5 = h_te if h_rev else h_ts
+    is_rev = int((dir >> 1) != (dir & 1)) ^ h_rev
+    if (dir >> 1) != (dir & 1):
+        is_larger = (dir >> 1) ^ is_rev
+    else:
+        is_larger = (dir >> 1) ^ r0 ^ h_rev
+    ts = (pos5 + lo if is_larger else pos5 - hi) - (0 if not is_rev else qlen)
+    te = (pos5 + hi if is_larger else pos5 - lo) + (qlen if not is_rev else 0)
+    return max(ts, 0), min(te, int(ctg_len)), is_rev
+
+
+def meth_rev(mt):
+    """l2b_meth_rev (l2bit.h:63-66)."""
+    return 0 if mt == 0 else 2 if mt == 1 else 1
+
+
+def gen_nt4_mat(a, b, b_ts, b_ambi, mt=0):
+    """ksw_gen_nt4_mat (ksw2.h:199-219), int8 arguments as there."""
+    a, b, b_ts, b_ambi = (int(np.int8(x)) for x in (a, b, b_ts, b_ambi))
+    a, b, b_ambi = abs(a), -abs(b), -abs(b_ambi)
+    mat = np.zeros(25, np.int8)
+    for i in range(4):
+        for j in range(4):
+            mat[i * 5 + j] = a if i == j else b
+        mat[i * 5 + 4] = b_ambi
+    mat[20:25] = b_ambi
+    if b_ts != 0 and b_ts != b:
+        mat[2] = mat[8] = mat[10] = mat[16] = -abs(b_ts)
+    if mt == 1:
+        mat[8] = a
+    elif mt == 2:
+        mat[10] = a
+    return mat
+
+
+def rescue(ref, opt, tid, ts, te, query, meth, min_sc, rev):
+    """One rescue candidate through the oracle's restatements: l2b_getseq, mb_ungap, the
+    narrowing and thresholds of pe.c:347-353, ksw_ll with the matrix scaled by a and extz2 on
+    the reversed prefixes (pe.c:249-300), the hit as pe.c:291-304 and 361-368 derive it.
+    Returns the fields of ksw2g_rescue_result_t that the device pipeline fills, and the CIGAR."""
+    o = opt
+    q = np.ascontiguousarray(query, np.uint8)
+    qlen = len(q)
+    ref_seq = l2b_getseq(ref, tid, ts, te - ts)
+    max_ug, max_i, n_good, n_kmer = ungap(q, ref_seq, 7, meth)
+    out = dict(max_ug=max_ug, max_i=max_i, n_good=n_good, n_kmer=n_kmer, ts2=ts, te2=te, ll_done=0, ext_done=0,
+               rescued=0, cigar=[])
+    ts2, te2 = ts, te
+    if max_ug >= 10 and max_ug >= qlen >> 1 and n_good == 1:
+        ts2 = ts + max_i - qlen // 2
+        te2 = ts2 + qlen * 2
+        ts2, te2 = max(ts2, ts), min(te2, te)
+    out["ts2"], out["te2"] = ts2, te2
+    if not (max_ug >= 10 or max_ug >= n_kmer * 0.33):
+        return out
+    t = ref_seq[ts2 - ts:te2 - ts]
+    max_sc = min(qlen, len(t))
+    if max_sc >= 32767:
+        return out
+    a = o["a"]
+    b_mm = (o["b"] + a - 1) // a
+    mat = gen_nt4_mat(1, b_mm, (o["b_ts"] + a - 1) // a, (o["b_ambi"] + a - 1) // a, meth)
+    size = 1 if max_sc < 255 - b_mm else 2
+    r, _ = ll(size, q, t, 5, mat, (o["q"] + a - 1) // a, (o["e"] + a - 1) // a, 0x40000 | o["min_len"])
+    out.update(ll_done=1, ll_score=r["score"], ll_te=r["te"], ll_qe=r["qe"], ll_score2=r["score2"], ll_te2=r["te2"])
+    if not (r["score"] >= o["min_dp_max"] and r["score"] >= min_sc):
+        return out
+    qe, te_ = r["qe"] + 1, r["te"] + 1
+    flag = 0x40 | 0x02 | 0x80 | (0x04 if meth else 0)  # EXTZ_ONLY | RIGHT | REV_CIGAR (| GENERIC_SC)
+    mat = gen_nt4_mat(a, o["b"], o["b_ts"], o["b_ambi"], meth)
+    ez, _ = extz(0, q[:qe][::-1], t[:te_][::-1], 5, mat, o["q"], o["e"], o["q"], o["e"], o["bw"], o["zdrop"],
+                 o["end_bonus"], flag)
+    out["ext_done"] = 1
+    out["ext"] = ez
+    out["cigar"] = ez["cigar"]
+    if ez["n_cigar"] > 0 and ez["max"] >= o["min_dp_max"] * a:
+        qs = qe - (qe if ez["reach_end"] else ez["max_q"] + 1)
+        qe2 = qe
+        hts = ts2 + te_ - (ez["mqe_t"] + 1 if ez["reach_end"] else ez["max_t"] + 1)
+        d2 = int(np.int32(int(np.float64(ez["max"]) / r["score"] * r["score2"] + .499)))
+        if rev:
+            qs, qe2 = qlen - qe2, qlen - qs
+        out.update(rescued=1, ts=hts, te=ts2 + te_, qs=qs, qe=qe2, dp_max2=max(d2, 0))
+    return out

@@ -226,3 +226,15 @@ inline unsigned long long atomicAdd(unsigned long long *p, unsigned long long v)
   return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST);
 }
 inline int atomicOr(int *p, int v) { return __atomic_fetch_or(p, v, __ATOMIC_SEQ_CST); }
+inline int atomicMax(int *p, int v) {
+  int o = __atomic_load_n(p, __ATOMIC_SEQ_CST);
+  while (o < v && !__atomic_compare_exchange_n(p, &o, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+  }
+  return o;
+}
+inline int atomicMin(int *p, int v) {
+  int o = __atomic_load_n(p, __ATOMIC_SEQ_CST);
+  while (o > v && !__atomic_compare_exchange_n(p, &o, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+  }
+  return o;
+}

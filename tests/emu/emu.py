@@ -52,6 +52,8 @@ def lib():
         _L.emu_shape_threads.restype = i
         _L.emu_shape_threads.argtypes = [i]
         _L.emu_num_shapes.restype = i
+        _L.emu_ungap.restype = i
+        _L.emu_ungap.argtypes = [i, vp, vp, vp, vp, vp, C.c_longlong]
     return _L
 
 
@@ -152,3 +154,33 @@ def ll(size, m, mat, gapo, gape, qs, ts, xtra, threads=None, dpx=False):
     if rc != 0:
         raise RuntimeError(f"emu_ll rc={rc}")
     return res
+
+
+UNGAP_JOB = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"), ("meth", "<i4"),
+                      ("pad", "<i4")])
+
+
+def ungap(pairs, meth, global_hist=False):
+    """mb_ungap of (query, target) pairs through the emulated device kernel; returns a list of
+    (max, max_i, n_good, n_kmer).  Targets sit in a padded arena as the window gather leaves them."""
+    L = lib()
+    n = len(pairs)
+    jobs = np.zeros(n, UNGAP_JOB)
+    qs, ts, qo, to = [], [], 0, 0
+    for i, (q, t) in enumerate(pairs):
+        jobs[i]["qoff"], jobs[i]["qlen"], jobs[i]["toff"] = qo, len(q), to + 32
+        jobs[i]["tlen"], jobs[i]["meth"] = len(t), meth[i]
+        qs.append(np.asarray(q, np.uint8))
+        qo += len(q)
+        slot = np.zeros(slot_bytes(len(t)), np.uint8)
+        slot[32:32 + len(t)] = t
+        ts.append(slot)
+        to += len(slot)
+    qa = np.concatenate(qs + [np.zeros(16, np.uint8)])
+    ta = np.concatenate(ts + [np.zeros(64, np.uint8)])
+    res = np.zeros((n, 4), np.int32)
+    cap = max([len(t) for _, t in pairs] + [1])
+    hist = np.zeros(cap, np.int32) if global_hist else None
+    L.emu_ungap(n, jobs.ctypes.data, qa.ctypes.data, ta.ctypes.data, res.ctypes.data,
+                hist.ctypes.data if hist is not None else None, cap if global_hist else 0)
+    return [tuple(int(x) for x in r) for r in res]

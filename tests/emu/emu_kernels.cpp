@@ -22,11 +22,13 @@ LaneState g_lane_state[1024];
 #include "../../minibwa_gb300/csrc/host_common.h"
 #include "../../minibwa_gb300/csrc/ll.cuh"
 #include "../../minibwa_gb300/csrc/shapes.h"
+#include "../../minibwa_gb300/csrc/ungap.cuh"
 
 namespace ksw2g {
 alignas(16) int16_t ll_smem[1 << 20];
 alignas(16) uint32_t lld_smem[1 << 20];
 alignas(16) int16_t llw_smem[1 << 22];
+alignas(16) uint32_t ug_smem[kUngapSmemMax / 4];
 }
 
 using namespace ksw2g;
@@ -159,6 +161,15 @@ int emu_ll(int size, int slen_max, int n, const ksw2g_ll_job *jobs, const uint8_
   }
   if (!f) return -1;
   run_block(threads, [&] { f(jobs, n, arena, mat, m, gapo, gape, res, blist, blist_off, &counter); });
+  return 0;
+}
+
+// mb_ungap of every job with one emulated block (shared-memory histogram when
+// ghist is null, else ghist[0, hist_cap)).
+int emu_ungap(int n, const UngapJob *jobs, const uint8_t *qarena, const uint8_t *tarena, UngapRes *res,
+              int32_t *ghist, long long hist_cap) {
+  int counter = 0;
+  run_block(kUngapThreads, [&] { ungap_kernel(n, jobs, qarena, tarena, res, &counter, ghist, hist_cap); });
   return 0;
 }
 }

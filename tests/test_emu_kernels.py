@@ -138,3 +138,30 @@ def test_emulated_block_wide_kernel(emu):
                 for f in got:
                     assert got[f] == exp[f], (flag, dual, k, f, got[f], exp[f])
                 assert cig[k] == exp["cigar"], (flag, dual, k)
+
+
+@pytest.mark.parametrize("global_hist", [False, True])
+def test_emulated_ungap_kernel(emu, global_hist):
+    """The device mb_ungap (shared-memory or global vote histogram) against the oracle's
+    restatement, on the golden rescue windows plus planted, N-rich and degenerate pairs."""
+    from oracle import oracle as O
+    from test_rescue import load_rescue_golden
+    g, ref, opt = load_rescue_golden()
+    pairs, meth = [], []
+    for j in g["jobs"][:120]:
+        pairs.append((g["qbuf"][j["qoff"]:j["qoff"] + j["qlen"]],
+                      O.l2b_getseq(ref, int(j["tid"]), int(j["ts"]), int(j["te"] - j["ts"]))))
+        meth.append(int(j["meth"]))
+    rng = np.random.default_rng(17)
+    for it in range(40):
+        q = rng.integers(0, 4, int(rng.integers(0, 300))).astype(np.uint8)
+        t = rng.integers(0, 4, int(rng.integers(0, 2000))).astype(np.uint8)
+        if len(t) > len(q) and it % 2:
+            p = int(rng.integers(0, len(t) - len(q) + 1))
+            t[p:p + len(q)] = q
+        if it % 3 == 0 and len(t):
+            t[rng.random(len(t)) < 0.03] = 4
+        pairs.append((q, t)), meth.append(it % 3)
+    got = emu.ungap(pairs, meth, global_hist)
+    for i, ((q, t), mt) in enumerate(zip(pairs, meth)):
+        assert got[i] == O.ungap(q, t, 7, mt), i
