@@ -59,6 +59,8 @@ WORKLOADS = {
     "cfg2": "cfg2: 200k long extd2 (log-normal median 2 kb, w=500) + 1M short extz2 (150 nt, w=25), "
             "one CUDA graph, CIGAR",
     "cfg3": "cfg3: 2M ksw_ll i16 rescue jobs, 150 nt vs 500-1000 nt",
+    "rescue": "rescue: 500k pe.c mate-rescue candidates (mb_ungap + ksw_ll + reverse extz2) over an "
+              "80 Mb resident 2-bit reference, reads 100-250 nt, insert bounds [50, 800]",
 }
 
 
@@ -235,11 +237,147 @@ def cpu_baseline(w, sample, reference_preferred=True):
             "sample": f"first {n_done} units of the workload (same mix), {threads} threads, {dt:.2f} s wall"}, dt
 
 
-DEFAULT_SAMPLE = {"cfg1": 40000, "cfg0": 20000, "cfg2": 6000, "cfg3": 40000}
+DEFAULT_SAMPLE = {"cfg1": 40000, "cfg0": 20000, "cfg2": 6000, "cfg3": 40000, "rescue": 60000}
+
+
+def rescue_cpu_baseline(ref, jobs, qbuf, sample):
+    """The CPU restatement of the rescue (oracle/rescue_cpu.c) on the first `sample` candidates
+    with all host threads; returns (baseline dict, its results, CIGAR words)."""
+    from minibwa_gb300 import synth
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    k = min(sample, len(jobs))
+    t0 = time.perf_counter()
+    res, cig = O.rescue_batch(ref, synth.RESCUE_OPT_SR, jobs[:k], qbuf, threads)
+    dt = time.perf_counter() - t0
+    return ({"value": k / dt, "unit": "candidates/s", "cores": threads, "kind": "port",
+             "sample": f"first {k} candidates of the workload, {threads} threads, {dt:.2f} s wall "
+                       f"(scalar C restatement of pe.c's rescue over the oracle's ksw2 restatement)"},
+            res, cig, dt)
+
+
+def run_rescue(args, rank, world):
+    """The mate-rescue workload: every step is one ksw2g_rescue_batch call over all candidates
+    (reads and job records from pinned host memory, results and CIGARs back to the host); the
+    2-bit reference stays resident in HBM.  The call's stages read one another's results on the
+    host, so there is no device-only variant: value and e2e are the same timed call."""
+    import torch
+    from minibwa_gb300 import Context, Reference, synth
+    from minibwa_gb300 import lib as K
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    L = K.load_library()
+    n = args.pairs or 500000
+    ref, jobs, qbuf = synth.rescue_workload(n, seed=synth.SEED + 60 + 1000 * rank)
+    ctx = Context(dev)
+    dref = Reference(ctx, ref.pac, ref.ctg_off, ref.ctg_len, ref.ambi)
+    opt = np.zeros(1, K.RESCUE_OPT)
+    for k_, v in synth.RESCUE_OPT_SR.items():
+        opt[k_] = v
+
+    def pinned(a):
+        t = torch.empty(max(1, a.nbytes), dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:a.nbytes] = a.view(np.uint8).reshape(-1)
+        return t
+
+    hj, hq = pinned(jobs), pinned(qbuf)
+    hres = torch.empty(n * K.RESCUE_RESULT.itemsize, dtype=torch.uint8, pin_memory=True)
+    cap = int((jobs["qlen"].astype(np.int64) + jobs["te"] - jobs["ts"] + 1).sum()) + 16
+    hcig = torch.empty(cap * 4, dtype=torch.uint8, pin_memory=True)
+    used = C.c_int64()
+
+    def step():
+        rc = L.ksw2g_rescue_batch(ctx.h, dref.h, opt.ctypes.data, n, hj.data_ptr(), hq.data_ptr(), len(qbuf),
+                                  hres.data_ptr(), hcig.data_ptr(), cap, C.byref(used))
+        if rc != 0:
+            raise RuntimeError(L.ksw2g_last_error().decode())
+
+    for _ in range(args.warmup):
+        step()
+    barrier(world)
+    torch.cuda.synchronize()
+    stage_ms = np.zeros(3)
+    launches = 0
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+            nl, ms3 = dref.rescue_stats()
+            launches += nl
+            stage_ms += ms3
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / args.steps
+    dt_max = allmax(dt, world)
+    barrier(world)
+    tot = allsum(n, world)
+    value = tot / dt_max
+    res = np.frombuffer(hres.numpy().tobytes(), K.RESCUE_RESULT)
+    cig = np.frombuffer(hcig.numpy()[:4 * used.value].tobytes(), np.uint32)
+    cb = None
+    checked = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb, ores, ocig, _ = rescue_cpu_baseline(ref, jobs, qbuf, args.cpu_sample or DEFAULT_SAMPLE["rescue"])
+        k = len(ores)
+        same = all(np.array_equal(res[f][:k], ores[f]) for f in
+                   ("max_ug", "max_i", "n_good", "n_kmer", "ts2", "te2", "ll_score", "ll_te", "ll_qe", "ll_score2",
+                    "rescued", "qs", "qe", "ts", "te", "dp_max2"))
+        for i in np.nonzero(ores["ext"]["n_cigar"] > 0)[0][:2000]:
+            a, b = res[i]["ext"], ores[i]["ext"]
+            same &= bool(np.array_equal(cig[a["cigar_off"]:a["cigar_off"] + a["n_cigar"]],
+                                        ocig[b["cigar_off"]:b["cigar_off"] + b["n_cigar"]]))
+        checked = f"first {k} candidates equal the CPU restatement field by field: {bool(same)}"
+    if rank == 0:
+        h2d = jobs.nbytes + len(qbuf)
+        d2h = res.nbytes + 4 * used.value
+        stage_ms /= args.steps
+        line = {
+            "metric": "rescue candidates/s", "value": value, "unit": "candidates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt_max * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int8/int16",
+            "data": "synthetic (seeded splitmix64 candidates over a seeded reference, no public dataset)",
+            "config": {"workload": WORKLOADS["rescue"], "units_per_gpu": n, "parallelism": f"replicas x{world}",
+                       "value_is_e2e": "the stages read each other's results on the host; the reference is "
+                                       "resident, reads and results cross PCIe/C2C every step",
+                       "rescued_fraction": float(res["rescued"].mean()),
+                       "ll_fraction": float(res["ll_done"].mean())},
+            "stages_ms": {"gather_prefilter": stage_ms[0], "ksw_ll": stage_ms[1], "extz2": stage_ms[2]},
+            "gpu_launches": launches,
+            "roofline": None,
+            "e2e": {"value": value, "unit": "candidates/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": dt_max * 1e3},
+            "clocks": clk.summary(),
+        }
+        if cb:
+            line["cpu_baseline"] = cb
+            line["parity"] = checked
+        print(json.dumps(line), flush=True)
+    dref.close()
+    ctx.close()
 
 
 def run_reference(args, rank, world):
     if rank != 0:
+        return
+    if args.workload == "rescue":
+        from minibwa_gb300 import synth
+        sample = args.cpu_sample or DEFAULT_SAMPLE["rescue"]
+        ref, jobs, qbuf = synth.rescue_workload(sample)
+        for _ in range(args.warmup):
+            rescue_cpu_baseline(ref, jobs, qbuf, max(1, sample // 20))
+        times = []
+        for _ in range(args.steps):
+            cb, _, _, dt = rescue_cpu_baseline(ref, jobs, qbuf, sample)
+            times.append(dt)
+        v = len(times) * sample / sum(times)
+        cb["value"] = v
+        print(json.dumps({"impl": "reference", "metric": "rescue candidates/s", "value": v, "unit": "candidates/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "int8/int16",
+                          "data": "synthetic (seeded splitmix64)",
+                          "config": {"workload": WORKLOADS["rescue"], "units_per_step": sample},
+                          "cpu_baseline": cb, "e2e": {"value": v, "unit": "candidates/s", "h2d_bytes_per_step": 0,
+                                                      "d2h_bytes_per_step": 0}}), flush=True)
         return
     w = Workload(args.workload, args, 0) if args.workload != "cfg1" else None
     if w is None:
@@ -273,6 +411,9 @@ def main():
     rank, world = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "rescue":
+        run_rescue(args, rank, world)
         return
     import torch
     from minibwa_gb300 import Context, Graph

@@ -173,6 +173,9 @@ typedef struct {
 int ksw2g_rescue_batch(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, const ksw2g_rescue_opt_t *opt, int n_jobs,
 					   const ksw2g_rescue_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
 					   ksw2g_rescue_result_t *res, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used);
+/* The last rescue call of ctx: kernels launched, and the wall time (ms) of its three
+ * stages (window gather + prefilter, ksw_ll, extz2), each including its copies. */
+int ksw2g_rescue_last_stats(const ksw2g_ctx_t *ctx, int *launches, double *ms3);
 
 /* ---- CUDA graphs: one launch runs several prepared batches concurrently ----
  * Captures the kernels of n prepared batches (extension or ll) into one CUDA

@@ -88,6 +88,8 @@ struct ksw2g_ctx {
   PinBuf one_h;         // per-call drop-in staging (pinned)
   DevBuf rs_q, rs_t, rs_meta, rs_res, rs_hist;  // mate-rescue prefilter: reads, windows, records, votes
   PinBuf rs_h;                                  // mate-rescue staging (pinned)
+  int rs_launches = 0;                          // kernels the last rescue call launched
+  double rs_ms[3] = {0, 0, 0};                  // its stages' wall time: prefilter, ksw_ll, extz2
   ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
   // two sub-contexts (own stream and traceback pool, half the budget each) that the
   // one-shot extension call alternates between, so the host prepares one chunk

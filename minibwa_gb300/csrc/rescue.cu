@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <vector>
 
 #include "../../include/ksw2.h"
@@ -54,6 +55,10 @@ void gen_nt4(int8_t *mat, int8_t a, int8_t b, int8_t b_ts, int8_t b_ambi, int mt
 
 inline int64_t al16(int64_t x) { return (x + 15) & ~(int64_t)15; }
 
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 }  // namespace
 
 extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const ksw2g_rescue_opt_t *opt, int n,
@@ -64,9 +69,11 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     return report_error(KSW2G_E_ARG, "rescue: bad arguments");
   if (opt->a <= 0) return report_error(KSW2G_E_ARG, "rescue: the match score must be positive");
   if (cigar_used) *cigar_used = 0;
+  c->rs_launches = 0, c->rs_ms[0] = c->rs_ms[1] = c->rs_ms[2] = 0;
   if (n == 0) return 0;
   if (cudaSetDevice(c->device) != cudaSuccess) return report_error(KSW2G_E_CUDA, "rescue: bad device");
   const ksw2g_rescue_opt_t &o = *opt;
+  auto t0 = std::chrono::steady_clock::now();
   int rc;
   for (int i = 0; i < n; ++i) {
     const ksw2g_rescue_job_t &J = jobs[i];
@@ -126,6 +133,9 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
           cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return report_error(KSW2G_E_CUDA, "rescue: prefilter failed");
+  c->rs_launches += 2;
+  c->rs_ms[0] = ms_since(t0);
+  t0 = std::chrono::steady_clock::now();
 
   // ---- stage 2: narrowing and thresholds (pe.c:347-353), then ksw_ll per (size, methylation) group
   const int b_mm = (o.b + o.a - 1) / o.a, b_ts = (o.b_ts + o.a - 1) / o.a, b_ambi = (o.b_ambi + o.a - 1) / o.a;
@@ -170,6 +180,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
       if ((rc = ksw2g_ll_batch_ref(c, ref, size, 5, mat, gapo, gape, (int)idx.size(), lj.data(), tids.data(),
                                    nullptr, qbuf, qbuf_len, lr.data())))
         return rc;
+      c->rs_launches += 1 + ksw2g_batch_launches(c->scratch);  // the window gather, then the DP
       for (size_t k = 0; k < idx.size(); ++k) {
         ksw2g_rescue_result_t &R = res[idx[k]];
         R.ll_done = 1, R.ll_score = lr[k].score, R.ll_te = lr[k].te, R.ll_qe = lr[k].qe;
@@ -177,6 +188,8 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
       }
     }
 
+  c->rs_ms[1] = ms_since(t0);
+  t0 = std::chrono::steady_clock::now();
   // ---- stage 3: extz2 on the reversed prefixes ending at ksw_ll's end (pe.c:283-300)
   int64_t used = 0;
   for (int mt = 0; mt <= 2; ++mt) {
@@ -192,37 +205,34 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     const int flag = KSW_EZ_EXTZ_ONLY | KSW_EZ_RIGHT | KSW_EZ_REV_CIGAR | (mt ? KSW_EZ_GENERIC_SC : 0);
     std::vector<ksw2g_job_t> ej(idx.size());
     std::vector<int32_t> tids(idx.size()), tfl(idx.size(), KSW2G_REF_REVERSE);
-    std::vector<uint8_t> rq;
-    int64_t cap = 16;
+    int64_t rq_len = 0;
+    for (int i : idx) rq_len += res[i].ll_qe + 1;
+    std::vector<uint8_t> rq((size_t)std::max<int64_t>(rq_len, 1));
+    int64_t qo = 0;
     for (size_t k = 0; k < idx.size(); ++k) {
       const int i = idx[k];
       const int qe = res[i].ll_qe + 1, te = res[i].ll_te + 1;
-      const int64_t qo = (int64_t)rq.size();
-      for (int p = qe - 1; p >= 0; --p) rq.push_back(qbuf[jobs[i].qoff + p]);  // mb_seq_rev(qe, qseq)
+      const uint8_t *src = qbuf + jobs[i].qoff;
+      for (int p = 0; p < qe; ++p) rq[qo + p] = src[qe - 1 - p];  // mb_seq_rev(qe, qseq)
       ej[k] = ksw2g_job_t{qo, res[i].ts2, qe, te, o.bw, o.zdrop, o.end_bonus, flag};
       tids[k] = jobs[i].tid;
-      cap += (int64_t)qe + te + 1;
+      qo += qe;
     }
     std::vector<ksw2g_ext_result_t> er(idx.size());
-    std::vector<uint32_t> cg((size_t)cap);
     int64_t u = 0;
+    // CIGARs go straight into the caller's buffer behind those of earlier groups
     if ((rc = ksw2g_ext_batch_ref(c, ref, 0, 5, mat, (int8_t)o.q, (int8_t)o.e, (int8_t)o.q, (int8_t)o.e,
-                                  (int)idx.size(), ej.data(), tids.data(), tfl.data(), rq.data(), (int64_t)rq.size(),
-                                  er.data(), cg.data(), cap, &u)))
+                                  (int)idx.size(), ej.data(), tids.data(), tfl.data(), rq.data(), rq_len, er.data(),
+                                  cigar ? cigar + used : nullptr, cigar ? cigar_cap - used : 0, &u)))
       return rc;
+    c->rs_launches += 1 + ksw2g_batch_launches(c->scratch);
     for (size_t k = 0; k < idx.size(); ++k) {
       const int i = idx[k];
       ksw2g_rescue_result_t &R = res[i];
       const ksw2g_ext_result_t &E = er[k];
       R.ext_done = 1;
       R.ext = E;
-      R.ext.cigar_off = -1;
-      if (E.n_cigar > 0 && cigar) {
-        if (used + E.n_cigar > cigar_cap) return report_error(KSW2G_E_CAPACITY, "rescue: CIGAR buffer too small");
-        memcpy(cigar + used, cg.data() + E.cigar_off, sizeof(uint32_t) * (size_t)E.n_cigar);
-        R.ext.cigar_off = used;
-        used += E.n_cigar;
-      }
+      R.ext.cigar_off = E.n_cigar > 0 && cigar ? E.cigar_off + used : -1;
       if (E.n_cigar > 0 && E.max >= o.min_dp_max * o.a) {  // the hit of pe.c:291-304 and 361-368
         const int qe = ej[k].qlen, te = ej[k].tlen;
         int qs = qe - (E.reach_end ? qe : E.max_q + 1), qe2 = qe;
@@ -238,7 +248,16 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
         R.qs = qs, R.qe = qe2;
       }
     }
+    if (cigar) used += u;
   }
   if (cigar_used) *cigar_used = used;
+  c->rs_ms[2] = ms_since(t0);
+  return 0;
+}
+
+extern "C" int ksw2g_rescue_last_stats(const ksw2g_ctx_t *c, int *launches, double *ms) {
+  if (!c) return report_error(KSW2G_E_ARG, "rescue: null ctx");
+  if (launches) *launches = c->rs_launches;
+  if (ms) ms[0] = c->rs_ms[0], ms[1] = c->rs_ms[1], ms[2] = c->rs_ms[2];
   return 0;
 }

@@ -126,3 +126,69 @@ int synth_ll(const synth_ll_spec_t *sp, uint64_t seed, int n, int64_t *qoff, int
 	*qused = qo, *tused = to;
 	return 0;
 }
+
+/* Mate-rescue candidates over a decoded genome (codes 0..4, contigs back to
+ * back): an anchor hit, one orientation dir with insert bounds [lo, hi], the
+ * candidate window and read orientation as pe.c:330-339 computes them, and the
+ * mate read in the orientation pe.c aligns (a mutated copy of a stretch of the
+ * window, or random bases), methylation-converted for methylation modes. */
+typedef struct {
+	int qlen_lo, qlen_hi, lo, hi;
+	double p_random, p_meth, sub_rate, indel_rate;
+	int min_sc_hi;
+} synth_rescue_spec_t;
+
+typedef struct {
+	int64_t qoff, ts, te;
+	int32_t qlen, tid, meth, min_sc, rev, pad;
+} synth_rescue_job_t;
+
+int synth_rescue(const synth_rescue_spec_t *sp, uint64_t seed, const uint8_t *genome, int n_ctg,
+				 const uint64_t *ctg_off, const uint64_t *ctg_len, int n, synth_rescue_job_t *jobs, uint8_t *qbuf,
+				 int64_t qcap, int64_t *qused)
+{
+	uint64_t s = seed;
+	int64_t qo = 0;
+	uint8_t tmp[65536];
+	int i, k, tries = 0;
+	for (i = 0; i < n;) {
+		int t = ri(&s, 0, n_ctg - 1), l0 = ri(&s, sp->qlen_lo, sp->qlen_hi), L = ri(&s, sp->qlen_lo, sp->qlen_hi);
+		int h_rev = ri(&s, 0, 1), r0 = ri(&s, 0, 1), dir = ri(&s, 0, 3), is_rev, is_larger, mt0 = 0, mt;
+		int64_t clen = (int64_t)ctg_len[t], h_ts, pos5, ts, te;
+		if (++tries > 100 * (n + 16)) return -2;
+		if (clen < 3 * ((int64_t)sp->hi + 2 * sp->qlen_hi) || L > 32768) continue;
+		if (unif(&s) < sp->p_meth) mt0 = ri(&s, 1, 2);
+		h_ts = (int64_t)(sm64(&s) % (uint64_t)(clen - l0));
+		pos5 = h_rev ? h_ts + l0 : h_ts;
+		is_rev = ((dir >> 1) != (dir & 1)) ^ h_rev;
+		is_larger = (dir >> 1) != (dir & 1) ? (dir >> 1) ^ is_rev : (dir >> 1) ^ r0 ^ h_rev;
+		ts = (is_larger ? pos5 + sp->lo : pos5 - sp->hi) - (!is_rev ? 0 : L);
+		te = (is_larger ? pos5 + sp->hi : pos5 - sp->lo) + (!is_rev ? L : 0);
+		if (ts < 0) ts = 0;
+		if (te > clen) te = clen;
+		if (te - ts <= L) continue;
+		mt = mt0 == 0 ? 0 : is_rev ? 3 - mt0 : mt0;  /* l2b_meth_rev */
+		if (unif(&s) < sp->p_random) {
+			for (k = 0; k < L; ++k) tmp[k] = base(&s);
+		} else {
+			int64_t ms = ts + (int64_t)(sm64(&s) % (uint64_t)(te - ts - L + 1));
+			L = (int)mutate(&s, genome + ctg_off[t] + ms, L, tmp, sizeof tmp, sp->sub_rate, sp->indel_rate, 0.5, 3);
+			if (mt)
+				for (k = 0; k < L; ++k)
+					if (tmp[k] == (mt == 1 ? 1 : 2) && unif(&s) < 0.9) tmp[k] = mt == 1 ? 3 : 0;
+		}
+		/* the window follows the read's final length, as pe.c computes it from len */
+		ts = (is_larger ? pos5 + sp->lo : pos5 - sp->hi) - (!is_rev ? 0 : L);
+		te = (is_larger ? pos5 + sp->hi : pos5 - sp->lo) + (!is_rev ? L : 0);
+		if (ts < 0) ts = 0;
+		if (te > clen) te = clen;
+		if (te - ts <= L || L <= 0) continue;
+		if (qo + L > qcap) return -1;
+		memcpy(qbuf + qo, tmp, (size_t)L);
+		jobs[i].qoff = qo, jobs[i].ts = ts, jobs[i].te = te, jobs[i].qlen = L, jobs[i].tid = t;
+		jobs[i].meth = mt, jobs[i].min_sc = ri(&s, 0, sp->min_sc_hi), jobs[i].rev = is_rev, jobs[i].pad = 0;
+		qo += L, ++i;
+	}
+	*qused = qo;
+	return 0;
+}

@@ -120,6 +120,7 @@ def load_library():
                                         C.POINTER(vp)]),
         "ksw2g_ll_batch_ref": (i32, [vp, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp, u8p, i64, vp]),
         "ksw2g_rescue_batch": (i32, [vp, vp, vp, i32, vp, u8p, i64, vp, vp, i64, vp]),
+        "ksw2g_rescue_last_stats": (i32, [vp, vp, vp]),
         "ksw2g_graph_create": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
         "ksw2g_graph_launch": (i32, [vp, vp]),
         "ksw2g_graph_launches": (i32, [vp]),
@@ -430,6 +431,13 @@ class Reference:
         _check(self.L.ksw2g_rescue_batch(self.ctx.h, self.h, _ptr(opt), len(jobs), _ptr(jobs), _ptr(qbuf), len(qbuf),
                                          _ptr(res), _ptr(cig), cap, C.byref(used)))
         return res, cig[:used.value]
+
+    def rescue_stats(self):
+        """(kernel launches, [prefilter, ksw_ll, extz2] stage ms) of the context's last rescue call."""
+        n = C.c_int()
+        ms = (C.c_double * 3)()
+        _check(self.L.ksw2g_rescue_last_stats(self.ctx.h, C.byref(n), ms))
+        return n.value, list(ms)
 
     def close(self):
         if self.h:

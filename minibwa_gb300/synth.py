@@ -32,6 +32,12 @@ class ExtSpec(C.Structure):
                 ("junk_frac", C.c_double), ("junk_len", C.c_int)]
 
 
+class RescueSpec(C.Structure):
+    _fields_ = [("qlen_lo", C.c_int), ("qlen_hi", C.c_int), ("lo", C.c_int), ("hi", C.c_int),
+                ("p_random", C.c_double), ("p_meth", C.c_double), ("sub_rate", C.c_double),
+                ("indel_rate", C.c_double), ("min_sc_hi", C.c_int)]
+
+
 class LLSpec(C.Structure):
     _fields_ = [("qlen", C.c_int), ("tlen_lo", C.c_int), ("tlen_hi", C.c_int), ("plant_frac", C.c_double),
                 ("sub_rate", C.c_double), ("indel_rate", C.c_double), ("indel_p", C.c_double),
@@ -54,6 +60,9 @@ def _lib():
             f.restype = C.c_int
         _L.synth_ext.argtypes = [C.POINTER(ExtSpec), C.c_uint64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        _L.synth_rescue.restype = C.c_int
+        _L.synth_rescue.argtypes = [C.POINTER(RescueSpec), C.c_uint64, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                    C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
         _L.synth_ll.argtypes = [C.POINTER(LLSpec), C.c_uint64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
         del args
@@ -221,10 +230,19 @@ class Reference2b:
                 runs.append([int(st), en])
         self.ambi = np.array(runs, np.uint64).reshape(-1, 2)
         n_pac = (tot + 31) // 32
-        pac = np.zeros(n_pac * 32, np.uint64)
-        pac[:tot] = self.bases
-        pac = pac.reshape(n_pac, 32) << (2 * np.arange(32, dtype=np.uint64))
-        self.pac = np.bitwise_or.reduce(pac, axis=1).astype(np.uint64)
+        b = np.zeros(n_pac * 32, np.uint8)
+        b[:tot] = self.bases
+        b = b.reshape(n_pac, 32)
+        self.pac = np.zeros(n_pac, np.uint64)
+        for k in range(32):
+            self.pac |= b[:, k].astype(np.uint64) << np.uint64(2 * k)
+
+    def decoded(self):
+        """All contigs as codes 0..4 (N runs applied)."""
+        g = self.bases.copy()
+        for s0, e0 in self.ambi:
+            g[int(s0):int(e0)] = 4
+        return g
 
     def window(self, tid, st, length, flags=0):
         """The decoded window, computed here with numpy (an independent cross-check)."""
@@ -382,3 +400,28 @@ def _mutate(rng, m, sub, indel):
         out.append(int(m[i]))
         i += 1
     return np.array(out, np.uint8)
+
+
+RESCUE_SPEC = dict(qlen_lo=100, qlen_hi=250, lo=50, hi=800, p_random=0.2, p_meth=0.0, sub_rate=0.02,
+                   indel_rate=0.005, min_sc_hi=40)
+
+
+def rescue_workload(n, ctg_len=(40_000_000, 25_000_000, 15_000_000), spec=None, seed=SEED + 60, ref=None):
+    """n mate-rescue candidates (the C generator) over a Reference2b of the given contigs:
+    anchors uniform on the contigs, insert bounds [50, 800] (minibwa's pe_lo / pe_hi), reads of
+    100-250 nt with 2% substitutions and 0.5% indels, 20% unrelated reads.
+    Returns (reference, RESCUE_JOB array, read buffer)."""
+    sp = RescueSpec(**{**RESCUE_SPEC, **(spec or {})})
+    if ref is None:
+        ref = Reference2b(list(ctg_len), n_runs=200, run_max=500, seed=seed, n_repeats=2000)
+    g = ref.decoded()
+    jobs = np.zeros(n, RESCUE_JOB)
+    qbuf = np.zeros(int(n) * (sp.qlen_hi * 2 + 8) + 64, np.uint8)
+    used = C.c_int64()
+    off = np.ascontiguousarray(ref.ctg_off, np.uint64)
+    ln = np.ascontiguousarray(ref.ctg_len, np.uint64)
+    rc = _lib().synth_rescue(C.byref(sp), seed, g.ctypes.data, len(off), off.ctypes.data, ln.ctypes.data, int(n),
+                             jobs.ctypes.data, qbuf.ctypes.data, len(qbuf), C.byref(used))
+    if rc != 0:
+        raise RuntimeError(f"synth_rescue failed ({rc})")
+    return ref, jobs, qbuf[:used.value].copy()

@@ -101,6 +101,34 @@ void orc_l2b_getseq(const uint64_t *pac, const uint64_t *ctg_off, int64_t n_ambi
 int orc_ungap(int qlen, const uint8_t *qseq, int tlen, const uint8_t *tseq, int kmer, int mt, int *max_i,
 			  int *n_good, int *n_kmer);
 
+/* Mate rescue (rescue_cpu.c); layouts of ksw2g_rescue_opt_t / _job_t / _result_t. */
+typedef struct {
+	int32_t a, b, b_ts, b_ambi, q, e;
+	int32_t bw, zdrop, end_bonus, min_len, min_dp_max;
+} orc_rescue_opt_t;
+typedef struct {
+	int64_t qoff, ts, te;
+	int32_t qlen, tid, meth, min_sc, rev, pad;
+} orc_rescue_job_t;
+typedef struct {
+	int32_t max_ug, max_i, n_good, n_kmer;
+	int64_t ts2, te2;
+	int32_t ll_done, ll_score, ll_te, ll_qe, ll_score2, ll_te2;
+	int32_t ext_done, rescued;
+	int32_t qs, qe, dp_max2, pad;
+	int64_t ts, te;
+	struct {
+		int32_t score, max, max_q, max_t, mqe, mqe_t, mte, mte_q;
+		int32_t zdropped, reach_end, n_cigar, n_diag;
+		int64_t cigar_off, cells;
+	} ext;
+} orc_rescue_res_t;
+/* Rescue of n candidates over nthreads threads; CIGARs at res[i].ext.cigar_off in
+ * cigar (qlen + te - ts + 1 words reserved per candidate).  Returns the words
+ * reserved, or -1 if cigar_cap is too small. */
+int64_t orc_rescue_batch(const orc_rescue_opt_t *o, int n, const orc_rescue_job_t *jobs, const uint8_t *qbuf,
+						 const uint64_t *pac, const uint64_t *ctg_off, int64_t n_ambi, const uint64_t *ambi,
+						 orc_rescue_res_t *res, uint32_t *cigar, int64_t cigar_cap, int nthreads);
 #ifdef __cplusplus
 }
 #endif

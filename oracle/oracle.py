@@ -26,6 +26,17 @@ ORC_RES = np.dtype([("score", "<i4"), ("max", "<i4"), ("max_q", "<i4"), ("max_t"
                     ("mqe", "<i4"), ("mqe_t", "<i4"), ("mte", "<i4"), ("mte_q", "<i4"),
                     ("zdropped", "<i4"), ("reach_end", "<i4"), ("n_cigar", "<i4"), ("n_diag", "<i4"),
                     ("cigar_off", "<i8")])
+ORC_RESCUE_JOB = np.dtype([("qoff", "<i8"), ("ts", "<i8"), ("te", "<i8"), ("qlen", "<i4"), ("tid", "<i4"),
+                           ("meth", "<i4"), ("min_sc", "<i4"), ("rev", "<i4"), ("pad", "<i4")])
+ORC_RESCUE_RES = np.dtype([("max_ug", "<i4"), ("max_i", "<i4"), ("n_good", "<i4"), ("n_kmer", "<i4"),
+                           ("ts2", "<i8"), ("te2", "<i8"),
+                           ("ll_done", "<i4"), ("ll_score", "<i4"), ("ll_te", "<i4"), ("ll_qe", "<i4"),
+                           ("ll_score2", "<i4"), ("ll_te2", "<i4"), ("ext_done", "<i4"), ("rescued", "<i4"),
+                           ("qs", "<i4"), ("qe", "<i4"), ("dp_max2", "<i4"), ("pad", "<i4"),
+                           ("ts", "<i8"), ("te", "<i8"),
+                           ("ext", [(k, "<i4") for k in ("score", "max", "max_q", "max_t", "mqe", "mqe_t", "mte",
+                                                          "mte_q", "zdropped", "reach_end", "n_cigar", "n_diag")]
+                            + [("cigar_off", "<i8"), ("cells", "<i8")])])
 ORC_LLRES = np.dtype([("score", "<i4"), ("te", "<i4"), ("qe", "<i4"), ("score2", "<i4"), ("te2", "<i4")])
 
 
@@ -94,6 +105,8 @@ def _load(path, prefix):
         L.orc_l2b_getseq.restype = None
         L.orc_l2b_getseq.argtypes = [vp, vp, i64, vp, i64, i64, i64, i32, vp]
         L.orc_ungap.restype = i32
+        L.orc_rescue_batch.restype = i64
+        L.orc_rescue_batch.argtypes = [vp, i32, vp, vp, vp, vp, i64, vp, vp, vp, i64, i32]
         L.orc_ungap.argtypes = [i32, vp, i32, vp, i32, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
     _libs[path] = L
     return L
@@ -372,3 +385,23 @@ def rescue(ref, opt, tid, ts, te, query, meth, min_sc, rev):
             qs, qe2 = qlen - qe2, qlen - qs
         out.update(rescued=1, ts=hts, te=ts2 + te_, qs=qs, qe=qe2, dp_max2=max(d2, 0))
     return out
+
+
+def rescue_batch(ref, opt, jobs, qbuf, nthreads=1):
+    """The C restatement of the rescue (rescue_cpu.c) over a batch of candidates on nthreads
+    threads; returns (results in the ksw2g_rescue_result_t layout, CIGAR words)."""
+    L = oracle_lib()
+    o = np.array([opt[k] for k in RESCUE_SC], np.int32)
+    jobs = np.ascontiguousarray(jobs).view(ORC_RESCUE_JOB) if len(jobs) else np.zeros(0, ORC_RESCUE_JOB)
+    res = np.zeros(len(jobs), ORC_RESCUE_RES)
+    cap = int((jobs["qlen"].astype(np.int64) + jobs["te"] - jobs["ts"] + 1).sum()) + 1
+    cig = np.zeros(cap, np.uint32)
+    amb = np.ascontiguousarray(ref.ambi, np.uint64).reshape(-1)
+    q = np.ascontiguousarray(qbuf, np.uint8)
+    pac = np.ascontiguousarray(ref.pac, np.uint64)
+    off = np.ascontiguousarray(ref.ctg_off, np.uint64)
+    rc = L.orc_rescue_batch(_p(o), len(jobs), _p(jobs), _p(q), _p(pac), _p(off), len(amb) // 2,
+                            _p(amb) if len(amb) else None, _p(res), _p(cig), cap, int(nthreads))
+    if rc < 0:
+        raise RuntimeError("CIGAR buffer too small")
+    return res, cig
