@@ -80,3 +80,36 @@ def compare_ll(gres, ores):
     for f in LL_FIELDS:
         bad = np.nonzero(gres[f] != ores[f])[0]
         assert len(bad) == 0, f"ll field {f}: {len(bad)} differ, first {bad[0]}: gpu {gres[f][bad[0]]} vs {ores[f][bad[0]]}"
+
+
+TRACE = os.path.join(ROOT, "tests", "golden", "minibwa_trace.npz")
+TRACE_OUT = ["max", "zdropped", "max_q", "max_t", "mqe", "mqe_t", "mte", "mte_q", "score", "m_cigar", "n_cigar",
+             "reach_end"]
+
+
+@pytest.fixture(scope="session")
+def trace():
+    return dict(np.load(TRACE))
+
+
+def trace_ext_calls(g):
+    """The extension calls the reference's minibwa issued (tests/golden/make_trace.py)."""
+    for i in range(len(g["ext_kind"])):
+        qlen, tlen, m, q, e, q2, e2, w, zdrop, eb, flag, m0 = [int(x) for x in g["ext_hdr"][i]]
+        yield dict(dual=int(g["ext_kind"][i]) == 2, m=m, q=q, e=e, q2=q2, e2=e2, w=w, zdrop=zdrop, end_bonus=eb,
+                   flag=flag, m_cigar_in=m0,
+                   mat=g["ext_mat"][g["ext_matoff"][i]:g["ext_matoff"][i + 1]].view(np.int8).copy(),
+                   query=g["ext_q"][g["ext_qoff"][i]:g["ext_qoff"][i + 1]],
+                   target=g["ext_t"][g["ext_toff"][i]:g["ext_toff"][i + 1]],
+                   out=dict(zip(TRACE_OUT, [int(x) for x in g["ext_out"][i]])),
+                   cigar=[int(x) for x in g["ext_cigar"][g["ext_cigoff"][i]:g["ext_cigoff"][i + 1]]])
+
+
+def trace_ll_calls(g):
+    for i in range(len(g["ll_kind"])):
+        size, qlen, m, tlen, gapo, gape, xtra = [int(x) for x in g["ll_hdr"][i]]
+        yield dict(kind=int(g["ll_kind"][i]), size=size, m=m, gapo=gapo, gape=gape, xtra=xtra,
+                   mat=g["ll_mat"][g["ll_matoff"][i]:g["ll_matoff"][i + 1]].view(np.int8).copy(),
+                   query=g["ll_q"][g["ll_qoff"][i]:g["ll_qoff"][i + 1]],
+                   target=g["ll_t"][g["ll_toff"][i]:g["ll_toff"][i + 1]],
+                   out=dict(zip(LL_FIELDS, [int(x) for x in g["ll_out"][i]])))
