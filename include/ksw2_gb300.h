@@ -138,6 +138,26 @@ int ksw2g_ll_batch_ref(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int size, int m
 					   int gape, int n_jobs, const ksw2g_ll_job_t *jobs, const int32_t *tid, const int32_t *tflags,
 					   const uint8_t *qbuf, int64_t qbuf_len, ksw2g_ll_result_t *res);
 
+/* ---- align.c's pair alignment (mb_align_pair, align.c:329-390) over a batch ----
+ * Every left extension, chain gap fill and right extension mb_align1 issues goes
+ * through mb_align_pair: the ungapped shortcuts, the band shrink of short pairs,
+ * the DP memory cap, then ksw_extz2_sse (q == q2 and e == e2) or ksw_extd2_sse.
+ * ksw2g_align_pairs applies the shortcuts on the host and runs the pairs that need
+ * DP as one batch; each result equals mb_align_pair's ksw_extz_t (n_diag and cells
+ * are 0 for pairs settled without DP).  jobs[k].zdrop is mb_align_pair's zdrop
+ * argument (scaled by a here, as there) and jobs[k].flag its ksw_flag; mat is
+ * ksw_gen_nt4_mat's 5x5 matrix. */
+typedef struct {
+	int32_t a, b, b_ts, b_ambi, q, e, q2, e2;  /* mb_opt_t scores */
+	int32_t meth, pad;                         /* opt->flag & MB_F_METH */
+	int64_t max_sw_mat;                        /* opt->max_sw_mat (0: no cap) */
+} ksw2g_align_opt_t;
+
+int ksw2g_align_pairs(ksw2g_ctx_t *ctx, const ksw2g_align_opt_t *opt, const int8_t *mat, int n_jobs,
+					  const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+					  int64_t tbuf_len, ksw2g_ext_result_t *res, uint32_t *cigar, int64_t cigar_cap,
+					  int64_t *cigar_used);
+
 /* ---- mate rescue over the resident reference (pe.c:209-372) ----
  * One candidate is one (read, window) pair of mb_matesw_core: the window
  * [ts, te) on contig tid computed from the insert-size statistics and clamped

@@ -59,6 +59,7 @@ def build(verbose=False, force=False):
         ("graph.cu", "graph.o", []),
         ("ref.cu", "ref.o", []),
         ("rescue.cu", "rescue.o", []),
+        ("align_pairs.cu", "align_pairs.o", []),
     ]
     hdrs = _headers()
     procs, objs = [], []

@@ -35,6 +35,8 @@ LL_JOB = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "
 LL_RESULT = np.dtype([("score", "<i4"), ("te", "<i4"), ("qe", "<i4"), ("score2", "<i4"),
                       ("te2", "<i4"), ("rows", "<i4")])
 assert EXT_JOB.itemsize == 40 and EXT_RESULT.itemsize == 64 and LL_JOB.itemsize == 32 and LL_RESULT.itemsize == 24
+ALIGN_OPT = np.dtype([(k, "<i4") for k in ("a", "b", "b_ts", "b_ambi", "q", "e", "q2", "e2", "meth", "pad")]
+                     + [("max_sw_mat", "<i8")])
 RESCUE_OPT = np.dtype([(k, "<i4") for k in ("a", "b", "b_ts", "b_ambi", "q", "e", "bw", "zdrop", "end_bonus",
                                             "min_len", "min_dp_max")])
 RESCUE_JOB = np.dtype([("qoff", "<i8"), ("ts", "<i8"), ("te", "<i8"), ("qlen", "<i4"), ("tid", "<i4"),
@@ -121,6 +123,7 @@ def load_library():
         "ksw2g_ll_batch_ref": (i32, [vp, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp, u8p, i64, vp]),
         "ksw2g_rescue_batch": (i32, [vp, vp, vp, i32, vp, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_rescue_last_stats": (i32, [vp, vp, vp]),
+        "ksw2g_align_pairs": (i32, [vp, vp, vp, i32, vp, u8p, i64, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_graph_create": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
         "ksw2g_graph_launch": (i32, [vp, vp]),
         "ksw2g_graph_launches": (i32, [vp]),
@@ -282,6 +285,25 @@ class Context:
         used = C.c_int64()
         _check(self.L.ksw2g_ext_batch(self.h, int(dual), m, _ptr(mat), q, e, q2, e2, n, _ptr(jobs), _ptr(qbuf),
                                       len(qbuf), _ptr(tbuf), len(tbuf), _ptr(res), _ptr(cig), cap, C.byref(used)))
+        return res, cig[:used.value]
+
+    def align_pairs(self, opt, mat, jobs, qbuf, tbuf):
+        """align.c's mb_align_pair over a batch (ksw2g_align_pairs): opt is a dict or ALIGN_OPT
+        record; returns (results, cigar words)."""
+        if isinstance(opt, dict):
+            o = np.zeros(1, ALIGN_OPT)
+            for k, v in opt.items():
+                o[k] = v
+            opt = o
+        opt = np.ascontiguousarray(opt, ALIGN_OPT)
+        jobs = np.ascontiguousarray(jobs, EXT_JOB)
+        qbuf, tbuf, mat = _u8(qbuf), _u8(tbuf), np.ascontiguousarray(mat, np.int8)
+        res = np.zeros(len(jobs), EXT_RESULT)
+        cap = int(((jobs["qlen"].astype(np.int64) + jobs["tlen"] + 1)).sum()) + 16
+        cig = np.zeros(cap, np.uint32)
+        used = C.c_int64()
+        _check(self.L.ksw2g_align_pairs(self.h, _ptr(opt), _ptr(mat), len(jobs), _ptr(jobs), _ptr(qbuf), len(qbuf),
+                                        _ptr(tbuf), len(tbuf), _ptr(res), _ptr(cig), cap, C.byref(used)))
         return res, cig[:used.value]
 
     def ll_batch(self, size, m, mat, gapo, gape, jobs, qbuf, tbuf):

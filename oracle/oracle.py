@@ -405,3 +405,85 @@ def rescue_batch(ref, opt, jobs, qbuf, nthreads=1):
     if rc < 0:
         raise RuntimeError("CIGAR buffer too small")
     return res, cig
+
+
+ALIGN_SC = ("a", "b", "b_ts", "b_ambi", "q", "e", "q2", "e2", "meth")
+ALIGN_OUT = ("max", "zdropped", "max_q", "max_t", "mqe", "mqe_t", "mte", "mte_q", "score", "n_cigar", "reach_end")
+
+
+def ref_align_pair(opt, mat, query, target, w, end_bonus, zdrop, flag):
+    """The reference's own mb_align_pair (align.c:329-390) through _ref/libmbpe.so."""
+    L = refpe_lib()
+    if not hasattr(L, "_refal"):
+        L.refal_align_pair.restype = C.c_int
+        L.refal_align_pair.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        L._refal = True
+    sc = np.array([int(opt[k]) for k in ALIGN_SC], np.int32)
+    q = np.ascontiguousarray(query, np.uint8)
+    t = np.ascontiguousarray(target, np.uint8)
+    m = np.ascontiguousarray(mat, np.int8)
+    out = np.zeros(11, np.int32)
+    cig = np.zeros(len(q) + len(t) + 8, np.uint32)
+    rc = L.refal_align_pair(_p(sc), int(opt.get("max_sw_mat", 0)), len(q), _p(q) if len(q) else None, len(t),
+                            _p(t) if len(t) else None, _p(m), w, end_bonus, zdrop, flag, _p(out), _p(cig), len(cig))
+    if rc:
+        raise RuntimeError("CIGAR buffer too small")
+    d = {k: int(v) for k, v in zip(ALIGN_OUT, out)}
+    d["cigar"] = [int(x) for x in cig[:d["n_cigar"]]]
+    return d
+
+
+def align_pair(opt, mat, query, target, w, end_bonus, zdrop, flag):
+    """mb_align_pair (align.c:329-390) restated over the oracle's extz2/extd2: the ungapped
+    shortcuts, the band shrink of short pairs, the memory cap, then the DP call."""
+    a, b, b_ts, q, e, q2, e2 = (int(opt[k]) for k in ("a", "b", "b_ts", "q", "e", "q2", "e2"))
+    qs = np.ascontiguousarray(query, np.uint8)
+    ts = np.ascontiguousarray(target, np.uint8)
+    mat = np.ascontiguousarray(mat, np.int8)
+    qlen, tlen = len(qs), len(ts)
+    if (b_ts != 0 and b != b_ts) or opt.get("meth", 0):
+        flag |= 0x04
+    neg = -0x40000000
+    reset = dict(max=0, zdropped=0, max_q=-1, max_t=-1, mqe=neg, mqe_t=-1, mte=neg, mte_q=-1, score=neg, n_cigar=0,
+                 reach_end=0, cigar=[])
+    n_mm = -1
+    if (flag & 0x40) and tlen >= qlen:
+        r = dict(reset)
+        score = mx = 0
+        for j in range(qlen):
+            s = int(mat[ts[j] * 5 + qs[j]])
+            score += s
+            n_mm += int(ts[j] > 3 or qs[j] > 3 or s < 0)
+            if mx < score:
+                mx, r["max_q"], r["max_t"] = score, j, j
+        r["score"], r["max"] = score, mx
+        if n_mm <= 2:
+            r["mqe"], r["mqe_t"] = score, qlen - 1
+            if r["mqe"] + end_bonus >= r["max"]:
+                r.update(reach_end=1, n_cigar=1, cigar=[qlen << 4])
+                return r
+    elif qlen == tlen and not (flag & 0x40):
+        r = dict(reset)
+        score = 0
+        for j in range(qlen):
+            s = int(mat[ts[j] * 5 + qs[j]])
+            score += s
+            n_mm += int(ts[j] > 3 or qs[j] > 3 or s < 0)
+        r["score"] = score
+        if n_mm <= 3 or score > (qlen - 2) * a - 2 * (q + e):
+            r.update(n_cigar=1, cigar=[qlen << 4])
+            return r
+    if n_mm >= 0 and min(qlen, tlen) < 100:
+        x = n_mm * (a + b)
+        max1 = (x - q + e - 1) // e if x >= q + e else 0
+        max2 = (x - q2 + e2 - 1) // e2 if x >= q2 + e2 else 0
+        w = min(w, max(max1, max2) + 4)
+    msm = int(opt.get("max_sw_mat", 0))
+    if msm > 0 and tlen * qlen > msm:
+        r = dict(reset)
+        r["zdropped"] = 1
+        return r
+    dual = not (q == q2 and e == e2)
+    ez, _ = extz(int(dual), qs, ts, 5, mat, q, e, q2, e2, w, zdrop * a, end_bonus, flag)
+    return {k: ez[k] for k in ALIGN_OUT + ("cigar",)}
