@@ -118,6 +118,8 @@ extern "C" void ksw2g_ctx_destroy(ksw2g_ctx_t *c) {
   c->one.release();
   c->one_h.release();
   for (DevBuf *d : {&c->rs_q, &c->rs_t, &c->rs_meta, &c->rs_res, &c->rs_hist}) d->release();
+  for (ksw2g_batch *b : c->rs_ll)
+    if (b) ksw2g_batch_free(b);
   c->rs_h.release();
   cudaStreamDestroy(c->st);
   delete c;
@@ -934,8 +936,19 @@ int ll_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int size, int m, const int8_t 
   std::vector<int64_t> qpad, tpad;
   int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad, rt);
   if (rc) return rc;
+  // Jobs in the device table by segment count, longest first (counting sort, stable): the
+  // groups of a warp then run queries of similar length side by side, so the segments
+  // one group skips are not computed for another, and the longest jobs start first.
   std::vector<ksw2g_ll_job> dj(n);
-  for (int i = 0; i < n; ++i) dj[i] = ksw2g_ll_job{qpad[i], tpad[i], jobs[i].qlen, jobs[i].tlen, jobs[i].xtra, 0};
+  {
+    std::vector<int32_t> cnt((size_t)slen + 2, 0);
+    auto key = [&](int i) { return slen - (jobs[i].qlen + lanes - 1) / lanes; };
+    for (int i = 0; i < n; ++i) ++cnt[(size_t)key(i)];
+    int32_t acc = 0;
+    for (auto &x : cnt) { const int32_t t = x; x = acc; acc += t; }
+    for (int i = 0; i < n; ++i)
+      dj[cnt[(size_t)key(i)]++] = ksw2g_ll_job{qpad[i], tpad[i], jobs[i].qlen, jobs[i].tlen, jobs[i].xtra, i};
+  }
   if ((rc = b->jobs.ensure(sizeof(ksw2g_ll_job) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->res.ensure(sizeof(ksw2g_ll_result) * (size_t)std::max(n, 1)))) return rc;
   if ((rc = b->counters.ensure(16))) return rc;
@@ -1054,7 +1067,7 @@ static ksw_llrst_t ll_one(void *q_, int tlen, const uint8_t *target, int gapo, i
   }
   uint8_t *hb = (uint8_t *)c->one_h.p, *d = (uint8_t *)c->one.p;
   memset(hb, 0, o_arena);
-  ksw2g_ll_job J{32, slot_bytes(qlen) + 32, qlen, tlen, xtra, 0};
+  ksw2g_ll_job J{32, slot_bytes(qlen) + 32, qlen, tlen, xtra, 0};  // slot 0: the one result
   memcpy(hb + o_job, &J, sizeof J);
   memcpy(hb + o_mat, (uint8_t *)(h + 1), (size_t)m * m);
   memset(hb + o_arena, 0, arena_bytes);

@@ -83,8 +83,14 @@ __device__ __forceinline__ uint32_t ld_tw(const uint8_t *tp, int p, int tlen) {
 #ifndef KSW2G_EXT_MINB4
 #define KSW2G_EXT_MINB4 4  // resident blocks per SM asked of shapes with K <= 4
 #endif
+// resident blocks per SM asked of a shape: two-word shapes fit five (extd2) or six (extz2)
+// blocks of 128 threads without spilling
+template <int VAR, int K>
+constexpr int ext_min_blocks() {
+  return K <= 2 ? (VAR ? 5 : 6) : K <= 4 ? KSW2G_EXT_MINB4 : K <= 5 ? 3 : 2;
+}
 template <int VAR, int MODE, int G, int K>
-__global__ void __launch_bounds__(128, (K <= 4 ? KSW2G_EXT_MINB4 : (K <= 5 ? 3 : 2)))
+__global__ void __launch_bounds__(128, ext_min_blocks<VAR, K>())
 ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ order, int n_jobs,
               const uint8_t *__restrict__ arena, const ksw2g_ext_params P, ksw2g_ext_result *__restrict__ res,
               ksw2g_bt *__restrict__ bts, uint8_t *__restrict__ tb_pool, const int64_t *__restrict__ tb_off,

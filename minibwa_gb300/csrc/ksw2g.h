@@ -55,10 +55,12 @@ struct ksw2g_ext_params {
   int8_t mat[256];              // m*m scores (m <= 16 for GENERIC_SC on device)
 };
 
+// The device table may list jobs in any order: `slot` is the job's index in the
+// results and the second-best lists (the host orders the table by query length).
 struct ksw2g_ll_job {
   int64_t qoff, toff;
   int32_t qlen, tlen;
-  int32_t xtra, pad;
+  int32_t xtra, slot;
 };
 
 struct ksw2g_ll_result {

@@ -80,6 +80,7 @@ ll_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__re
       if (active) {
         jid = j;
         const ksw2g_ll_job J = jobs[jid];
+        jid = J.slot;
         qlen = J.qlen, tlen = J.tlen, xtra = J.xtra;
         slen = (qlen + LANES - 1) / LANES;
         tp = arena + J.toff;
@@ -268,6 +269,7 @@ ll_wide_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t 
       if (active) {
         jid = j;
         const ksw2g_ll_job J = jobs[jid];
+        jid = J.slot;
         qlen = J.qlen, tlen = J.tlen, xtra = J.xtra;
         slen = (qlen + LANES - 1) / LANES;
         tp = arena + J.toff;
@@ -481,6 +483,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
       if (active) {
         jid = j;
         const ksw2g_ll_job J = jobs[jid];
+        jid = J.slot;
         qlen = J.qlen, tlen = J.tlen, xtra = J.xtra;
         slen = (qlen + LANES - 1) / LANES;
         tp = arena + J.toff;
@@ -543,19 +546,39 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
           f = __viaddmax_s16x2(f, NGE, tt);
         }
       }
-      bool fin = false;  // lazy-F (ksw2_ll_sse.c:175-185 / 287-297)
+      // lazy-F (ksw2_ll_sse.c:175-185 / 287-297): the reference stops after the first segment
+      // at which f <= H - gapoe holds in every lane.  Segments go in chunks of four: each
+      // chunk's candidate H values and exit tests are computed, one group-wide AND of the
+      // tests finds the first exiting segment, and H is kept only up to it.
+      bool fin = false;
       for (int kk = 0; kk < 16 && !fin; ++kk) {
         const uint32_t fu = __shfl_up_sync(gm, f, 1, T), fw = __shfl_sync(gm, f, T - 1, T);
         f = t ? fu : (fw << 16);
 #pragma unroll
-        for (int s = 0; s < SLEN; ++s) {
-          if (s < slen && !fin) {
-            const uint32_t hv = __vmaxs2(H[s], f);
-            H[s] = hv;
-            if (s == slen - 1) hl = hv;
-            const uint32_t hh = __viaddmax_s16x2(hv, NGOE, 0u);
-            f = __viaddmax_s16x2(f, NGE, 0u);
-            fin = __all_sync(gm, (__vmaxs2(f, hh) ^ hh) == 0u);  // f <= hh in every lane
+        for (int c = 0; c < SLEN; c += 4) {
+          if (c < slen && !fin) {
+            uint32_t nh[4];
+            unsigned ok = 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              nh[u] = 0;
+              if (c + u < SLEN && c + u < slen) {
+                nh[u] = __vmaxs2(H[c + u], f);
+                const uint32_t hh = __viaddmax_s16x2(nh[u], NGOE, 0u);
+                f = __viaddmax_s16x2(f, NGE, 0u);
+                if ((__vmaxs2(f, hh) ^ hh) == 0u) ok |= 1u << u;  // f <= hh in this thread's lanes
+              }
+            }
+            const unsigned all = __reduce_and_sync(gm, ok);
+            const int last = all ? __ffs(all) - 1 : 3;  // the last segment of the chunk that is kept
+            fin = all != 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              if (c + u < SLEN && c + u < slen && u <= last) {
+                H[c + u] = nh[u];
+                if (c + u == slen - 1) hl = nh[u];
+              }
+            }
           }
         }
       }

@@ -160,34 +160,54 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     if (max_sc >= 32767) continue;  // mb_matesw_align returns before ksw_ll
     ll_size[i] = max_sc < 255 - b_mm ? 1 : 2;
   }
+  // one batch per (size, methylation mode); all are prepared, then run on the context's two
+  // streams at once, the largest alone on the first, so the few i16 jobs overlap the u8 ones
+  struct LLGroup {
+    int slot, size;
+    std::vector<int> idx;
+  };
+  std::vector<LLGroup> groups;
   for (int size = 1; size <= 2; ++size)
     for (int mt = 0; mt <= 2; ++mt) {
-      std::vector<int> idx;
+      LLGroup g{(size - 1) * 3 + mt, size, {}};
       for (int i = 0; i < n; ++i)
-        if (ll_size[i] == size && jobs[i].meth == mt) idx.push_back(i);
-      if (idx.empty()) continue;
+        if (ll_size[i] == size && jobs[i].meth == mt) g.idx.push_back(i);
+      if (g.idx.empty()) continue;
       int8_t mat[25];
       gen_nt4(mat, 1, (int8_t)b_mm, (int8_t)b_ts, (int8_t)b_ambi, mt);
-      std::vector<ksw2g_ll_job_t> lj(idx.size());
-      std::vector<int32_t> tids(idx.size());
-      for (size_t k = 0; k < idx.size(); ++k) {
-        const int i = idx[k];
+      std::vector<ksw2g_ll_job_t> lj(g.idx.size());
+      std::vector<int32_t> tids(g.idx.size());
+      for (size_t k = 0; k < g.idx.size(); ++k) {
+        const int i = g.idx[k];
         lj[k] = ksw2g_ll_job_t{jobs[i].qoff, res[i].ts2, jobs[i].qlen, (int32_t)(res[i].te2 - res[i].ts2),
                                KSW_LL_SUBO | o.min_len, 0};
         tids[k] = jobs[i].tid;
       }
-      std::vector<ksw2g_ll_result_t> lr(idx.size());
-      if ((rc = ksw2g_ll_batch_ref(c, ref, size, 5, mat, gapo, gape, (int)idx.size(), lj.data(), tids.data(),
-                                   nullptr, qbuf, qbuf_len, lr.data())))
-        return rc;
-      c->rs_launches += 1 + ksw2g_batch_launches(c->scratch);  // the window gather, then the DP
-      for (size_t k = 0; k < idx.size(); ++k) {
-        ksw2g_rescue_result_t &R = res[idx[k]];
-        R.ll_done = 1, R.ll_score = lr[k].score, R.ll_te = lr[k].te, R.ll_qe = lr[k].qe;
-        R.ll_score2 = lr[k].score2, R.ll_te2 = lr[k].te2;
-      }
+      if (!c->rs_ll[g.slot]) c->rs_ll[g.slot] = new ksw2g_batch;
+      const SeqSeg seg{lj.data(), (int)lj.size(), qbuf, qbuf_len, nullptr, 0};
+      const RefTargets rt{ref, tids.data(), nullptr};
+      if ((rc = ll_prepare_segs(c, c->rs_ll[g.slot], size, 5, mat, gapo, gape, 1, &seg, &rt))) return rc;
+      groups.push_back(std::move(g));
     }
-
+  if (groups.size() > 1 && !c->aux && cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking) != cudaSuccess)
+    return report_error(KSW2G_E_CUDA, "rescue: stream creation failed");
+  std::sort(groups.begin(), groups.end(), [](const LLGroup &x, const LLGroup &y) { return x.idx.size() > y.idx.size(); });
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    ksw2g_batch *b = c->rs_ll[groups[gi].slot];
+    if ((rc = ll_run_on(b, gi == 0 ? c->st : c->aux))) return rc;
+    c->rs_launches += 1 + b->launches;  // the window gather, then the DP
+  }
+  if (groups.size() > 1 && cudaStreamSynchronize(c->aux) != cudaSuccess)
+    return report_error(KSW2G_E_CUDA, "rescue: ksw_ll failed");
+  for (const LLGroup &g : groups) {
+    std::vector<ksw2g_ll_result_t> lr(g.idx.size());
+    if ((rc = ksw2g_ll_fetch(c, c->rs_ll[g.slot], lr.data()))) return rc;
+    for (size_t k = 0; k < g.idx.size(); ++k) {
+      ksw2g_rescue_result_t &R = res[g.idx[k]];
+      R.ll_done = 1, R.ll_score = lr[k].score, R.ll_te = lr[k].te, R.ll_qe = lr[k].qe;
+      R.ll_score2 = lr[k].score2, R.ll_te2 = lr[k].te2;
+    }
+  }
   c->rs_ms[1] = ms_since(t0);
   t0 = std::chrono::steady_clock::now();
   // ---- stage 3: extz2 on the reversed prefixes ending at ksw_ll's end (pe.c:283-300)

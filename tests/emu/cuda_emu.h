@@ -152,28 +152,31 @@ inline unsigned __ballot_sync(unsigned mask, int pred) {
   return r;
 }
 // __reduce_*_sync over the lanes named in mask (sm_80+ warp reductions)
-inline uint64_t emu_reduce(unsigned mask, uint64_t v, int op) {  // op 0: max s32, 1: min u32, 2: add u32, 3: max u32
+inline uint64_t emu_reduce(unsigned mask, uint64_t v, int op) {  // op 0: max s32, 1: min u32, 2: add u32, 3: max u32, 4: and
   emu::Barrier &b = emu::enter(mask);
   b.slot[emu::lane()] = v;
   b.arrive();
   mask &= emu::warp().present;
   int64_t smax = INT64_MIN;
-  uint64_t umin = UINT64_MAX, umax = 0, sum = 0;
+  uint64_t umin = UINT64_MAX, umax = 0, sum = 0, band = 0xffffffffu;
   for (int i = 0; i < 32; ++i)
     if ((mask >> i) & 1) {
       const uint32_t x = (uint32_t)b.slot[i];
+      band &= x;
       smax = std::max<int64_t>(smax, (int32_t)x);
       umin = std::min<uint64_t>(umin, x);
       umax = std::max<uint64_t>(umax, x);
       sum += x;
     }
   b.arrive();
-  return op == 0 ? (uint64_t)(uint32_t)(int32_t)smax : op == 1 ? umin : op == 2 ? (uint32_t)sum : umax;
+  return op == 0 ? (uint64_t)(uint32_t)(int32_t)smax : op == 1 ? umin : op == 2 ? (uint32_t)sum : op == 3 ? umax : band;
 }
 inline int __reduce_max_sync(unsigned mask, int v) { return (int)(uint32_t)emu_reduce(mask, (uint32_t)v, 0); }
 inline unsigned __reduce_min_sync(unsigned mask, unsigned v) { return (unsigned)emu_reduce(mask, v, 1); }
 inline unsigned __reduce_add_sync(unsigned mask, unsigned v) { return (unsigned)emu_reduce(mask, v, 2); }
 inline unsigned __reduce_max_sync(unsigned mask, unsigned v) { return (unsigned)emu_reduce(mask, v, 3); }
+inline unsigned __reduce_and_sync(unsigned mask, unsigned v) { return (unsigned)emu_reduce(mask, v, 4); }
+inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
 inline int __all_sync(unsigned mask, int pred) { return __ballot_sync(mask, pred) == (mask & emu::warp().present); }
 inline int __any_sync(unsigned mask, int pred) { return __ballot_sync(mask, pred) != 0; }
 inline void __syncwarp(unsigned mask = 0xffffffffu) { (void)__ballot_sync(mask, 1); }

@@ -142,6 +142,7 @@ def ll(size, m, mat, gapo, gape, qs, ts, xtra, threads=None, dpx=False):
     jobs["qlen"] = [len(x) for x in qs]
     jobs["tlen"] = [len(x) for x in ts]
     jobs["xtra"] = xtra
+    jobs["pad"] = np.arange(n)  # the result slot of each job
     lanes = 16 if size == 1 else 8
     threads = threads or lanes
     slen = max(1, max((len(x) + lanes - 1) // lanes for x in qs))

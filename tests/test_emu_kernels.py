@@ -70,8 +70,12 @@ def test_emulated_wide_band_shapes(emu):
     p = synth.config1(4, seed=9)
     qs = [p.query(i) for i in range(len(p))]
     ts = [p.target(i) for i in range(len(p))]
-    for w, shape in ((100, 3), (100, 4), (180, 6), (230, 6), (480, 7), (480, 8), (900, 9)):
-        res, cig = emu.ext(1, 5, p.mat, 12, 2, 24, 1, qs, ts, w, 100, 10, 0x40, shape=shape)
+    L = emu.lib()
+    index = {(L.emu_shape_threads(s), L.emu_shape_words(s) // L.emu_shape_threads(s)): s
+             for s in range(L.emu_num_shapes())}
+    for w, g, k in ((100, 16, 2), (100, 8, 4), (100, 4, 8), (180, 16, 4), (230, 16, 4), (480, 32, 4), (480, 32, 5),
+                    (900, 32, 8)):
+        res, cig = emu.ext(1, 5, p.mat, 12, 2, 24, 1, qs, ts, w, 100, 10, 0x40, shape=index[(g, k)])
         for i in range(len(qs)):
             exp, _ = O.extz(1, qs[i], ts[i], 5, p.mat, 12, 2, 24, 1, w, 100, 10, 0x40)
             assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (w, i)
