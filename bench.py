@@ -48,10 +48,10 @@ OPS_PER_CELL = {
 }
 # DRAM bytes per nominal cell of the DP kernel, from ncu (dram__bytes_read.sum + dram__bytes_write.sum
 # of one captured launch / its cells), scaled to the workload's launches by their cell counts.
-# extd2: 1,036,943,360 B over 674,520,661 cells (ext_dp_kernel<1,1,8,4>, 20,000 config-1 pairs);
-# ll_i16: 112,092,672 B over 11,259,234,900 cells (ll_dpx_kernel<2,24>, 100,000 config-3 jobs).
+# extd2: 1,038,595,072 B over 674,520,661 cells (ext_dp_kernel<1,1,16,2>, 20,000 config-1 pairs);
+# ll_i16: 111,992,832 B over 11,259,234,900 cells (ll_dpx_kernel<2,20>, 100,000 config-3 jobs).
 # Both grow with the cells a launch processes (traceback rows and sequences), so they scale.
-DRAM_BYTES_PER_CELL = {"extd2": 1036943360 / 674520661, "extz2": None, "ll_i16": 112092672 / 11259234900}
+DRAM_BYTES_PER_CELL = {"extd2": 1038595072 / 674520661, "extz2": None, "ll_i16": 111992832 / 11259234900}
 
 WORKLOADS = {
     "cfg1": "cfg1: 1M extd2 extension pairs, 100-300 nt, w=100, CIGAR",

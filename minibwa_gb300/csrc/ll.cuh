@@ -15,6 +15,10 @@
 #pragma once
 #include "ksw2g.h"
 
+#ifndef KSW2G_LL_LZC
+#define KSW2G_LL_LZC 4
+#endif
+
 namespace ksw2g {
 
 template <int LANES>
@@ -450,6 +454,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
   // reference) in a thread-interleaved column, which is written only when the maximum grows.
   extern __shared__ uint32_t lld_smem[];
   constexpr int SP = ll_dpx_sp(SLEN);
+  constexpr int LZC = KSW2G_LL_LZC;  // lazy-F segments per exit test
   uint16_t *prof = (uint16_t *)(lld_smem + grp * ll_dpx_group_words(m, SLEN, T));
   uint32_t *hm = lld_smem + ll_dpx_hm_offset(m, SLEN, T) + threadIdx.x;  // hm[s * 128]
 
@@ -547,7 +552,7 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
         }
       }
       // lazy-F (ksw2_ll_sse.c:175-185 / 287-297): the reference stops after the first segment
-      // at which f <= H - gapoe holds in every lane.  Segments go in chunks of four: each
+      // at which f <= H - gapoe holds in every lane.  Segments go in chunks of LZC: each
       // chunk's candidate H values and exit tests are computed, one group-wide AND of the
       // tests finds the first exiting segment, and H is kept only up to it.
       bool fin = false;
@@ -555,12 +560,12 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
         const uint32_t fu = __shfl_up_sync(gm, f, 1, T), fw = __shfl_sync(gm, f, T - 1, T);
         f = t ? fu : (fw << 16);
 #pragma unroll
-        for (int c = 0; c < SLEN; c += 4) {
+        for (int c = 0; c < SLEN; c += LZC) {
           if (c < slen && !fin) {
-            uint32_t nh[4];
+            uint32_t nh[LZC];
             unsigned ok = 0;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < LZC; ++u) {
               nh[u] = 0;
               if (c + u < SLEN && c + u < slen) {
                 nh[u] = __vmaxs2(H[c + u], f);
@@ -570,10 +575,10 @@ ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *
               }
             }
             const unsigned all = __reduce_and_sync(gm, ok);
-            const int last = all ? __ffs(all) - 1 : 3;  // the last segment of the chunk that is kept
+            const int last = all ? __ffs(all) - 1 : LZC - 1;  // the last segment of the chunk that is kept
             fin = all != 0;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < LZC; ++u) {
               if (c + u < SLEN && c + u < slen && u <= last) {
                 H[c + u] = nh[u];
                 if (c + u == slen - 1) hl = nh[u];
