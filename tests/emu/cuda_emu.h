@@ -177,6 +177,7 @@ inline unsigned __reduce_add_sync(unsigned mask, unsigned v) { return (unsigned)
 inline unsigned __reduce_max_sync(unsigned mask, unsigned v) { return (unsigned)emu_reduce(mask, v, 3); }
 inline unsigned __reduce_and_sync(unsigned mask, unsigned v) { return (unsigned)emu_reduce(mask, v, 4); }
 inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
+inline int __popc(unsigned x) { return __builtin_popcount(x); }
 inline int __all_sync(unsigned mask, int pred) { return __ballot_sync(mask, pred) == (mask & emu::warp().present); }
 inline int __any_sync(unsigned mask, int pred) { return __ballot_sync(mask, pred) != 0; }
 inline void __syncwarp(unsigned mask = 0xffffffffu) { (void)__ballot_sync(mask, 1); }
