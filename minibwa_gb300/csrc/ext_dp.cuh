@@ -55,11 +55,17 @@ __device__ __forceinline__ uint32_t pick(const uint32_t (&a)[K], int j) {  // a[
 template <int K>
 __device__ __forceinline__ int32_t pickH(const int32_t (&h0)[K], const int32_t (&h1)[K], const int32_t (&h2)[K],
                                          const int32_t (&h3)[K], int j, int b) {
+  // byte b of slot j: every candidate is compared by its position 4i+b, a compile-time
+  // constant, so no array is indexed at run time (the compiler otherwise lowers the
+  // selection to a local-memory table for some shapes)
+  const int t = 4 * j + b;
   int32_t v = 0;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    int32_t c = b == 0 ? h0[i] : b == 1 ? h1[i] : b == 2 ? h2[i] : h3[i];
-    v = (j == i) ? c : v;
+    v = t == 4 * i ? h0[i] : v;
+    v = t == 4 * i + 1 ? h1[i] : v;
+    v = t == 4 * i + 2 ? h2[i] : v;
+    v = t == 4 * i + 3 ? h3[i] : v;
   }
   return v;
 }
@@ -238,22 +244,22 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           top = enb;
           const int wtop = (enb - wb) << 2;
 #pragma unroll
-          for (int i = 0; i < K; ++i)
-            if (((k + G * i) & ~3) == wtop) {
-              U[i] = V[i] = X[i] = Y[i] = init4;
-              if (D2) X2[i] = Y2[i] = init24;
-            }
+          for (int i = 0; i < K; ++i) {  // selects, not a conditional store: no slot is indexed at run time
+            const bool e = ((k + G * i) & ~3) == wtop;
+            U[i] = e ? init4 : U[i], V[i] = e ? init4 : V[i], X[i] = e ? init4 : X[i], Y[i] = e ? init4 : Y[i];
+            if (D2) X2[i] = e ? init24 : X2[i], Y2[i] = e ? init24 : Y2[i];
+          }
         }
         if (en >= r) {  // top row boundary (ksw2_extz2_sse.c:115, ksw2_extd2_sse.c:152-155)
           const int pr = r - base, wr = pr >> 2, sh = (pr & 3) * 8;
           const uint32_t keep = ~(0xffu << sh);
 #pragma unroll
-          for (int i = 0; i < K; ++i)
-            if (k + G * i == wr) {
-              Y[i] = (Y[i] & keep) | (initb << sh);
-              U[i] = (U[i] & keep) | (vb << sh);
-              if (D2) Y2[i] = (Y2[i] & keep) | (init2b << sh);
-            }
+          for (int i = 0; i < K; ++i) {
+            const bool e = k + G * i == wr;
+            Y[i] = e ? (Y[i] & keep) | (initb << sh) : Y[i];
+            U[i] = e ? (U[i] & keep) | (vb << sh) : U[i];
+            if (D2) Y2[i] = e ? (Y2[i] & keep) | (init2b << sh) : Y2[i];
+          }
         }
         // ---- substitution scores written by the 16-byte stores from st0 (ksw2_extz2_sse.c:117-136) ----
         {

@@ -1,5 +1,5 @@
 /*
- * cpu_batch.c -- multi-threaded CPU batch runner (TEST / BASELINE INFRASTRUCTURE).
+ * cpu_batch.c -- multi-threaded CPU batch runner (TEST AND CPU-BASELINE INFRASTRUCTURE).
  *
  * Compiled twice by oracle/Makefile:
  *   - into liboracle.so against the scalar restatement (ksw2_oracle.c), and

@@ -1,5 +1,5 @@
 /*
- * rescue_cpu.c -- mate rescue on the CPU (TEST / BASELINE INFRASTRUCTURE ONLY).
+ * rescue_cpu.c -- mate rescue on the CPU (TEST AND CPU-BASELINE INFRASTRUCTURE ONLY).
  *
  * A scalar C restatement of pe.c's rescue of one candidate window
  * (mb_matesw_core's body, pe.c:340-368, and mb_matesw_align, pe.c:249-300)
