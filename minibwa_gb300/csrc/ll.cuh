@@ -438,8 +438,11 @@ inline size_t ll_dpx_smem_bytes(int m, int slen, int T) {
 // The u8 form is exact for every input.  The i16 form is exact when the host
 // has checked that no H value can reach 32767 and that 0 <= gape, gapo+gape
 // <= 32767; otherwise the host launches ll_kernel above.
+// Resident blocks asked per SM: six up to 16 segments and five up to 24 fit the
+// registers without spilling (config 3's 19 segments: 970 -> 1,131 GCUPS
+// going from four blocks to five).
 template <int SIZE, int SLEN>
-__global__ void __launch_bounds__(128, SLEN <= 24 ? 4 : (SLEN <= 32 ? 3 : 2))
+__global__ void __launch_bounds__(128, SLEN <= 16 ? 6 : SLEN <= 24 ? 5 : (SLEN <= 32 ? 3 : 2))
 ll_dpx_kernel(const ksw2g_ll_job *__restrict__ jobs, int n_jobs, const uint8_t *__restrict__ arena,
               const int8_t *__restrict__ mat_g, int m, int gapo, int gape, ksw2g_ll_result *__restrict__ res,
               uint64_t *__restrict__ blist, const int64_t *__restrict__ blist_off, int *__restrict__ job_counter) {
