@@ -587,10 +587,12 @@ static int sub_ctx(ksw2g_ctx *c, int i, ksw2g_ctx **out) {
   return 0;
 }
 
+// With rt the targets are windows of the device-resident reference (toff is the
+// window start on contig rt->tid[i]) and only the queries are uploaded.
 static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e, int8_t q2,
                              int8_t e2, int n, const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len,
                              const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ext_result_t *res, uint32_t *cigar,
-                             int64_t cigar_cap, int64_t *cigar_used) {
+                             int64_t cigar_cap, int64_t *cigar_used, const RefTargets *rt = nullptr) {
   const int nch = (n + kChunkJobs - 1) / kChunkJobs;
   const int per = (n + nch - 1) / nch;
   ksw2g_ctx *sc[2];
@@ -599,6 +601,7 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
     if ((rc = sub_ctx(c, i, &sc[i]))) return rc;
   int64_t used = 0;
   int pending[2] = {-1, -1};  // chunk index in flight on each sub-context
+  c->oneshot_launches = 0;
   auto finish = [&](int s) -> int {
     const int ch = pending[s];
     if (ch < 0) return 0;
@@ -635,22 +638,29 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
     for (int i = j0; i < j0 + nj; ++i) {
       const ksw2g_job_t &J = jobs[i];
       if (J.qoff < 0 || J.toff < 0 || J.qlen < 0 || J.tlen < 0 || J.qoff + J.qlen > qbuf_len ||
-          J.toff + J.tlen > tbuf_len) {
+          (!rt && J.toff + J.tlen > tbuf_len)) {
         rc = set_err(KSW2G_E_ARG, "job %d: sequence out of buffer bounds", i);
         break;
       }
       qlo = std::min(qlo, J.qoff), qhi = std::max<int64_t>(qhi, J.qoff + J.qlen);
-      tlo = std::min(tlo, J.toff), thi = std::max<int64_t>(thi, J.toff + J.tlen);
+      if (!rt) tlo = std::min(tlo, J.toff), thi = std::max<int64_t>(thi, J.toff + J.tlen);
     }
     if (rc) break;
     if (qlo > qhi) qlo = qhi = 0;
-    if (tlo > thi) tlo = thi = 0;
+    if (rt || tlo > thi) tlo = thi = 0;
     std::vector<ksw2g_job_t> cj(jobs + j0, jobs + j0 + nj);
     for (auto &J : cj) J.qoff -= qlo, J.toff -= tlo;
-    if ((rc = ext_prepare_into(x, b, dual, m, mat, q, e, q2, e2, nj, cj.data(), qbuf + qlo, qhi - qlo, tbuf + tlo,
-                               thi - tlo)))
-      break;
+    if (rt) {
+      const SeqSeg seg{cj.data(), nj, qbuf + qlo, qhi - qlo, nullptr, 0};
+      const RefTargets crt{rt->ref, rt->tid + j0, rt->flags ? rt->flags + j0 : nullptr};
+      rc = ext_prepare_segs(x, b, dual, m, mat, q, e, q2, e2, 1, &seg, &crt);
+    } else {
+      rc = ext_prepare_into(x, b, dual, m, mat, q, e, q2, e2, nj, cj.data(), qbuf + qlo, qhi - qlo, tbuf + tlo,
+                            thi - tlo);
+    }
+    if (rc) break;
     if ((rc = ext_run(x, b))) break;
+    c->oneshot_launches += b->launches + (rt ? 1 : 0) + (nj ? 1 : 0);  // DP and backtrack, window gather, packing
     if (res && nj)
       CK(cudaMemcpyAsync(res + j0, b->res.p, sizeof(ksw2g_ext_result) * nj, cudaMemcpyDeviceToHost, x->st));
     pending[s] = ch;
@@ -710,12 +720,18 @@ extern "C" int ksw2g_ext_batch_ref(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int d
                                    ksw2g_ext_result_t *res, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used) {
   if (!c || !ref) return set_err(KSW2G_E_ARG, "null ctx/ref");
   CK(cudaSetDevice(c->device));
+  const RefTargets rt{ref, tid, tflags};
+  if (n_jobs > kChunkJobs) {
+    if (!tid) return set_err(KSW2G_E_ARG, "reference targets need a contig id per job");
+    return ext_batch_chunked(c, dual, m, mat, q, e, q2, e2, n_jobs, jobs, qbuf, qbuf_len, nullptr, 0, res, cigar,
+                             cigar_cap, cigar_used, &rt);
+  }
   if (!c->scratch) c->scratch = new ksw2g_batch;
   const SeqSeg seg{jobs, n_jobs, qbuf, qbuf_len, nullptr, 0};
-  const RefTargets rt{ref, tid, tflags};
   int rc = ext_prepare_segs(c, c->scratch, dual, m, mat, q, e, q2, e2, 1, &seg, &rt);
   if (rc) return rc;
   if ((rc = ext_run(c, c->scratch))) return rc;
+  c->oneshot_launches = c->scratch->launches + 1 + (n_jobs ? 1 : 0);
   return ksw2g_ext_fetch(c, c->scratch, res, cigar, cigar_cap, cigar_used);
 }
 

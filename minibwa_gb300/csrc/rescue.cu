@@ -195,7 +195,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     ksw2g_batch *b = c->rs_ll[groups[gi].slot];
     if ((rc = ll_run_on(b, gi == 0 ? c->st : c->aux))) return rc;
-    c->rs_launches += 1 + b->launches;  // the window gather, then the DP
+    c->rs_launches += 2 + b->launches;  // query packing and window gather, then the DP
   }
   if (groups.size() > 1 && cudaStreamSynchronize(c->aux) != cudaSuccess)
     return report_error(KSW2G_E_CUDA, "rescue: ksw_ll failed");
@@ -245,7 +245,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
                                   (int)idx.size(), ej.data(), tids.data(), tfl.data(), rq.data(), rq_len, er.data(),
                                   cigar ? cigar + used : nullptr, cigar ? cigar_cap - used : 0, &u)))
       return rc;
-    c->rs_launches += 1 + ksw2g_batch_launches(c->scratch);
+    c->rs_launches += c->oneshot_launches;
     for (size_t k = 0; k < idx.size(); ++k) {
       const int i = idx[k];
       ksw2g_rescue_result_t &R = res[i];

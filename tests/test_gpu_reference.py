@@ -49,6 +49,24 @@ def test_ext_batch_with_reference_targets(ref_ctx, dual):
         assert np.array_equal(gcig[o:o + n], wcig[wo:wo + n]), i
 
 
+def test_chunked_ext_batch_with_reference_targets(ref_ctx):
+    """Above 131,072 jobs the one-shot call runs in chunks on two sub-contexts; with reference
+    targets each chunk gathers its own windows.  Results equal the same jobs with host targets."""
+    from minibwa_gb300 import synth
+    r, ctx, dev = ref_ctx
+    flags = np.random.default_rng(9).choice([0, 1, 2, 5], 140000)
+    p, tids, tfl = synth.ref_pairs(r, 140000, qlen_lo=60, qlen_hi=160, flags=flags, seed=90)
+    want, wcig = ctx.ext_batch(p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf)
+    jobs = p.jobs.copy()
+    jobs["toff"] = p.ref_toff
+    got, gcig = dev.ext_batch(p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, jobs, tids, tfl, p.qbuf)
+    for f in EXT_FIELDS:
+        assert np.array_equal(got[f], want[f]), f
+    for i in range(0, len(p), 7):
+        o, n, wo = int(got["cigar_off"][i]), int(got["n_cigar"][i]), int(want["cigar_off"][i])
+        assert np.array_equal(gcig[o:o + n], wcig[wo:wo + n]), i
+
+
 def test_ll_batch_with_reference_targets(ref_ctx):
     from minibwa_gb300 import synth
     from minibwa_gb300.lib import LL_JOB
