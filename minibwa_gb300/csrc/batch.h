@@ -88,6 +88,7 @@ struct ksw2g_ctx {
   PinBuf one_h;         // per-call drop-in staging (pinned)
   DevBuf rs_q, rs_t, rs_meta, rs_res, rs_hist;  // mate-rescue prefilter: reads, windows, records, votes
   PinBuf rs_h;                                  // mate-rescue staging (pinned)
+  PinBuf rs_rq;                                 // mate-rescue reversed read prefixes (pinned)
   int oneshot_launches = 0;                     // kernels the last one-shot extension call launched
   ksw2g_batch *rs_ll[6] = {};                   // mate-rescue ksw_ll batches, one per (size, methylation)
   int rs_launches = 0;                          // kernels the last rescue call launched

@@ -121,6 +121,7 @@ extern "C" void ksw2g_ctx_destroy(ksw2g_ctx_t *c) {
   for (ksw2g_batch *b : c->rs_ll)
     if (b) ksw2g_batch_free(b);
   c->rs_h.release();
+  c->rs_rq.release();
   cudaStreamDestroy(c->st);
   delete c;
 }

@@ -55,6 +55,18 @@ void gen_nt4(int8_t *mat, int8_t a, int8_t b, int8_t b_ts, int8_t b_ambi, int mt
 
 inline int64_t al16(int64_t x) { return (x + 15) & ~(int64_t)15; }
 
+// dst[p] = src[n-1-p], eight bytes at a time
+void reverse_bytes(uint8_t *dst, const uint8_t *src, int n) {
+  int p = 0;
+  for (; p + 8 <= n; p += 8) {
+    uint64_t w;
+    memcpy(&w, src + n - p - 8, 8);
+    w = __builtin_bswap64(w);
+    memcpy(dst + p, &w, 8);
+  }
+  for (; p < n; ++p) dst[p] = src[n - 1 - p];
+}
+
 double ms_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -227,13 +239,15 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     std::vector<int32_t> tids(idx.size()), tfl(idx.size(), KSW2G_REF_REVERSE);
     int64_t rq_len = 0;
     for (int i : idx) rq_len += res[i].ll_qe + 1;
-    std::vector<uint8_t> rq((size_t)std::max<int64_t>(rq_len, 1));
+    // the reversed prefixes go to a reused pinned buffer: no zero fill, and the upload is a DMA
+    if ((rc = c->rs_rq.ensure((size_t)std::max<int64_t>(rq_len, 1)))) return rc;
+    uint8_t *rq = (uint8_t *)c->rs_rq.p;
     int64_t qo = 0;
     for (size_t k = 0; k < idx.size(); ++k) {
       const int i = idx[k];
       const int qe = res[i].ll_qe + 1, te = res[i].ll_te + 1;
       const uint8_t *src = qbuf + jobs[i].qoff;
-      for (int p = 0; p < qe; ++p) rq[qo + p] = src[qe - 1 - p];  // mb_seq_rev(qe, qseq)
+      reverse_bytes(rq + qo, src, qe);  // mb_seq_rev(qe, qseq)
       ej[k] = ksw2g_job_t{qo, res[i].ts2, qe, te, o.bw, o.zdrop, o.end_bonus, flag};
       tids[k] = jobs[i].tid;
       qo += qe;
@@ -242,7 +256,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     int64_t u = 0;
     // CIGARs go straight into the caller's buffer behind those of earlier groups
     if ((rc = ksw2g_ext_batch_ref(c, ref, 0, 5, mat, (int8_t)o.q, (int8_t)o.e, (int8_t)o.q, (int8_t)o.e,
-                                  (int)idx.size(), ej.data(), tids.data(), tfl.data(), rq.data(), rq_len, er.data(),
+                                  (int)idx.size(), ej.data(), tids.data(), tfl.data(), rq, rq_len, er.data(),
                                   cigar ? cigar + used : nullptr, cigar ? cigar_cap - used : 0, &u)))
       return rc;
     c->rs_launches += c->oneshot_launches;
