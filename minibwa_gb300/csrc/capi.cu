@@ -1026,10 +1026,66 @@ extern "C" int ksw2g_ll_fetch(ksw2g_ctx_t *c, ksw2g_batch_t *b, ksw2g_ll_result_
   return 0;
 }
 
+// One-shot ksw_ll batches of more than kLLChunkJobs jobs run as chunks that alternate
+// between the two sub-contexts, so each chunk's uploads overlap the previous chunk's DP.
+static const int kLLChunkJobs = 262144;
+
+static int ll_batch_chunked(ksw2g_ctx *c, int size, int m, const int8_t *mat, int gapo, int gape, int n,
+                            const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+                            int64_t tbuf_len, ksw2g_ll_result_t *res) {
+  const int nch = (n + kLLChunkJobs - 1) / kLLChunkJobs;
+  const int per = (n + nch - 1) / nch;
+  ksw2g_ctx *sc[2];
+  int rc;
+  for (int i = 0; i < 2; ++i)
+    if ((rc = sub_ctx(c, i, &sc[i]))) return rc;
+  int pending[2] = {-1, -1};
+  auto finish = [&](int s) -> int {
+    const int ch = pending[s];
+    if (ch < 0) return 0;
+    pending[s] = -1;
+    return ksw2g_ll_fetch(sc[s], sc[s]->scratch, res ? res + (size_t)ch * per : nullptr);
+  };
+  for (int ch = 0; ch < nch && !rc; ++ch) {
+    const int s = ch & 1;
+    if ((rc = finish(s))) break;
+    const int j0 = ch * per, nj = std::min(per, n - j0);
+    int64_t qlo = qbuf_len, qhi = 0, tlo = tbuf_len, thi = 0;
+    for (int i = j0; i < j0 + nj; ++i) {
+      const ksw2g_ll_job_t &J = jobs[i];
+      if (J.qoff < 0 || J.toff < 0 || J.qlen < 0 || J.tlen < 0 || J.qoff + J.qlen > qbuf_len ||
+          J.toff + J.tlen > tbuf_len) {
+        rc = set_err(KSW2G_E_ARG, "ll job %d: sequence out of buffer bounds", i);
+        break;
+      }
+      qlo = std::min(qlo, J.qoff), qhi = std::max<int64_t>(qhi, J.qoff + J.qlen);
+      tlo = std::min(tlo, J.toff), thi = std::max<int64_t>(thi, J.toff + J.tlen);
+    }
+    if (rc) break;
+    if (qlo > qhi) qlo = qhi = 0;
+    if (tlo > thi) tlo = thi = 0;
+    std::vector<ksw2g_ll_job_t> cj(jobs + j0, jobs + j0 + nj);
+    for (auto &J : cj) J.qoff -= qlo, J.toff -= tlo;
+    ksw2g_ctx *x = sc[s];
+    if ((rc = ll_prepare_into(x, x->scratch, size, m, mat, gapo, gape, nj, cj.data(), qbuf + qlo, qhi - qlo,
+                              tbuf + tlo, thi - tlo)))
+      break;
+    if ((rc = ll_run(x, x->scratch))) break;
+    pending[s] = ch;
+  }
+  for (int k = 0; k < 2 && !rc; ++k) rc = finish(pending[0] >= 0 && (pending[1] < 0 || pending[0] < pending[1]) ? 0 : 1);
+  if (rc)
+    for (int s = 0; s < 2; ++s) cudaStreamSynchronize(sc[s]->st);
+  return rc;
+}
+
 extern "C" int ksw2g_ll_batch(ksw2g_ctx_t *c, int size, int m, const int8_t *mat, int gapo, int gape, int n_jobs,
                               const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
                               int64_t tbuf_len, ksw2g_ll_result_t *res) {
   if (!c) return set_err(KSW2G_E_ARG, "null ctx");
+  CK(cudaSetDevice(c->device));
+  if (n_jobs > kLLChunkJobs && jobs && mat)
+    return ll_batch_chunked(c, size, m, mat, gapo, gape, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len, res);
   if (!c->scratch) c->scratch = new ksw2g_batch;
   int rc = ll_prepare_into(c, c->scratch, size, m, mat, gapo, gape, n_jobs, jobs, qbuf, qbuf_len, tbuf, tbuf_len);
   if (rc) return rc;

@@ -130,3 +130,20 @@ def test_long_queries_shared_memory_kernel(ctx):
         K.ll_free(qp)
         want, _ = O.ll(2, q, t, 5, r.mat, r.gapo, r.gape, 0)
         assert (s, qe, te) == (want["score"], want["qe"], want["te"])
+
+
+def test_one_shot_chunked_equals_resident(ctx):
+    """Above 262,144 jobs the one-shot ksw_ll call runs in chunks on two sub-contexts; its
+    results equal the resident batch's, with the pe.c u8 scoring and second-best lists."""
+    from minibwa_gb300 import LLBatch, synth
+    from minibwa_gb300.lib import KSW_LL_SUBO
+    r = synth.config3(600000, seed=77)
+    jobs = r.jobs.copy()
+    jobs["xtra"] = np.where(np.arange(len(jobs)) % 2 == 0, KSW_LL_SUBO | 19, 0)
+    b = LLBatch(ctx, r.size, 5, r.mat, r.gapo, r.gape, jobs, r.qbuf, r.tbuf)
+    b.run()
+    want = b.fetch()
+    b.free()
+    got = ctx.ll_batch(r.size, 5, r.mat, r.gapo, r.gape, jobs, r.qbuf, r.tbuf)
+    compare_ll(got, want)
+    assert np.array_equal(got["rows"], want["rows"])
