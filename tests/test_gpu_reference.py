@@ -50,7 +50,7 @@ def test_ext_batch_with_reference_targets(ref_ctx, dual):
 
 
 def test_chunked_ext_batch_with_reference_targets(ref_ctx):
-    """Above 131,072 jobs the one-shot call runs in chunks on two sub-contexts; with reference
+    """Above 32,768 jobs the one-shot call runs in chunks on two sub-contexts; with reference
     targets each chunk gathers its own windows.  Results equal the same jobs with host targets."""
     from minibwa_gb300 import synth
     r, ctx, dev = ref_ctx
