@@ -34,6 +34,9 @@ cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params 
               : launch_ext_dp_z2(mode, shape, P, L, max_blocks, st);
 }
 
+static const int64_t kWaveTarget = (int64_t)1 << 30;  // traceback bytes per wave of short pairs
+static const double kLongCells = 200000.0;             // mean band cells above which pairs count as long
+
 // shape preference per (dual, mode, n_col); 0 = use the smallest shape that fits
 static const int kMaxPrefCol = 512;
 static int g_pref[2][3][kMaxPrefCol + 1];
@@ -316,6 +319,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   std::vector<int> shape(n), mode(n);
   std::vector<int64_t> foot(n);
   int64_t cig = 0, wide_max = 0;
+  double band_cells = 0;  // sum of (qlen + tlen) x band width: the batch's size class
   int n_wide = 0;
   for (int i = 0; i < n; ++i) {
     const ksw2g_job_t &J = jobs[i];
@@ -336,6 +340,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
       return set_err(KSW2G_E_CAPACITY, "job %d: traceback needs %lld bytes, budget %lld", i, (long long)foot[i],
                      (long long)c->tb_budget);
     if (mode[i] != 0) cig += J.qlen + J.tlen + 1;
+    band_cells += (double)(J.qlen + J.tlen) * (nc > 1 ? 16.0 * (nc - 1) : 0.0);
   }
   std::vector<int64_t> qpad, tpad;
   int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad, rt);
@@ -361,7 +366,14 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     for (int i = 0; i < n; ++i) srt[cnt[(size_t)(maxkey - ((int64_t)ql[i] + tl[i]))]++] = i;
   }
   b->waves.clear();
-  const int64_t wave_cap = std::max<int64_t>(c->tb_budget / std::max(c->wave_div, 1), 16);
+  // Runs that alternate waves between two streams cut batches of short pairs into waves
+  // of at most 1 GiB of traceback rows (a single larger job still gets a wave of its
+  // own, up to the budget): on 1,000,000 config-1 pairs a step takes 187.8 ms with 1 GiB
+  // waves, 190.1 with 4 GiB and 192.5 with 8 GiB.  Batches of long pairs keep the largest
+  // waves, because every wave ends with the tail of its longest pair (config 2's long
+  // pairs ran 3.6x slower in 1 GiB waves).
+  int64_t wave_cap = std::max<int64_t>(c->tb_budget / std::max(c->wave_div, 1), 16);
+  if (c->wave_div >= 2 && n > 0 && band_cells / n < kLongCells) wave_cap = std::min<int64_t>(wave_cap, kWaveTarget);
   std::vector<int64_t> tbo(n);
   std::vector<int32_t> ord(n);
   int64_t ordp = 0;
@@ -581,7 +593,6 @@ extern "C" int ksw2g_ext_fetch(ksw2g_ctx_t *c, ksw2g_batch_t *b, ksw2g_ext_resul
 // 32,768 than of 131,072.  So batches whose pairs average more than kLongCells
 // band cells use the larger chunk.
 static const int kChunkJobs = 32768, kChunkJobsLong = 131072;
-static const double kLongCells = 200000.0;
 
 static int chunk_jobs(int n, const ksw2g_job_t *jobs) {
   double cells = 0;
