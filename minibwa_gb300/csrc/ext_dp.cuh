@@ -18,8 +18,8 @@
 // Per anti-diagonal each thread first exchanges, in one packed shuffle per
 // slot, the last bytes of its x, v (and x2) words with its neighbour, then
 // computes all its slots back to back (independent chains).  Words past the
-// band's last padded block are computed too but never read; a block that
-// enters the band is reset to the reference's initial state first.  The maximum and
+// band's last padded block are skipped and hold stale state, never read; a block
+// that enters the band is reset to the reference's initial state first.  The maximum and
 // its tie-break use single-instruction warp reductions.
 //
 // Every cell operation reproduces the reference's byte-lane semantics
@@ -52,24 +52,6 @@ __device__ __forceinline__ uint32_t pick(const uint32_t (&a)[K], int j) {  // a[
   for (int i = 1; i < K; ++i) v = (j == i) ? a[i] : v;
   return v;
 }
-template <int K>
-__device__ __forceinline__ int32_t pickH(const int32_t (&h0)[K], const int32_t (&h1)[K], const int32_t (&h2)[K],
-                                         const int32_t (&h3)[K], int j, int b) {
-  // byte b of slot j: every candidate is compared by its position 4i+b, a compile-time
-  // constant, so no array is indexed at run time (the compiler otherwise lowers the
-  // selection to a local-memory table for some shapes)
-  const int t = 4 * j + b;
-  int32_t v = 0;
-#pragma unroll
-  for (int i = 0; i < K; ++i) {
-    v = t == 4 * i ? h0[i] : v;
-    v = t == 4 * i + 1 ? h1[i] : v;
-    v = t == 4 * i + 2 ? h2[i] : v;
-    v = t == 4 * i + 3 ? h3[i] : v;
-  }
-  return v;
-}
-
 // shift a per-slot array down by four words (word i <- word i+4)
 template <int G, int K, typename T>
 __device__ __forceinline__ void shift4(T (&a)[K], T fill, int k, unsigned gm) {
@@ -132,7 +114,8 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
   const uint8_t *qp = nullptr, *tp = nullptr;
   uint8_t *tb = nullptr;
   int32_t ez_max = 0, max_q = -1, max_t = -1, mqe = KSW2G_NEG_INF, mqe_t = -1, mte = KSW2G_NEG_INF, mte_q = -1;
-  int32_t score = KSW2G_NEG_INF, zdropped = 0, H_left = KSW2G_NEG_INF, last_max_H = 0, Hz = 0, last_H0_t = 0;
+  int32_t score = KSW2G_NEG_INF, zdropped = 0, last_max_H = 0, Hz = 0, last_H0_t = 0;
+  int32_t hA = 0, hB = 0, last_en0 = 0;  // H[en0] and H[en0 - 1] after the last anti-diagonal
   bool active = false, need = true;
 
   auto vv = [&](uint32_t byte) -> int32_t { return D2 ? (int32_t)(int8_t)(uint8_t)byte : (int32_t)(byte & 0xffu) - qe; };
@@ -172,7 +155,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         }
         qp = arena + J.qoff, tp = arena + J.toff;
         if (CIG) tb = tb_pool + tb_off[jid];
-        r = 0, wb = 0, top = 0, H_left = KSW2G_NEG_INF, last_max_H = 0, Hz = 0, last_H0_t = 0;
+        r = 0, wb = 0, top = 0, last_max_H = 0, Hz = 0, last_H0_t = 0, hA = hB = 0, last_en0 = 0;
 #pragma unroll
         for (int i = 0; i < K; ++i) {
           U[i] = V[i] = X[i] = Y[i] = init4;
@@ -208,7 +191,6 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           const uint32_t vr = __shfl_sync(gm, V[0], 3, G) >> 24;
           uint32_t x2r = 0;
           if (D2) x2r = __shfl_sync(gm, X2[0], 3, G) >> 24;
-          H_left = __shfl_sync(gm, H3[0], 3, G);
           shift4<G, K>(U, init4, k, gm);
           shift4<G, K>(V, init4, k, gm);
           shift4<G, K>(X, init4, k, gm);
@@ -239,8 +221,8 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         const int en = (enb << 4) + 15;
         if (enb > top) {
           // A 16-byte block enters the band (at most one per anti-diagonal).  Words past
-          // the last live block are computed every anti-diagonal but never read, so the
-          // entering block gets the state the reference's untouched memory holds.
+          // the last live block hold stale state, so the entering block gets the state the
+          // reference's untouched memory holds.
           top = enb;
           const int wtop = (enb - wb) << 2;
 #pragma unroll
@@ -316,14 +298,18 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
 #pragma unroll
           for (int i = 0; i < K; ++i) {
             const uint32_t send = (k == G - 1) ? (i > 0 ? pk[i > 0 ? i - 1 : 0] : 0u) : pk[i];
-            rv[i] = __shfl_sync(gm, send, (k - 1) & (G - 1), G);
+            rv[i] = 0u;
+            if (G * i < nlive) rv[i] = __shfl_sync(gm, send, (k - 1) & (G - 1), G);  // group-uniform
           }
           if (k == 0) rv[0] = x1 | (v1 << 8) | (x21 << 16);
         }
 #pragma unroll
         for (int i = 0; i < K; ++i) {
           const int wi = k + G * i;
-          const bool live = wi < nlive;
+          // A word past the last live block is never read before its block enters the band
+          // and is reset, so it is not computed; a slot dead in every group of the warp costs
+          // nothing (the groups of a warp mostly run pairs of equal length in step).
+          if (wi >= nlive) continue;
           uint32_t xt1 = __byte_perm(rv[i], X[i], 0x6540);  // x[r-1][t-1 .. t+2]
           uint32_t vt1 = __byte_perm(rv[i], V[i], 0x6541);
           if (!D2 && i == 0 && k == 0) xt1 |= extx, vt1 |= extv;
@@ -423,52 +409,65 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           }
           U[i] = nu, V[i] = nv, X[i] = nx, Y[i] = ny;
           if (D2) X2[i] = nx2, Y2[i] = ny2;
-          if (CIG && live) row[wi] = d;
+          if (CIG) row[wi] = d;
         }
         ++n_diag;
         cells += en0 - st0 + 1;
         // ---- exact or approximate max, z-drop (ksw2_extz2_sse.c:216-278, ksw2_extd2_sse.c:315-385) ----
         if (!(flag & KSW2G_APPROX_MAX)) {
-          const int pe = en0 - base;
+          const int pe = en0 - base, ws = pe >> 2, bs = pe & 3;
           int32_t Hen0;
           if (r == 0) {
             Hen0 = vv(__shfl_sync(gm, V[0], 0, G) & 0xff) - qe;
-          } else {
-            const int ws = pe >> 2, bs = pe & 3;
-            if (en0 > 0) {
+          } else if (en0 > 0) {
+            // H[en0 - 1] of the anti-diagonal before: its H[en0] when en0 moved up by one,
+            // else its H[en0 - 1] (hA and hB carry the two from one anti-diagonal to the next;
+            // the second may be a cell that already left the band, as in the reference's array)
+            const int32_t hm1 = en0 > last_en0 ? hA : hB;
+            const uint32_t uw = __shfl_sync(gm, pick<K>(U, ws / G), ws & (G - 1), G);
+            Hen0 = hm1 + vv(uw >> (8 * bs));
+            hB = hm1;
+            if (en0 - 1 >= st0) {  // H[en0 - 1] takes this anti-diagonal's v (pe - 1 >= st0 - base >= 0)
               const int pm = pe - 1;
-              int32_t hm1 = pm >= 0 ? __shfl_sync(gm, pickH<K>(H0, H1, H2, H3, (pm >> 2) / G, pm & 3), (pm >> 2) & (G - 1), G)
-                                    : H_left;
-              const uint32_t uw = __shfl_sync(gm, pick<K>(U, ws / G), ws & (G - 1), G);
-              Hen0 = hm1 + vv(uw >> (8 * bs));
-            } else {
-              const int32_t h = __shfl_sync(gm, pickH<K>(H0, H1, H2, H3, ws / G, bs), ws & (G - 1), G);
-              const uint32_t vw = __shfl_sync(gm, pick<K>(V, ws / G), ws & (G - 1), G);
-              Hen0 = h + vv(vw >> (8 * bs));
+              const uint32_t vw = __shfl_sync(gm, pick<K>(V, (pm >> 2) / G), (pm >> 2) & (G - 1), G);
+              hB += vv(vw >> (8 * (pm & 3)));
             }
+          } else {
+            const uint32_t vw = __shfl_sync(gm, pick<K>(V, ws / G), ws & (G - 1), G);
+            Hen0 = hA + vv(vw >> (8 * bs));
           }
-          // update H over [st0, en0] and find the local maximum
+          hA = Hen0, last_en0 = en0;
+          // Update H over [st0, en0) and set H[en0]; then the local maximum.  Cells past en0
+          // take the additions too: they start at KSW2G_NEG_INF, stay far below any score, and
+          // are set when en0 reaches them.  Cells below st0 keep their value (the reference
+          // reads one back through H[en0 - 1] above); only window words 0-3 -- threads 0-3 of
+          // slot 0 -- can lie below st0, since the window starts at st0's 16-cell block.
+          const int se = ws / G;  // slot and thread of H[en0]
+          const bool own = k == (ws & (G - 1));
+          const int lo = st0 - base - 4 * k;  // slot 0: bytes b >= lo are at or above st0
           int32_t lmax = INT32_MIN;
 #pragma unroll
           for (int i = 0; i < K; ++i) {
-            const int p0 = base + 4 * (k + G * i);
-            if (p0 + 3 >= st0 && p0 <= en0) {
-              const uint32_t vw = V[i];
-              if (p0 >= st0 && p0 + 3 < en0) {
-                H0[i] += vv(vw), H1[i] += vv(vw >> 8), H2[i] += vv(vw >> 16), H3[i] += vv(vw >> 24);
-                lmax = max(lmax, max(max(H0[i], H1[i]), max(H2[i], H3[i])));
-              } else {
-                auto upd = [&](int32_t &h, int b) {
-                  const int p = p0 + b;
-                  if (p == en0) h = Hen0;
-                  else if (p >= st0 && p < en0) h += vv(vw >> (8 * b));
-                  if (p >= st0 && p <= en0) lmax = max(lmax, h);
-                };
-                upd(H0[i], 0);
-                upd(H1[i], 1);
-                upd(H2[i], 2);
-                upd(H3[i], 3);
-              }
+            const uint32_t vw = V[i];
+            if (i == 0) {
+              H0[0] += lo <= 0 ? vv(vw) : 0;
+              H1[0] += lo <= 1 ? vv(vw >> 8) : 0;
+              H2[0] += lo <= 2 ? vv(vw >> 16) : 0;
+              H3[0] += lo <= 3 ? vv(vw >> 24) : 0;
+            } else {
+              H0[i] += vv(vw), H1[i] += vv(vw >> 8), H2[i] += vv(vw >> 16), H3[i] += vv(vw >> 24);
+            }
+            if (i == se) {  // group-uniform
+              H0[i] = own && bs == 0 ? Hen0 : H0[i];
+              H1[i] = own && bs == 1 ? Hen0 : H1[i];
+              H2[i] = own && bs == 2 ? Hen0 : H2[i];
+              H3[i] = own && bs == 3 ? Hen0 : H3[i];
+            }
+            if (i == 0) {
+              lmax = max(max(lo <= 0 ? H0[0] : INT32_MIN, lo <= 1 ? H1[0] : INT32_MIN),
+                         max(lo <= 2 ? H2[0] : INT32_MIN, lo <= 3 ? H3[0] : INT32_MIN));
+            } else {
+              lmax = max(lmax, max(max(H0[i], H1[i]), max(H2[i], H3[i])));
             }
           }
           const int32_t gmax = __reduce_max_sync(gm, lmax);
@@ -502,8 +501,9 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           const int mt = key == 0 ? en0 : st0 + (int)(key & 0xffffffu);
           if (en0 == tlen - 1 && Hen0 > mte) mte = Hen0, mte_q = r - en0;
           if (r - st0 == qlen - 1) {
-            const int ps = st0 - base;
-            const int32_t hs = __shfl_sync(gm, pickH<K>(H0, H1, H2, H3, (ps >> 2) / G, ps & 3), (ps >> 2) & (G - 1), G);
+            const int ps = st0 - base, bsel = ps & 3;  // H[st0]: slot 0 of thread ps / 4
+            const int32_t h0 = bsel == 0 ? H0[0] : bsel == 1 ? H1[0] : bsel == 2 ? H2[0] : H3[0];
+            const int32_t hs = __shfl_sync(gm, h0, ps >> 2, G);
             if (hs > mqe) mqe = hs, mqe_t = st0;
           }
           // ksw_apply_zdrop (ksw2.h:181-197)
