@@ -95,6 +95,9 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
   const uint32_t mis4 = splat8(D2 ? P.c_mis : P.c_mis + P.c_qe2);
   const uint32_t N4 = splat8(D2 ? P.c_N : P.c_N + P.c_qe2);
   const uint32_t m14 = splat8(P.c_m1), maxsc4 = splat8(P.c_maxsc), mchraw4 = splat8(P.c_mch);
+  // score table of the byte-permute lookup: lane index 0 = match, 1-3 = mismatch, 4-7 = N
+  const bool nt4 = P.c_m1 == 4;
+  const uint32_t sc_lo = (mch4 & 0xffu) | (mis4 & 0xffffff00u), sc_hi = N4;
   const uint32_t initb = D2 ? (uint32_t)(uint8_t)(-P.q - P.e) : 0u;
   const uint32_t init2b = D2 ? (uint32_t)(uint8_t)(-P.q2 - P.e2) : 0u;
   const uint32_t init4 = splat8(initb), init24 = splat8(init2b);
@@ -258,7 +261,12 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
               const uint32_t Tw = TW[i];
               uint32_t sn;
-              if (!generic) {
+              if (!generic && nt4 && ((Tw | Qw) & 0xf8f8f8f8u) == 0) {
+                // codes 0-4 with N = 4: lane index (t ^ q) & 3 | (t | q) & 4 is 0 for a match,
+                // 1-3 for a mismatch and 4-7 when either base is N; one byte permute looks it up
+                const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | ((Tw | Qw) & 0x04040404u);
+                sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
+              } else if (!generic) {
                 const uint32_t eq = eqz8(Tw ^ Qw);
                 const uint32_t nn = eqz8(Tw ^ m14) | eqz8(Qw ^ m14);
                 sn = sel(bmask(eq), mch4, mis4);
@@ -478,22 +486,26 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           const bool need_mt = ez_e < 0 || gmax > ez_max || (zdrop >= 0 && ez_max - gmax > zdrop);
           uint32_t key = 0xffffffffu;
           if (need_mt && lmax == gmax) {
-            const int en1 = st0 + (((en0 - st0) >> 2) << 2);
+            // cells holding the maximum: one bit per cell of the thread's words (cells past en0
+            // never hold it; cells below st0 are masked), then the key of each, usually one
+            const int E = en0 - st0, L4 = E & ~3;
+            uint32_t mm = 0;
 #pragma unroll
             for (int i = 0; i < K; ++i) {
-              const int p0 = base + 4 * (k + G * i);
-              if (p0 + 3 >= st0 && p0 <= en0) {
-                const int32_t hv[4] = {H0[i], H1[i], H2[i], H3[i]};
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                  const int p = p0 + b;
-                  if (p >= st0 && p <= en0 && hv[b] == gmax) {
-                    const uint32_t c = p == en0 ? 0u : p < en1 ? (uint32_t)(1 + ((p - st0) & 3)) : 5u;
-                    const uint32_t kk = p == en0 ? 0u : (c << 24) | (uint32_t)(p - st0);
-                    key = min(key, kk);
-                  }
-                }
-              }
+              mm |= (H0[i] == gmax ? 1u : 0u) << (4 * i);
+              mm |= (H1[i] == gmax ? 2u : 0u) << (4 * i);
+              mm |= (H2[i] == gmax ? 4u : 0u) << (4 * i);
+              mm |= (H3[i] == gmax ? 8u : 0u) << (4 * i);
+            }
+            if (lo > 0) mm &= lo >= 4 ? ~0xfu : ~((1u << lo) - 1u);
+            while (mm) {
+              const int j = __ffs(mm) - 1;
+              mm &= mm - 1;
+              const int o = base + 4 * (k + G * (j >> 2)) + (j & 3) - st0;
+              const uint32_t kk = o == E  ? 0u
+                                  : o < L4 ? ((uint32_t)(1 + (o & 3)) << 24) | (uint32_t)o
+                                           : (5u << 24) | (uint32_t)o;
+              key = min(key, kk);
             }
           }
           if (need_mt) key = __reduce_min_sync(gm, key);
