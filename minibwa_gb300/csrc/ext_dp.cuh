@@ -250,6 +250,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         {
           const bool generic = flag & KSW2G_GENERIC_SC;
           const int fend = generic ? en0 : st0 + (((en0 - st0) >> 4) << 4) + 15;
+          const int wf = (fend - base) >> 2;
           const int o = (r + 1) & 3;
           const uint32_t qsel = (uint32_t)((o + 3) | ((o + 2) << 4) | ((o + 1) << 8) | (o << 12));
 #pragma unroll
@@ -281,10 +282,17 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
                   sn |= v << (8 * b);
                 }
               }
-              const int lo = st0 - p0, hi = fend - p0;
+              // only the word holding st0 (slot 0) and the one holding fend (slot wf / G) are
+              // partly outside the stores; every other word takes all four scores
               uint32_t wm = 0xffffffffu;
-              if (lo > 0) wm <<= 8 * lo;
-              if (hi < 3) wm &= 0xffffffffu >> (8 * (3 - hi));
+              if (i == 0) {
+                const int lo = st0 - p0;
+                if (lo > 0) wm <<= 8 * lo;
+              }
+              if (i == wf / G) {  // group-uniform
+                const int hi = fend - p0;
+                if (hi < 3) wm &= 0xffffffffu >> (8 * (3 - hi));
+              }
               S[i] = (S[i] & ~wm) | (sn & wm);
             }
           }
@@ -401,16 +409,16 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             b2 = sub8(b2, tq);
             if (MODE == 1) {
               const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi, ga2 = gt0s8(a2) & kHi, gb2 = gt0s8(b2) & kHi;
-              nx = sub8(a & bmask(ga), qe4);
-              ny = sub8(b & bmask(gb), qe4);
-              nx2 = sub8(a2 & bmask(ga2), qe24);
-              ny2 = sub8(b2 & bmask(gb2), qe24);
+              nx = sub8_nn((a & bmask(ga)) | kHi, qe4);
+              ny = sub8_nn((b & bmask(gb)) | kHi, qe4);
+              nx2 = sub8_nn((a2 & bmask(ga2)) | kHi, qe24);
+              ny2 = sub8_nn((b2 & bmask(gb2)) | kHi, qe24);
               d |= (ga >> 4) | (gb >> 3) | (ga2 >> 2) | (gb2 >> 1);
             } else {
-              nx = sub8(relu8(a), qe4);
-              ny = sub8(relu8(b), qe4);
-              nx2 = sub8(relu8(a2), qe24);
-              ny2 = sub8(relu8(b2), qe24);
+              nx = sub8_nn(relu8(a) | kHi, qe4);
+              ny = sub8_nn(relu8(b) | kHi, qe4);
+              nx2 = sub8_nn(relu8(a2) | kHi, qe24);
+              ny2 = sub8_nn(relu8(b2) | kHi, qe24);
               if (MODE == 2)
                 d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3) | ((~a2 & kHi) >> 2) | ((~b2 & kHi) >> 1);
             }

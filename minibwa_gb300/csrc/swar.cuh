@@ -37,6 +37,9 @@ __device__ __forceinline__ uint32_t add8(uint32_t a, uint32_t b) {
 __device__ __forceinline__ uint32_t sub8(uint32_t a, uint32_t b) {
   return ((a | kHi) - (b & kLo)) ^ ((a ^ ~b) & kHi);
 }
+// lane-wise r - c (mod 256) for lanes r in [0, 127], given rh = r | 0x80 in every lane: the
+// biased lanes r + 128 - (c & 127) never borrow, and the msb is fixed up from c's msb
+__device__ __forceinline__ uint32_t sub8_nn(uint32_t rh, uint32_t c) { return (rh - (c & kLo)) ^ (~c & kHi); }
 // msb mask of (int8)a > (int8)b
 __device__ __forceinline__ uint32_t gts8(uint32_t a, uint32_t b) {
   uint32_t c = (b | kHi) - (a & kLo);            // bit7: b_lo >= a_lo
