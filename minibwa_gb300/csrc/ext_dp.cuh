@@ -314,8 +314,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
 #pragma unroll
           for (int i = 0; i < K; ++i) {
             const uint32_t send = (k == G - 1) ? (i > 0 ? pk[i > 0 ? i - 1 : 0] : 0u) : pk[i];
-            rv[i] = 0u;
-            if (G * i < nlive) rv[i] = __shfl_sync(gm, send, (k - 1) & (G - 1), G);  // group-uniform
+            rv[i] = __shfl_sync(gm, send, (k - 1) & (G - 1), G);
           }
           if (k == 0) rv[0] = x1 | (v1 << 8) | (x21 << 16);
         }

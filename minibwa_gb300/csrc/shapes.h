@@ -4,8 +4,8 @@
 // stores running past en0 land in the kernel's extra score-only slot.
 // Without a tuned preference a pair runs on the first shape that holds its
 // band, so among shapes of equal words the first is the default.  For 32-word
-// bands (8,4) runs 1,000,000 pairs of 100-300 nt at w=100 in 192.8 ms, (16,2),
-// which fits five extd2 blocks per SM instead of four, in 194.2 ms.
+// bands (8,4) runs extd2 pairs of 100-300 nt at w=100 in 149.7 ns per pair on a
+// GB300, (16,2), which fits five extd2 blocks per SM instead of four, in 170.4 ns.
 #pragma once
 #define KSW2G_SHAPES(X)                                                                              \
   X(0, 4, 3) X(1, 4, 4) X(2, 8, 3) X(3, 8, 4) X(4, 16, 2) X(5, 4, 8) X(6, 16, 3) X(7, 16, 4) X(8, 32, 4) \
