@@ -250,9 +250,13 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         {
           const bool generic = flag & KSW2G_GENERIC_SC;
           const int fend = generic ? en0 : st0 + (((en0 - st0) >> 4) << 4) + 15;
-          const int wf = (fend - base) >> 2;
           const int o = (r + 1) & 3;
           const uint32_t qsel = (uint32_t)((o + 3) | ((o + 2) << 4) | ((o + 1) << 8) | (o << 12));
+          // Bytes of a word outside [st0, fend] keep their old scores (the reference does not
+          // store them).  The scores are first taken by a byte-permute lookup, exact for m = 5
+          // (N = 4) when in every lane t | q <= 4; otherwise the thread runs the loop again with
+          // the general comparisons (or the matrix), over the same byte masks.
+          uint32_t bad = generic || !nt4 ? 0xffffffffu : 0u;
 #pragma unroll
           for (int i = 0; i <= K; ++i) {
             const int p0 = base + 4 * (k + G * i);
@@ -261,39 +265,49 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
               const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
               const uint32_t Tw = TW[i];
-              uint32_t sn;
-              if (!generic && nt4 && ((Tw | Qw) & 0xf8f8f8f8u) == 0) {
-                // codes 0-4 with N = 4: lane index (t ^ q) & 3 | (t | q) & 4 is 0 for a match,
-                // 1-3 for a mismatch and 4-7 when either base is N; one byte permute looks it up
-                const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | ((Tw | Qw) & 0x04040404u);
-                sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
-              } else if (!generic) {
-                const uint32_t eq = eqz8(Tw ^ Qw);
-                const uint32_t nn = eqz8(Tw ^ m14) | eqz8(Qw ^ m14);
-                sn = sel(bmask(eq), mch4, mis4);
-                sn = sel(bmask(nn), N4, sn);
-              } else {
-                sn = 0;
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                  const int tc = (Tw >> (8 * b)) & 0xff, qc = (Qw >> (8 * b)) & 0xff;
-                  uint32_t v = (uint32_t)(uint8_t)P.mat[(tc * P.m + qc) & 255];
-                  if (!D2) v = (v + P.c_qe2) & 0xffu;
-                  sn |= v << (8 * b);
-                }
-              }
-              // only the word holding st0 (slot 0) and the one holding fend (slot wf / G) are
-              // partly outside the stores; every other word takes all four scores
-              uint32_t wm = 0xffffffffu;
-              if (i == 0) {
-                const int lo = st0 - p0;
-                if (lo > 0) wm <<= 8 * lo;
-              }
-              if (i == wf / G) {  // group-uniform
-                const int hi = fend - p0;
-                if (hi < 3) wm &= 0xffffffffu >> (8 * (3 - hi));
-              }
+              // lanes with t | q <= 4 (codes 0-3, or N = 4 against 0 or N): the lane index
+              // (t ^ q) & 3 | (t | q) & 4 is 0 for a match, 1-3 for a mismatch and 4 for N, and
+              // one byte permute looks it up; any other lane (t | q >= 5) marks the word bad
+              const uint32_t tq = Tw | Qw;
+              const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | (tq & 0x04040404u);
+              const uint32_t sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
+              bad |= tq | (tq + 0x03030303u);  // bits 3-7 of a lane set iff t | q >= 5
+              const int lo = st0 - p0, hi = fend - p0;
+              const uint32_t wm = (lo > 0 ? 0xffffffffu << (8 * lo) : 0xffffffffu) &
+                                  (hi < 3 ? 0xffffffffu >> (8 * (3 - hi)) : 0xffffffffu);
               S[i] = (S[i] & ~wm) | (sn & wm);
+            }
+          }
+          if (bad & 0xf8f8f8f8u) {  // group-divergent only on inputs with other codes
+#pragma unroll
+            for (int i = 0; i <= K; ++i) {
+              const int p0 = base + 4 * (k + G * i);
+              if (p0 + 3 >= st0 && p0 <= fend) {
+                const int idx0 = r - p0 - 3;
+                const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
+                const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
+                const uint32_t Tw = TW[i];
+                uint32_t sn;
+                if (!generic) {
+                  const uint32_t eq = eqz8(Tw ^ Qw);
+                  const uint32_t nn = eqz8(Tw ^ m14) | eqz8(Qw ^ m14);
+                  sn = sel(bmask(eq), mch4, mis4);
+                  sn = sel(bmask(nn), N4, sn);
+                } else {
+                  sn = 0;
+#pragma unroll
+                  for (int b = 0; b < 4; ++b) {
+                    const int tc = (Tw >> (8 * b)) & 0xff, qc = (Qw >> (8 * b)) & 0xff;
+                    uint32_t v = (uint32_t)(uint8_t)P.mat[(tc * P.m + qc) & 255];
+                    if (!D2) v = (v + P.c_qe2) & 0xffu;
+                    sn |= v << (8 * b);
+                  }
+                }
+                const int lo = st0 - p0, hi = fend - p0;
+                const uint32_t wm = (lo > 0 ? 0xffffffffu << (8 * lo) : 0xffffffffu) &
+                                    (hi < 3 ? 0xffffffffu >> (8 * (3 - hi)) : 0xffffffffu);
+                S[i] = (S[i] & ~wm) | (sn & wm);
+              }
             }
           }
         }

@@ -63,6 +63,28 @@ def test_emulated_lockstep_groups_and_work_counter(emu):
         assert {f: int(res[i][f]) for f in LL_FIELDS} == exp, i
 
 
+def test_emulated_codes_above_n(emu):
+    """Bytes 5-7 in the sequences take the general score comparisons, not the nt4 lookup."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(23)
+    mat = np.array([2 if i // 5 == i % 5 else -4 for i in range(25)], np.int8)
+    mat[20:25] = -1
+    mat[4::5] = -1
+    for dual, flag in ((0, 0x42), (1, 0x40), (0, 0x00)):
+        qs, ts = [], []
+        for _ in range(8):
+            base = rng.integers(0, 4, 70).astype(np.uint8)
+            q, t = base[: int(rng.integers(20, 70))].copy(), base[: int(rng.integers(20, 70))].copy()
+            q[rng.random(len(q)) < 0.2] = rng.integers(4, 8)
+            t[rng.random(len(t)) < 0.1] = rng.integers(4, 8)
+            qs.append(q), ts.append(t)
+        res, cig = emu.ext(dual, 5, mat, 6, 1, 20, 1, qs, ts, 7, 100, 5, flag)
+        for i in range(len(qs)):
+            exp, _ = O.extz(dual, qs[i], ts[i], 5, mat, 6, 1, 20 if dual else 6, 1, 7, 100, 5, flag)
+            assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, i)
+            assert cig[i] == exp["cigar"], (dual, flag, i)
+
+
 def test_emulated_wide_band_shapes(emu):
     """Wide bands select the 16- and 32-thread shapes."""
     from minibwa_gb300 import synth

@@ -129,6 +129,34 @@ def test_random_cases_per_call_against_oracle(built):
         K.free_extz(ez)
 
 
+def test_codes_above_n_and_random_matrices(built):
+    """Bytes 5-7 (neither a base nor N) compare by equality in the reference's non-generic scores
+    (ksw2_extz2_sse.c:117-131); any matrix, not only match/mismatch/N ones."""
+    import minibwa_gb300.lib as K
+    rng = np.random.default_rng(17)
+    for it in range(400):
+        c = _rand_case(rng)
+        if not c["dual"]:
+            c["q2"], c["e2"] = c["q"], c["e"]
+        if not c["flag"] & 0x04:
+            for s in ("query", "target"):
+                x = c[s]
+                hit = rng.random(len(x)) < 0.1
+                x[hit] = rng.integers(0, 8, hit.sum())
+        if rng.random() < 0.5:
+            a = int(c["mat"][0])
+            mat = rng.integers(-8, a + 1, 25).astype(np.int8)
+            mat[0] = a
+            c["mat"] = mat
+        ez = _dropin(c)
+        got = ez.fields()
+        exp, _ = O.extz(c["dual"], c["query"], c["target"], c["m"], c["mat"], c["q"], c["e"], c["q2"], c["e2"],
+                        c["w"], c["zdrop"], c["end_bonus"], c["flag"])
+        for f in EXT_FIELDS + ["cigar"]:
+            assert got[f] == exp[f], (it, f, got[f], exp[f])
+        K.free_extz(ez)
+
+
 def _batch_vs_oracle(ctx, p, nthreads=8):
     res, cig = ctx.ext_batch(p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf)
     ores, ocig = O.ext_batch("orc", p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf, nthreads)
