@@ -73,6 +73,13 @@ struct PinBuf {
 };
 
 // ---------------------------------------------------------------- context
+// Chunks of a one-shot call in flight at once.  Preparing a chunk on the host takes about as
+// long as the device runs one, and with two in flight the host waited on the previous chunk
+// of the same sub-context: 1,000,000 pairs of 100-300 nt took 150.7 ms end to end in chunks of
+// 32,768 two deep, 143.2 ms three deep and 136.7 ms in chunks of 16,384 three deep (the device
+// alone: 133.6 ms).
+static const int kOneShotDepth = 3;
+
 struct ksw2g_ctx {
   int device = 0;
   cudaStream_t st = nullptr;
@@ -94,10 +101,10 @@ struct ksw2g_ctx {
   int rs_launches = 0;                          // kernels the last rescue call launched
   double rs_ms[3] = {0, 0, 0};                  // its stages' wall time: prefilter, ksw_ll, extz2
   ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
-  // two sub-contexts (own stream and traceback pool, half the budget each) that the
-  // one-shot extension call alternates between, so the host prepares one chunk
-  // while the device runs the previous one
-  ksw2g_ctx *sub[2] = {nullptr, nullptr};
+  // sub-contexts (own stream and traceback pool, half the budget each) that the
+  // one-shot calls rotate their chunks through, so the host prepares the next chunks
+  // while the device runs the earlier ones
+  ksw2g_ctx *sub[kOneShotDepth] = {};
 };
 
 // ---------------------------------------------------------------- batches

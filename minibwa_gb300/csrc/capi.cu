@@ -582,17 +582,17 @@ extern "C" int ksw2g_ext_fetch(ksw2g_ctx_t *c, ksw2g_batch_t *b, ksw2g_ext_resul
 }
 
 // One-shot extension batches of more than kChunkJobs jobs run as chunks that
-// alternate between two sub-contexts: while the device runs chunk i, the host
-// prepares chunk i+1 (job table, wave plan, uploads) on the other stream.
+// rotate through kOneShotDepth sub-contexts: while the device runs chunks i and i+1,
+// the host prepares chunk i+2 (job table, wave plan, uploads) on a third stream.
 // Each chunk's CIGARs are appended to the caller's buffer as the chunk
 // completes, and its results' cigar_off are shifted to match.  Small chunks keep
 // the gaps between them short: on 1,000,000 pairs of 100-300 nt the call takes
-// 197 ms with chunks of 32,768 jobs, 207 ms with 131,072 and 218 ms with 500,000.
+// 136.7 ms with chunks of 16,384 jobs and 143.2 ms with 32,768.
 // Long pairs want larger chunks, because every chunk ends with the tail of its own
 // longest pair: 200,000 pairs of 0.5-30 kb at w=500 run 14% slower in chunks of
 // 32,768 than of 131,072.  So batches whose pairs average more than kLongCells
 // band cells use the larger chunk.
-static const int kChunkJobs = 32768, kChunkJobsLong = 131072;
+static const int kChunkJobs = 16384, kChunkJobsLong = 131072;
 
 static int chunk_jobs(int n, const ksw2g_job_t *jobs) {
   double cells = 0;
@@ -612,7 +612,7 @@ static int sub_ctx(ksw2g_ctx *c, int i, ksw2g_ctx **out) {
     c->sub[i]->scratch = new ksw2g_batch;
   }
   c->sub[i]->tb_budget = std::max<int64_t>(c->tb_budget / 2, 1 << 20);
-  c->sub[i]->wave_div = 1;  // each sub-context runs one stream; the two alternate chunks
+  c->sub[i]->wave_div = 1;  // each sub-context runs one stream; the chunks rotate through them
   *out = c->sub[i];
   return 0;
 }
@@ -626,12 +626,13 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
   const int cj_jobs = chunk_jobs(n, jobs);
   const int nch = (n + cj_jobs - 1) / cj_jobs;
   const int per = (n + nch - 1) / nch;
-  ksw2g_ctx *sc[2];
+  ksw2g_ctx *sc[kOneShotDepth];
   int rc;
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < kOneShotDepth; ++i)
     if ((rc = sub_ctx(c, i, &sc[i]))) return rc;
   int64_t used = 0;
-  int pending[2] = {-1, -1};  // chunk index in flight on each sub-context
+  int pending[kOneShotDepth];  // chunk index in flight on each sub-context
+  std::fill(pending, pending + kOneShotDepth, -1);
   c->oneshot_launches = 0;
   auto finish = [&](int s) -> int {
     const int ch = pending[s];
@@ -659,7 +660,7 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
     return 0;
   };
   for (int ch = 0; ch < nch && !rc; ++ch) {
-    const int s = ch & 1;
+    const int s = ch % kOneShotDepth;
     if ((rc = finish(s))) break;
     const int j0 = ch * per, nj = std::min(per, n - j0);
     ksw2g_ctx *x = sc[s];
@@ -697,12 +698,10 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
     pending[s] = ch;
   }
   // drain in chunk order (the CIGAR buffer is filled in chunk order)
-  for (int k = 0; k < 2 && !rc; ++k) {
-    int s = pending[0] >= 0 && (pending[1] < 0 || pending[0] < pending[1]) ? 0 : 1;
-    rc = finish(s);
-  }
+  for (int ch = nch - kOneShotDepth; ch < nch && !rc; ++ch)
+    if (ch >= 0) rc = finish(ch % kOneShotDepth);
   if (rc) {
-    for (int s = 0; s < 2; ++s) cudaStreamSynchronize(sc[s]->st);
+    for (int s = 0; s < kOneShotDepth; ++s) cudaStreamSynchronize(sc[s]->st);
     return rc;
   }
   if (cigar_used) *cigar_used = used;
@@ -1056,8 +1055,8 @@ extern "C" int ksw2g_ll_fetch(ksw2g_ctx_t *c, ksw2g_batch_t *b, ksw2g_ll_result_
   return 0;
 }
 
-// One-shot ksw_ll batches of more than kLLChunkJobs jobs run as chunks that alternate
-// between the two sub-contexts, so each chunk's uploads overlap the previous chunk's DP.
+// One-shot ksw_ll batches of more than kLLChunkJobs jobs run as chunks that rotate
+// through the sub-contexts, so each chunk's uploads overlap the earlier chunks' DP.
 static const int kLLChunkJobs = 262144;
 
 static int ll_batch_chunked(ksw2g_ctx *c, int size, int m, const int8_t *mat, int gapo, int gape, int n,
@@ -1065,11 +1064,12 @@ static int ll_batch_chunked(ksw2g_ctx *c, int size, int m, const int8_t *mat, in
                             int64_t tbuf_len, ksw2g_ll_result_t *res) {
   const int nch = (n + kLLChunkJobs - 1) / kLLChunkJobs;
   const int per = (n + nch - 1) / nch;
-  ksw2g_ctx *sc[2];
+  ksw2g_ctx *sc[kOneShotDepth];
   int rc;
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < kOneShotDepth; ++i)
     if ((rc = sub_ctx(c, i, &sc[i]))) return rc;
-  int pending[2] = {-1, -1};
+  int pending[kOneShotDepth];
+  std::fill(pending, pending + kOneShotDepth, -1);
   auto finish = [&](int s) -> int {
     const int ch = pending[s];
     if (ch < 0) return 0;
@@ -1077,7 +1077,7 @@ static int ll_batch_chunked(ksw2g_ctx *c, int size, int m, const int8_t *mat, in
     return ksw2g_ll_fetch(sc[s], sc[s]->scratch, res ? res + (size_t)ch * per : nullptr);
   };
   for (int ch = 0; ch < nch && !rc; ++ch) {
-    const int s = ch & 1;
+    const int s = ch % kOneShotDepth;
     if ((rc = finish(s))) break;
     const int j0 = ch * per, nj = std::min(per, n - j0);
     int64_t qlo = qbuf_len, qhi = 0, tlo = tbuf_len, thi = 0;
@@ -1103,9 +1103,10 @@ static int ll_batch_chunked(ksw2g_ctx *c, int size, int m, const int8_t *mat, in
     if ((rc = ll_run(x, x->scratch))) break;
     pending[s] = ch;
   }
-  for (int k = 0; k < 2 && !rc; ++k) rc = finish(pending[0] >= 0 && (pending[1] < 0 || pending[0] < pending[1]) ? 0 : 1);
+  for (int ch = nch - kOneShotDepth; ch < nch && !rc; ++ch)
+    if (ch >= 0) rc = finish(ch % kOneShotDepth);
   if (rc)
-    for (int s = 0; s < 2; ++s) cudaStreamSynchronize(sc[s]->st);
+    for (int s = 0; s < kOneShotDepth; ++s) cudaStreamSynchronize(sc[s]->st);
   return rc;
 }
 
