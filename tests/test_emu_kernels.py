@@ -85,6 +85,28 @@ def test_emulated_codes_above_n(emu):
             assert cig[i] == exp["cigar"], (dual, flag, i)
 
 
+def test_emulated_one_cell_bands(emu):
+    """Narrow bands against short targets pinch to one cell on consecutive anti-diagonals; H[en0]
+    then reads H[en0-1] of a cell that already left the band (its last value, as the reference's
+    array holds it), which the kernel carries as a scalar."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(29)
+    mat = np.array([3 if i // 5 == i % 5 else -4 for i in range(25)], np.int8)
+    mat[20:25] = -1
+    mat[4::5] = -1
+    qs = [rng.integers(0, 4, 46).astype(np.uint8) for _ in range(4)]
+    ts = [q[:tl].copy() for q, tl in zip(qs, (1, 2, 3, 5))]
+    for dual in (0, 1):
+        for flag in (0x00, 0x01, 0x40, 0x42):
+            for w in (2, 3, 4, 6, 10):
+                res, cig = emu.ext(dual, 5, mat, 3, 1, 20, 1, qs, ts, w, -1, 5, flag)
+                for i in range(len(qs)):
+                    exp, _ = O.extz(dual, qs[i], ts[i], 5, mat, 3, 1, 20 if dual else 3, 1, w, -1, 5, flag)
+                    got = {f: int(res[i][f]) for f in EXT_FIELDS}
+                    assert got == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, w, i)
+                    assert cig[i] == exp["cigar"], (dual, flag, w, i)
+
+
 def test_emulated_wide_band_shapes(emu):
     """Wide bands select the 16- and 32-thread shapes."""
     from minibwa_gb300 import synth
