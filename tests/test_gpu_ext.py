@@ -157,6 +157,30 @@ def test_codes_above_n_and_random_matrices(built):
         K.free_extz(ez)
 
 
+def test_one_cell_bands(ctx):
+    """Bands that pinch to one cell on consecutive anti-diagonals read H of a cell that already
+    left the band; batched, against the checker."""
+    rng = np.random.default_rng(29)
+    mat = np.array([3 if i // 5 == i % 5 else -4 for i in range(25)], np.int8)
+    mat[20:25] = -1
+    mat[4::5] = -1
+    qs = [rng.integers(0, 4, 46).astype(np.uint8) for _ in range(4)]
+    ts = [q[:tl].copy() for q, tl in zip(qs, (1, 2, 3, 5))]
+    qbuf, tbuf = np.concatenate(qs), np.concatenate(ts)
+    for dual in (0, 1):
+        for flag in (0x00, 0x01, 0x40, 0x42):
+            for w in (2, 3, 4, 6, 10):
+                jobs = np.zeros(4, O.ORC_JOB)
+                jobs["qoff"] = np.cumsum([0] + [len(q) for q in qs[:-1]])
+                jobs["toff"] = np.cumsum([0] + [len(t) for t in ts[:-1]])
+                jobs["qlen"], jobs["tlen"] = [len(q) for q in qs], [len(t) for t in ts]
+                jobs["w"], jobs["zdrop"], jobs["end_bonus"], jobs["flag"] = w, -1, 5, flag
+                q2 = 20 if dual else 3
+                res, cig = ctx.ext_batch(dual, 5, mat, 3, 1, q2, 1, jobs, qbuf, tbuf)
+                ores, ocig = O.ext_batch("orc", dual, 5, mat, 3, 1, q2, 1, jobs, qbuf, tbuf, 1)
+                compare_ext(res, cig, ores, ocig)
+
+
 def _batch_vs_oracle(ctx, p, nthreads=8):
     res, cig = ctx.ext_batch(p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf)
     ores, ocig = O.ext_batch("orc", p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf, nthreads)
