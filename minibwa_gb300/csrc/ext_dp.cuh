@@ -264,7 +264,8 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             // at an index clamped into the range the words inside read, and its byte mask is 0.
             // The extra slot K is mostly outside and keeps the branch.
             if (i < K || (p0 + 3 >= st0 && p0 <= fend)) {
-              const int idx0 = min(max(r - p0 - 3, r - fend - 3), r - st0);
+              // words of slots 1.. start above st0 (the window starts at st0's 16-cell block)
+              const int idx0 = i == 0 ? min(max(r - p0 - 3, r - fend - 3), r - st0) : max(r - p0 - 3, r - fend - 3);
               const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
               const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
               const uint32_t Tw = TW[i];
@@ -275,7 +276,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | (tq & 0x04040404u);
               const uint32_t sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
               bad |= tq | (tq + 0x03030303u);  // bits 3-7 of a lane set iff t | q >= 5
-              const int lo = st0 - p0, hi = fend - p0;
+              const int lo = i == 0 ? st0 - p0 : 0, hi = fend - p0;
               const uint32_t wm = lo > 3 || hi < 0 ? 0u
                                   : (lo > 0 ? 0xffffffffu << (8 * lo) : 0xffffffffu) &
                                         (hi < 3 ? 0xffffffffu >> (8 * (3 - hi)) : 0xffffffffu);
