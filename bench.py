@@ -35,15 +35,18 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Lane operations the reference SSE code spends per nominal cell (one 32-bit instruction carries
-# four byte lanes or two 16-bit lanes):
-#  extd2 with CIGAR: 54 byte-lane ops per 16-cell block (ksw2_extd2_sse.c:183-265) + 6 for the
-#    substitution scores (extd2:157-172), and 6 int32 lane ops of the exact max (extd2:315-345);
-#  extz2 with CIGAR: 29 + 6 byte-lane ops (ksw2_extz2_sse.c:117-136,163-188) and 5 int32 (extz2:216-243);
-#  ksw_ll i16: 10 int16-lane ops per cell (ksw2_ll_sse.c:265-286), lazy-F passes not counted.
+# 32-bit integer operations per nominal cell, from the reference SSE code's lane operations:
+# byte-lane ops count 1/4 (four byte lanes per 32-bit op), int16-lane ops 1/2, and int32-lane ops 1
+# (one lane per 32-bit op):
+#  extd2 with CIGAR: 54 byte-lane ops per cell of a 16-cell block (ksw2_extd2_sse.c:183-265) + 6 for
+#    the substitution scores (extd2:157-172), and 6 int32 lane ops of the exact max (extd2:315-345):
+#    60/4 + 6 = 21;
+#  extz2 with CIGAR: 29 + 6 byte-lane ops (ksw2_extz2_sse.c:117-136,163-188) and 5 int32 (extz2:216-243):
+#    35/4 + 5 = 13.75;
+#  ksw_ll i16: 10 int16-lane ops per cell (ksw2_ll_sse.c:265-286), lazy-F passes not counted: 10/2 = 5.
 OPS_PER_CELL = {
-    "extd2": (54 + 6) / 4 + 6 / 4,
-    "extz2": (29 + 6) / 4 + 5 / 4,
+    "extd2": (54 + 6) / 4 + 6,
+    "extz2": (29 + 6) / 4 + 5,
     "ll_i16": 10 / 2,
 }
 # DRAM bytes per nominal cell of the DP kernel, from ncu (dram__bytes_read.sum + dram__bytes_write.sum
@@ -176,24 +179,30 @@ class ClockSampler:
 class Workload:
     """The inputs of one benchmark configuration and how to run them."""
 
-    def __init__(self, name, args, rank):
+    def __init__(self, name, args, rank, sizes_only=False, prefix=None):
         from minibwa_gb300 import synth
         self.name, self.desc = name, WORKLOADS[name]
         seed_shift = rank * 1000
         n = args.pairs
         if name == "cfg1":
-            self.sets = [synth.config1(n or 1000000, seed=synth.SEED + 1 + seed_shift)]
+            spec = [(synth.config1, n or 1000000, synth.SEED + 1)]
         elif name == "cfg0":
-            self.sets = [synth.config0(n or 20000, seed=synth.SEED + seed_shift)]
+            spec = [(synth.config0, n or 20000, synth.SEED)]
         elif name == "cfg2":
             nl = (n or 1200000) // 6
-            self.sets = [synth.config2_long(nl, seed=synth.SEED + 2 + seed_shift),
-                         synth.config2_short(nl * 5, seed=synth.SEED + 3 + seed_shift)]
+            spec = [(synth.config2_long, nl, synth.SEED + 2), (synth.config2_short, nl * 5, synth.SEED + 3)]
         else:
-            self.sets = [synth.config3(n or 2000000, seed=synth.SEED + 4 + seed_shift)]
+            spec = [(synth.config3, n or 2000000, synth.SEED + 4)]
+        self.set_sizes = [k for _, k, _ in spec]
         self.ll = name == "cfg3"
         self.metric = "jobs/s" if self.ll else "alignments/s"
         self.unit = "jobs/s" if self.ll else "aln/s"
+        if sizes_only:
+            self.sets, self.n = [], sum(self.set_sizes)
+            return
+        if prefix is not None:  # the first units of every set (the generator is sequential per set)
+            spec = [(f, p, sd) for (f, _, sd), p in zip(spec, prefix)]
+        self.sets = [f(k, seed=sd + seed_shift) for f, k, sd in spec]
         self.kind = "ll_i16" if self.ll else ("extd2" if self.sets[0].dual else "extz2")
         self.n = sum(len(s) for s in self.sets)
 
@@ -215,29 +224,75 @@ def cells_of(s, res):
 
 
 def cpu_baseline(w, sample, reference_preferred=True):
-    """Time the CPU implementation on a bounded sample of the same units with all host threads."""
+    """Time the CPU implementation on a bounded sample of the same units with all host threads:
+    the reference's own ksw2 SIMD code (oracle/_ref, compiled from the reference's sources, jobs
+    spread by its kt_for) when it could be built, else the scalar restatement.  Returns (baseline
+    dict, seconds, per-set outputs), the outputs being (results, CIGAR words) of the first units of
+    every set."""
     from oracle import oracle as O
     kind = "reference" if (reference_preferred and O.have_ref()) else "port"
     which = "ref" if kind == "reference" else "orc"
     threads = os.cpu_count() or 1
     # the sample keeps the workload's mix: the same fraction of every set
     frac = min(1.0, sample / w.n)
-    n_done, t0 = 0, time.perf_counter()
+    subs = []
     for s in w.sets:
         k = max(1, int(round(len(s) * frac)))
-        sub = s.subset(np.arange(k))
+        subs.append(s.subset(np.arange(k)))
+    outs, n_done = [], 0
+    t0 = time.perf_counter()
+    for sub in subs:
         if hasattr(sub, "size"):
-            O.ll_batch(which, sub.size, 5, sub.mat, sub.gapo, sub.gape, sub.jobs, sub.qbuf, sub.tbuf, threads)
+            outs.append((O.ll_batch(which, sub.size, 5, sub.mat, sub.gapo, sub.gape, sub.jobs, sub.qbuf, sub.tbuf,
+                                    threads), None))
         else:
-            O.ext_batch(which, sub.dual, 5, sub.mat, sub.q, sub.e, sub.q2, sub.e2, sub.jobs, sub.qbuf, sub.tbuf,
-                        threads)
-        n_done += k
+            outs.append(O.ext_batch(which, sub.dual, 5, sub.mat, sub.q, sub.e, sub.q2, sub.e2, sub.jobs, sub.qbuf,
+                                    sub.tbuf, threads))
+        n_done += len(sub)
     dt = time.perf_counter() - t0
-    return {"value": n_done / dt, "unit": w.unit, "cores": threads, "kind": kind,
-            "sample": f"first {n_done} units of the workload (same mix), {threads} threads, {dt:.2f} s wall"}, dt
+    what = ("the reference's ksw2 SIMD functions (NEON via s2n-lite.h on Arm, SSE4 on x86-64) compiled from its "
+            "sources, jobs spread over the threads by its kt_for" if kind == "reference" else
+            "the scalar C restatement of the reference (the reference's sources were not available)")
+    return ({"value": n_done / dt, "unit": w.unit, "cores": threads, "kind": kind,
+             "sample": f"first {n_done} units of the benchmarked set (same seed, same mix), {threads} threads, "
+                       f"{dt:.2f} s wall; {what}"}, dt, outs)
 
 
-DEFAULT_SAMPLE = {"cfg1": 40000, "cfg0": 20000, "cfg2": 6000, "cfg3": 40000, "rescue": 60000}
+def parity_vs_cpu(w, results, outs, kind):
+    """Compare the GPU's results on the first units of every set with the CPU run's outputs,
+    field by field and CIGAR by CIGAR."""
+    fields_ext = ("score", "max", "max_q", "max_t", "mqe", "mqe_t", "mte", "mte_q", "zdropped", "reach_end",
+                  "n_cigar")
+    n, bad = 0, 0
+    for s, r, (cres, ccig) in zip(w.sets, results, outs):
+        k = len(cres)
+        n += k
+        if hasattr(s, "size"):
+            ok = np.ones(k, bool)
+            for f in ("score", "te", "qe", "score2", "te2"):
+                ok &= r[f][:k] == cres[f]
+        else:
+            gres, gcig = r
+            ok = np.ones(k, bool)
+            for f in fields_ext:
+                ok &= gres[f][:k] == cres[f]
+            for i in np.nonzero(ok)[0]:
+                m = int(gres["n_cigar"][i])
+                a, b = int(gres["cigar_off"][i]), int(cres["cigar_off"][i])
+                if m and not np.array_equal(gcig[a:a + m], ccig[b:b + m]):
+                    ok[i] = False
+        bad += int((~ok).sum())
+    return {"against": kind, "units": n, "mismatches": bad, "equal": bad == 0}
+
+
+DEFAULT_SAMPLE = {"cfg1": 100000, "cfg0": 20000, "cfg2": 6000, "cfg3": 100000, "rescue": 60000}
+
+
+def workload_config(name, n, world):
+    """The config dict of a workload; both arms print the same one."""
+    return {"workload": WORKLOADS[name], "units_per_gpu": n, "parallelism": f"replicas x{world}",
+            "graph": name == "cfg2",
+            "l2": "inputs and traceback rows exceed the 129 MB L2 on every step (no flush needed)"}
 
 
 def rescue_cpu_baseline(ref, jobs, qbuf, sample):
@@ -379,29 +434,27 @@ def run_reference(args, rank, world):
                           "cpu_baseline": cb, "e2e": {"value": v, "unit": "candidates/s", "h2d_bytes_per_step": 0,
                                                       "d2h_bytes_per_step": 0}}), flush=True)
         return
-    w = Workload(args.workload, args, 0) if args.workload != "cfg1" else None
-    if w is None:
-        from minibwa_gb300 import synth
-
-        class _W:
-            pass
-        w = _W()
-        w.sets = [synth.config1(max(args.cpu_sample or DEFAULT_SAMPLE["cfg1"], 1000))]
-        w.n, w.unit, w.metric, w.desc = len(w.sets[0]), "aln/s", "alignments/s", WORKLOADS["cfg1"]
+    # The benchmarked sets are generated by one sequential splitmix64 stream per set, so their first
+    # units do not depend on the set size: generate only the sample's prefix of each set.
     sample = args.cpu_sample or DEFAULT_SAMPLE[args.workload]
+    full = Workload(args.workload, args, 0, sizes_only=True)
+    frac = min(1.0, sample / full.n)
+    args_s = argparse.Namespace(**vars(args))
+    w = Workload(args.workload, args_s, 0, prefix=[max(1, int(round(n * frac))) for n in full.set_sizes])
     for _ in range(args.warmup):
-        cpu_baseline(w, max(1, sample // 20))
+        cpu_baseline(w, max(1, w.n // 20))
     times = []
     for _ in range(args.steps):
-        cb, dt = cpu_baseline(w, sample)
+        cb, dt, _ = cpu_baseline(w, w.n)
         times.append(dt)
-    v = len(times) * sample / sum(times)
+    v = len(times) * w.n / sum(times)
     cb["value"] = v
     line = {"impl": "reference", "metric": w.metric, "value": v, "unit": w.unit, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int16" if args.workload == "cfg3" else "int8",
-            "data": "synthetic (seeded splitmix64)", "config": {"workload": w.desc, "units_per_step": sample},
+            "data": "synthetic (seeded splitmix64, no public dataset)",
+            "config": workload_config(args.workload, full.n, args.gpus),
             "cpu_baseline": cb, "e2e": {"value": v, "unit": w.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -552,19 +605,19 @@ def main():
         h2d += len(s.qbuf) + len(s.tbuf) + s.jobs.nbytes
         d2h += r.nbytes + 4 * int(u.value)
 
-    cb = None
+    cb = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb, _ = cpu_baseline(w, args.cpu_sample or DEFAULT_SAMPLE[args.workload])
+        cb, _, outs = cpu_baseline(w, args.cpu_sample or DEFAULT_SAMPLE[args.workload])
+        parity = parity_vs_cpu(w, results, outs, cb["kind"])
 
     if rank == 0:
-        l2note = ("inputs and traceback rows (%.1f GB per step) exceed the 129 MB L2" % (alg_bytes / 1e9))
         line = {
             "metric": w.metric, "value": value, "unit": w.unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int16" if w.ll else "int8",
             "data": "synthetic (seeded splitmix64, no public dataset)",
-            "config": {"workload": w.desc, "units_per_gpu": w.n, "l2": l2note, "parallelism": f"replicas x{world}",
-                       "graph": graph is not None},
+            "config": workload_config(args.workload, w.n, world),
+            "bytes_per_step": alg_bytes,
             "gcups": tot_cells / (ms * 1e-3) / 1e9,
             "cells_per_step": tot_cells,
             "gpu_launches": launches_per_step * args.steps,
@@ -583,6 +636,7 @@ def main():
         }
         if cb:
             line["cpu_baseline"] = cb
+            line["parity_vs_cpu"] = parity
         print(json.dumps(line), flush=True)
     if graph is not None:
         graph.close()

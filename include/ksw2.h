@@ -1,8 +1,14 @@
 /*
  * ksw2.h -- drop-in C interface of the GB300 implementation of minibwa's ksw2
  * hot path.  Link libksw2gpu.so in place of ksw2_extz2_sse.o,
- * ksw2_extd2_sse.o and ksw2_ll_sse.o; callers (align.c, pe.c) compile
- * unchanged against this header.
+ * ksw2_extd2_sse.o and ksw2_ll_sse.o.
+ *
+ * This header declares only the six entry points the library replaces and
+ * the types and flags they take.  It is not a substitute for minibwa's own
+ * ksw2.h: callers (align.c, pe.c) keep compiling against that file, whose
+ * static inline helpers (ksw_push_cigar, ksw_backtrack, ksw_reset_extz,
+ * ksw_apply_zdrop, ksw_gen_nt4_mat) and further flags (KSW_CIGAR_N_SKIP,
+ * KSW_EZ_SPLICE_*, KSW_SPSC_OFFSET) stay compiled into them.
  *
  * Every declaration below has the signature, argument meaning and result
  * layout of the reference declaration it replaces (reference file ksw2.h).

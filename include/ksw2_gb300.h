@@ -233,7 +233,11 @@ int ksw2g_ext_set_shape(int dual, int mode, int ncol_lo, int ncol_hi, int shape)
  *           layout: every sequence starts 16-byte aligned with at least 32 zero
  *           bytes before it and zeros after it up to the next 16-byte boundary
  *           plus 32 bytes.  All jobs of one call use the same gap mode
- *           (score-only, left-aligned or right-aligned CIGAR).
+ *           (score-only, left-aligned or right-aligned CIGAR).  The host copies
+ *           the array on the stream, so it must stay unchanged until the stream
+ *           has passed the call.
+ *  arena_len bytes of d_arena; a job whose sequence plus its padding ends past
+ *           it is rejected (KSW2G_E_ARG) before any device work.
  *  d_res    device array of n_jobs results (as ksw2g_ext_batch fills them).
  *  d_cigar  device array of cigar_cap words; cigar_cap must be at least the sum
  *           of qlen+tlen+1 over the jobs when CIGARs are requested.
@@ -243,13 +247,15 @@ int ksw2g_ext_set_shape(int dual, int mode, int ncol_lo, int ncol_hi, int shape)
  * scratch (traceback rows, plus 64 bytes per job and at most 1 KiB) exceeds
  * KSW2G_NOALLOC_SCRATCH_BYTES.  The first call on each device looks up the
  * array's device address; make that first call before any stream capture.
+ * The address is kept for the life of the process, so calls after a
+ * cudaDeviceReset of that device are not supported.
  * Every call reuses the same array and clears its counters at the start:
  * calls whose work overlaps on the GPU (different streams, or another host
  * thread) race on it and must be serialised by the caller.
  */
 #define KSW2G_NOALLOC_SCRATCH_BYTES (64ll << 20)
 int ksw2g_ext_noalloc(int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e, int8_t q2, int8_t e2,
-					  int n_jobs, const ksw2g_job_t *jobs, const uint8_t *d_arena,
+					  int n_jobs, const ksw2g_job_t *jobs, const uint8_t *d_arena, int64_t arena_len,
 					  ksw2g_ext_result_t *d_res, uint32_t *d_cigar, int64_t cigar_cap, void *stream);
 
 /* ---- serving engine: continuous batching over a fixed traceback budget ----
@@ -284,6 +290,11 @@ int ksw2g_server_launch_stats(ksw2g_server_t *server, int64_t *launches, int64_t
  * Smaller launches finish sooner, larger ones fill the GPU: a latency /
  * throughput knob. */
 int ksw2g_server_set_merge(ksw2g_server_t *server, int max_jobs);
+
+/* Failure injection for host-side tests (no counterpart in the reference): the nth device
+ * buffer growth after this call fails as if the device had no memory left, so the call that
+ * needed it returns KSW2G_E_NOMEM; 0 turns the injection off.  Nothing runs on the GPU for it. */
+void ksw2g_debug_fail_device_alloc(int nth);
 
 /* Measured 32-bit integer instruction throughput of the device (lane-ops per
  * second), the denominator of the DP kernels' integer-pipe roofline. */

@@ -12,6 +12,9 @@
 
 namespace ksw2g {
 int report_error(int code, const char *msg);
+// Failure injection for host-side tests: when positive, the n-th next device buffer growth
+// fails as if the allocator had no memory left (ksw2g_debug_fail_device_alloc).
+bool take_injected_alloc_failure();
 }
 
 // ---------------------------------------------------------------- buffers
@@ -31,6 +34,7 @@ struct DevBuf {
     if (p) free_(p);
     p = nullptr, cap = 0;
     size_t c = n < 4096 ? 4096 : n + (st ? n / 2 : n / 8);
+    if (ksw2g::take_injected_alloc_failure()) return ksw2g::report_error(KSW2G_E_NOMEM, "device allocation failed (injected)");
     if (alloc_(&p, c) != cudaSuccess) {
       cudaGetLastError();
       if (alloc_(&p, n) != cudaSuccess) {

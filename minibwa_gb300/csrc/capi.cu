@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -83,9 +84,20 @@ static int set_err(int code, const char *fmt, ...) {
   } while (0)
 
 extern "C" const char *ksw2g_last_error(void) { return tl_err.c_str(); }
+
 namespace ksw2g {
 int report_error(int code, const char *msg) { return set_err(code, "%s", msg); }
+
+static std::atomic<int> g_fail_alloc{0};
+bool take_injected_alloc_failure() {
+  int n = g_fail_alloc.load(std::memory_order_relaxed);
+  while (n > 0)
+    if (g_fail_alloc.compare_exchange_weak(n, n - 1)) return n == 1;
+  return false;
+}
 }  // namespace ksw2g
+
+extern "C" void ksw2g_debug_fail_device_alloc(int nth) { ksw2g::g_fail_alloc.store(nth > 0 ? nth : 0); }
 
 extern "C" int ksw2g_ctx_create(int device, ksw2g_ctx_t **out) {
   if (!out) return set_err(KSW2G_E_ARG, "null output");

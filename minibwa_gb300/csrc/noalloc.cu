@@ -87,10 +87,10 @@ int fail(int code, const char *fmt, ...) {
 }  // namespace
 
 extern "C" int ksw2g_ext_noalloc(int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e, int8_t q2, int8_t e2,
-                                 int n_jobs, const ksw2g_job_t *jobs, const uint8_t *d_arena,
+                                 int n_jobs, const ksw2g_job_t *jobs, const uint8_t *d_arena, int64_t arena_len,
                                  ksw2g_ext_result_t *d_res, uint32_t *d_cigar, int64_t cigar_cap, void *stream) {
   using namespace ksw2g;
-  if (n_jobs < 0 || (n_jobs > 0 && (!jobs || !d_arena || !d_res)) || !mat)
+  if (n_jobs < 0 || (n_jobs > 0 && (!jobs || !d_arena || !d_res)) || !mat || arena_len < 0)
     return fail(KSW2G_E_ARG, "ksw2g_ext_noalloc: null or negative argument");
   if (n_jobs == 0) return 0;
   ksw2g_ext_params P;
@@ -105,6 +105,10 @@ extern "C" int ksw2g_ext_noalloc(int dual, int8_t m, const int8_t *mat, int8_t q
     if ((J.flag & KSW2G_GENERIC_SC) && m > 16) return fail(KSW2G_E_UNSUPPORTED, "GENERIC_SC needs m <= 16");
     if (J.qlen < 0 || J.tlen < 0 || J.qoff < 32 || J.toff < 32 || (J.qoff & 15) || (J.toff & 15))
       return fail(KSW2G_E_ARG, "ksw2g_ext_noalloc: job %d: offsets must be 16-aligned and >= 32 (padded arena)", i);
+    // the kernels read whole 16-byte blocks up to 32 bytes past a sequence's rounded end
+    if (J.qoff + (((int64_t)J.qlen + 15) & ~(int64_t)15) + 32 > arena_len ||
+        J.toff + (((int64_t)J.tlen + 15) & ~(int64_t)15) + 32 > arena_len)
+      return fail(KSW2G_E_ARG, "ksw2g_ext_noalloc: job %d: sequence plus its 32-byte padding ends past the arena", i);
     if (J.qlen > 0 && J.tlen > 0 && !P.skip_all) {
       const int nc = ext_ncol(J.qlen, J.tlen, J.w);
       max_nc = nc > max_nc ? nc : max_nc;

@@ -18,6 +18,7 @@
 // (qlen+tlen-1) anti-diagonals of n_col_*16 bytes each (ksw2_extz2_sse.c:84),
 // summed over the request.
 #include <cuda_runtime.h>
+#include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
@@ -217,6 +218,39 @@ int64_t ext_need(const Req *r, int64_t budget) {
   return f < budget ? f : budget;
 }
 
+// A request is checked in full when it is submitted, so that a bad one is refused on its own
+// instead of failing the merged launch it would join: every job inside its buffers, and no job
+// whose traceback rows alone exceed the engine's pool.
+template <typename J>
+int check_jobs(const J *jobs, int n, int64_t qlen, int64_t tlen) {
+  for (int i = 0; i < n; ++i)
+    if (jobs[i].qlen < 0 || jobs[i].tlen < 0 || jobs[i].qoff < 0 || jobs[i].toff < 0 ||
+        jobs[i].qoff + jobs[i].qlen > qlen || jobs[i].toff + jobs[i].tlen > tlen) {
+      char msg[96];
+      snprintf(msg, sizeof msg, "server: job %d: sequence out of buffer bounds", i);
+      return report_error(KSW2G_E_ARG, msg);
+    }
+  return 0;
+}
+
+int check_ext_request(const ksw2g_job_t *J, int n, int8_t m, int64_t qlen, int64_t tlen, int64_t pool) {
+  int rc = check_jobs(J, n, qlen, tlen);
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) {
+    if ((J[i].flag & KSW2G_GENERIC_SC) && m > 16) return report_error(KSW2G_E_UNSUPPORTED, "server: GENERIC_SC needs m <= 16");
+    if (J[i].qlen <= 0 || J[i].tlen <= 0 || ext_mode(J[i].flag) == 0) continue;
+    const int64_t f =
+        (((int64_t)(J[i].qlen + J[i].tlen - 1) * ext_ncol(J[i].qlen, J[i].tlen, J[i].w) * 16) + 15) & ~(int64_t)15;
+    if (f > pool) {
+      char msg[128];
+      snprintf(msg, sizeof msg, "server: job %d needs %lld traceback bytes, the engine's pool holds %lld", i,
+               (long long)f, (long long)pool);
+      return report_error(KSW2G_E_CAPACITY, msg);
+    }
+  }
+  return 0;
+}
+
 // Prepare (synchronous uploads on the slot's stream) and enqueue the run, the
 // result copies and the completion callback of a merged group.
 int launch_group(Slot *s) {
@@ -408,6 +442,7 @@ extern "C" int64_t ksw2g_server_submit_ext(ksw2g_server_t *S, int dual, int8_t m
                                            int64_t cigar_cap) {
   if (!S || !mat || n_jobs < 0 || (n_jobs > 0 && (!jobs || !res)) || m <= 0)
     return report_error(KSW2G_E_ARG, "server: bad request");
+  if (const int rc = check_ext_request(jobs, n_jobs, m, qbuf_len, tbuf_len, S->alloc.cap)) return rc;
   Req *r = new Req;
   r->kind = dual ? 1 : 0, r->n = n_jobs, r->m = m, r->q = q, r->e = e, r->q2 = q2, r->e2 = e2;
   r->mat.assign(mat, mat + m * m);
@@ -423,6 +458,7 @@ extern "C" int64_t ksw2g_server_submit_ll(ksw2g_server_t *S, int size, int m, co
                                           ksw2g_ll_result_t *res) {
   if (!S || !mat || n_jobs < 0 || (n_jobs > 0 && (!jobs || !res)) || m <= 0)
     return report_error(KSW2G_E_ARG, "server: bad request");
+  if (const int rc = check_jobs(jobs, n_jobs, qbuf_len, tbuf_len)) return rc;
   Req *r = new Req;
   r->kind = size > 1 ? 3 : 2, r->n = n_jobs, r->m = (int8_t)m, r->gapo = gapo, r->gape = gape;
   r->mat.assign(mat, mat + m * m);

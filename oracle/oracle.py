@@ -15,7 +15,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = os.environ.get("KSW2_REF_TREE", "/root/reference")
+# The reference's sources as `make stage` copies them (git-ignored; they travel with the working
+# tree to machines where the reference tree itself does not exist).
+STAGED_TREE = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "src")
 LIB_ORACLE = os.path.join(HERE, "liboracle.so")
 LIB_REF = os.path.join(HERE, "_ref", "libksw2ref.so")
 LIB_MBPE = os.path.join(HERE, "_ref", "libmbpe.so")
@@ -62,11 +64,37 @@ class OrcLL(C.Structure):
     _fields_ = [("score", C.c_int), ("te", C.c_int), ("qe", C.c_int), ("score2", C.c_int), ("te2", C.c_int)]
 
 
+def ref_tree():
+    """The reference source tree to compile: $KSW2_REF_TREE, else the staged copy, else None."""
+    t = os.environ.get("KSW2_REF_TREE")
+    if t and os.path.isdir(t):
+        return t
+    return STAGED_TREE if os.path.isfile(os.path.join(STAGED_TREE, "ksw2.h")) else None
+
+
+def stage(tree):
+    """Copy the reference's sources and test reads from `tree` into the staged folder."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "stage", f"REF={tree}"])
+
+
 def build(ref=True):
-    """Compile liboracle.so (and _ref/libksw2ref.so when the reference tree exists)."""
+    """Compile liboracle.so, and _ref/libksw2ref.so and _ref/libmbpe.so when a reference tree
+    (ref_tree()) exists."""
     subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
-    if ref and os.path.isdir(REF_TREE):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"])
+    t = ref_tree() if ref else None
+    if t:
+        subprocess.check_call(["make", "-s", "-C", HERE, "-j8", "ref", f"REF={t}"])
+
+
+def build_minibwa(gpulib_dir):
+    """Compile the reference's minibwa stock and relinked against libksw2gpu.so in gpulib_dir
+    (oracle/_ref/minibwa_{stock,gpu}{,_km}); needs a reference tree."""
+    t = ref_tree()
+    if not t:
+        raise RuntimeError("no reference tree: set KSW2_REF_TREE or stage one (make -C oracle stage REF=...)")
+    subprocess.check_call(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", "minibwa", f"REF={t}",
+                           f"GPULIB={gpulib_dir}"])
+    return {k: os.path.join(HERE, "_ref", "minibwa_" + k) for k in ("stock", "gpu", "stock_km", "gpu_km")}
 
 
 def have_ref():

@@ -152,17 +152,18 @@ def parse(fn):
 
 
 def main():
-    if not os.path.isdir(O.REF_TREE):
-        raise SystemExit("the reference tree is needed to record the trace")
-    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "trace", f"REF={O.REF_TREE}"])
+    tree = O.ref_tree()
+    if tree is None:
+        raise SystemExit("the reference tree is needed to record the trace (set KSW2_REF_TREE)")
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "trace", f"REF={tree}"])
     rng = np.random.default_rng(20241203)
-    g = read_fasta_gz(os.path.join(O.REF_TREE, "test", "chrM-human.fa.gz"))
+    g = read_fasta_gz(os.path.join(tree, "test", "chrM-human.fa.gz"))
     with tempfile.TemporaryDirectory() as d:
         tr = os.path.join(d, "trace.bin")
-        fa = os.path.join(O.REF_TREE, "test", "chrM-human.fa.gz")
+        fa = os.path.join(tree, "test", "chrM-human.fa.gz")
         run(["index", fa, "chrM"], os.devnull, d)
         run(["index", "--meth", fa, "chrMm"], os.devnull, d)
-        t1, t2 = (os.path.join(O.REF_TREE, "test", f"chrM-read_{i}.fa.gz") for i in (1, 2))
+        t1, t2 = (os.path.join(tree, "test", f"chrM-read_{i}.fa.gz") for i in (1, 2))
         run(["map", "chrM", t1, t2], tr, d)
         a, b = sim_pairs(rng, g, 1500)
         write_fa(os.path.join(d, "s1.fa"), a), write_fa(os.path.join(d, "s2.fa"), b)

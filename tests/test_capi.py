@@ -78,3 +78,27 @@ def test_synthetic_workloads_are_seeded(built):
     assert r.jobs["qlen"].min() == 150 and 500 <= r.jobs["tlen"].min() and r.jobs["tlen"].max() <= 1000
     s = a.subset([3, 1, 4])
     assert np.array_equal(s.query(0), a.query(3)) and np.array_equal(s.target(2), a.target(4))
+
+
+def test_noalloc_checks_job_descriptors_before_device_work(built):
+    """ksw2g_ext_noalloc refuses descriptors that would read past the caller's arena, or that
+    break the padded layout, with KSW2G_E_ARG before it touches a device (so this runs here)."""
+    from minibwa_gb300.lib import EXT_JOB, gen_nt4_mat, load_library
+    L = load_library()
+    f = L.ksw2g_ext_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int8, C.c_void_p, C.c_int8, C.c_int8, C.c_int8, C.c_int8, C.c_int, C.c_void_p,
+                  C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    mat = gen_nt4_mat(2, 8, 0, 1)
+    jobs = np.zeros(1, EXT_JOB)
+    jobs["qoff"], jobs["toff"], jobs["qlen"], jobs["tlen"], jobs["w"], jobs["flag"] = 32, 96, 10, 10, 10, 0x40
+    for arena_len, qoff, qlen, ok in ((144, 32, 10, True), (143, 32, 10, False), (4096, 40, 10, False),
+                                      (4096, 16, 10, False), (4096, 32, -1, False)):
+        j = jobs.copy()
+        j["qoff"], j["qlen"] = qoff, qlen
+        rc = f(1, 5, mat.ctypes.data, 12, 2, 24, 1, 1, j.ctypes.data, 16, arena_len, 16, 16, 1 << 20, None)
+        if ok:
+            assert rc != -2  # gets past the descriptor checks (and then finds no device)
+        else:
+            assert rc == -2, (arena_len, qoff, qlen, rc)
+    assert f(1, 5, mat.ctypes.data, 12, 2, 24, 1, -1, jobs.ctypes.data, 16, 4096, 16, 16, 1 << 20, None) == -2

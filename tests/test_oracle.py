@@ -64,7 +64,7 @@ def test_cell_counter(orc):
     assert st["cells"] == exp and st["n_diag"] == 79
 
 
-needs_ref = pytest.mark.skipif(not os.path.isdir(O.REF_TREE), reason="reference tree not present")
+needs_ref = pytest.mark.skipif(O.ref_tree() is None, reason="reference tree not present")
 
 
 @needs_ref
@@ -83,7 +83,7 @@ def test_oracle_equals_reference_on_benchmark_shapes(built):
 
 @needs_ref
 def test_differential_fuzz_against_reference(built):
-    subprocess.check_call(["make", "-s", "-C", O.HERE, "fuzz", f"REF={O.REF_TREE}"])
+    subprocess.check_call(["make", "-s", "-C", O.HERE, "fuzz", f"REF={O.ref_tree()}"])
     out = subprocess.run([os.path.join(O.HERE, "_ref", "fuzz_vs_ref"), "30000", "7"], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.startswith("OK")

@@ -41,7 +41,8 @@ def L(built):
     lib = load_library()
     lib.ksw2g_ext_noalloc.restype = C.c_int
     lib.ksw2g_ext_noalloc.argtypes = [C.c_int, C.c_int8, C.c_void_p, C.c_int8, C.c_int8, C.c_int8, C.c_int8, C.c_int,
-                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+                                      C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64,
+                                      C.c_void_p]
     return lib
 
 
@@ -56,7 +57,7 @@ def _run_noalloc(L, p):
     d_cig = torch.zeros(cap * 4, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
     rc = L.ksw2g_ext_noalloc(int(p.dual), 5, p.mat.ctypes.data, p.q, p.e, p.q2, p.e2, n, jobs.ctypes.data,
-                             C.c_void_p(d_arena.data_ptr()), C.c_void_p(d_res.data_ptr()),
+                             C.c_void_p(d_arena.data_ptr()), len(arena), C.c_void_p(d_res.data_ptr()),
                              C.c_void_p(d_cig.data_ptr()), cap, C.c_void_p(stream))
     assert rc == 0, L.ksw2g_last_error().decode()
     torch.cuda.synchronize()
@@ -91,7 +92,7 @@ def test_noalloc_rejects_oversized_batches(L):
     from minibwa_gb300 import synth
     p = synth.config1(3000, seed=79)  # about 170 MB of traceback rows: beyond the fixed scratch
     jobs, _ = _padded(p.subset(np.arange(3000)))
-    rc = L.ksw2g_ext_noalloc(1, 5, p.mat.ctypes.data, 12, 2, 24, 1, len(jobs), jobs.ctypes.data, 16, 16, 16, 1 << 30,
-                             None)
+    rc = L.ksw2g_ext_noalloc(1, 5, p.mat.ctypes.data, 12, 2, 24, 1, len(jobs), jobs.ctypes.data, 16, 1 << 40, 16, 16,
+                             1 << 30, None)
     assert rc == -5  # KSW2G_E_CAPACITY, before any device work
     assert b"scratch" in L.ksw2g_last_error()
