@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--pairs", type=int, default=None, help="override the workload's unit count")
     ap.add_argument("--cpu-sample", type=int, default=None, help="units in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lanes", type=int, default=-1, choices=[-1, 0, 1],
+                    help="extension DP lane width: -1 the library's choice, 0 bytes, 1 16-bit (DPX)")
     return ap.parse_args()
 
 
@@ -474,6 +476,7 @@ def main():
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     L = K.load_library()
+    K.set_ext_family(args.lanes)
     w = Workload(args.workload, args, rank)
     ctx = Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)

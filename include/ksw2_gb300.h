@@ -212,11 +212,20 @@ int ksw2g_graph_launches(const ksw2g_graph_t *graph);  /* kernel launches in one
 void ksw2g_graph_destroy(ksw2g_graph_t *graph);
 
 /* Select the thread-group shape used for extension jobs whose reference
- * n_col_ (16-byte blocks per anti-diagonal) lies in [ncol_lo, ncol_hi];
- * shape indexes ksw2g_ext_shapes().  Used by the autotuner. */
+ * n_col_ (16-byte blocks per anti-diagonal) lies in [ncol_lo, ncol_hi]:
+ * shape s < ksw2g_ext_num_shapes() runs the DP on four byte lanes per 32-bit
+ * register, shape ksw2g_ext_num_shapes() + s the same thread-group shape on two
+ * 16-bit lanes with DPX min/max instructions (used where the scoring allows
+ * it: gap costs non-negative, q+e and q2+e2 at most 128).  Both are bit-exact
+ * with the reference.  Used by the autotuner. */
 int ksw2g_ext_num_shapes(void);
 int ksw2g_ext_shape_info(int shape, int *group_threads, int *words_per_thread);
 int ksw2g_ext_set_shape(int dual, int mode, int ncol_lo, int ncol_hi, int shape);
+/* Force the lane width of extension batches prepared after the call: 0 bytes,
+ * 1 16-bit halves (where the scoring allows it), -1 (default) whatever the
+ * shape preferences select.  Process-wide.  Returns 0 or KSW2G_E_ARG. */
+int ksw2g_ext_set_family(int family);
+int ksw2g_ext_get_family(void);
 
 /*
  * Extension batch that allocates nothing (no counterpart in the reference).

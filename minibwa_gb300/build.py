@@ -51,6 +51,8 @@ def build(verbose=False, force=False):
     units = [
         ("ext_kernels.cu", "ext_z2.o", ["-DKSW2G_EXT_VAR=0"]),
         ("ext_kernels.cu", "ext_d2.o", ["-DKSW2G_EXT_VAR=1"]),
+        ("ext16_kernels.cu", "ext16_z2.o", ["-DKSW2G_EXT_VAR=0"]),
+        ("ext16_kernels.cu", "ext16_d2.o", ["-DKSW2G_EXT_VAR=1"]),
         ("ll_kernels.cu", "ll.o", []),
         ("capi.cu", "capi.o", []),
         ("probe.cu", "probe.o", []),

@@ -31,6 +31,9 @@ cudaError_t launch_ext_dp_d2(int mode, int shape, const ksw2g_ext_params &P, con
 cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,
                           int max_blocks, cudaStream_t st) {
   if (shape == kWideShape) return launch_ext_wide(P, L, st);
+  if (shape >= kExt16Base)
+    return dual ? launch_ext16_dp_d2(mode, shape - kExt16Base, P, L, max_blocks, st)
+                : launch_ext16_dp_z2(mode, shape - kExt16Base, P, L, max_blocks, st);
   return dual ? launch_ext_dp_d2(mode, shape, P, L, max_blocks, st)
               : launch_ext_dp_z2(mode, shape, P, L, max_blocks, st);
 }
@@ -38,27 +41,34 @@ cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params 
 static const int64_t kWaveTarget = (int64_t)1 << 30;  // traceback bytes per wave of short pairs
 static const double kLongCells = 200000.0;             // mean band cells above which pairs count as long
 
-// shape preference per (dual, mode, n_col); 0 = use the smallest shape that fits
+// shape preference per (dual, mode, n_col): shape code + 1 (codes from kNumExtShapes on are
+// the 16-bit-lane kernels); 0 = the smallest byte-lane shape that holds the band
 static const int kMaxPrefCol = 512;
 static int g_pref[2][3][kMaxPrefCol + 1];
 static std::mutex g_pref_mu;
+// lane width forced on every batch: -1 none (preferences decide), 0 bytes, 1 16-bit halves
+static std::atomic<int> g_family{-1};
 
 static bool shape_holds(int s, int n_col) {
   return s >= 0 && s < kNumExtShapes && kExtShapes[s].G * kExtShapes[s].K >= 4 * n_col;
 }
 
-int ext_shape_pick(int dual, int mode, int n_col) {
+int ext_shape_id(int dual, int mode, int n_col, const ksw2g_ext_params &P) {
   const int fit = ext_shape_for(n_col);
-  if (fit < 0) return -1;
+  if (fit < 0) return kWideShape;
+  int s = fit;
+  bool w16 = false;
   if (n_col >= 0 && n_col <= kMaxPrefCol) {
     const int p = g_pref[dual & 1][mode][n_col] - 1;
-    if (shape_holds(p, n_col)) return p;
+    if (p >= 0 && shape_holds(p % kNumExtShapes, n_col)) s = p % kNumExtShapes, w16 = p >= kNumExtShapes;
   }
-  return fit;
+  const int fam = g_family.load(std::memory_order_relaxed);
+  if (fam >= 0) w16 = fam == 1;
+  return w16 && ext16_params_ok(P) ? kExt16Base + s : s;
 }
-void ext_shape_set_pref(int dual, int mode, int lo, int hi, int shape) {
+void ext_shape_set_pref(int dual, int mode, int lo, int hi, int code) {
   std::lock_guard<std::mutex> g(g_pref_mu);
-  for (int c = lo < 0 ? 0 : lo; c <= hi && c <= kMaxPrefCol; ++c) g_pref[dual & 1][mode][c] = shape + 1;
+  for (int c = lo < 0 ? 0 : lo; c <= hi && c <= kMaxPrefCol; ++c) g_pref[dual & 1][mode][c] = code + 1;
 }
 }  // namespace ksw2g
 
@@ -345,7 +355,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     mode[i] = ext_mode(J.flag);
     const bool live = J.qlen > 0 && J.tlen > 0 && !b->P.skip_all;
     const int nc = live ? ext_ncol(J.qlen, J.tlen, J.w) : 1;
-    shape[i] = ext_shape_or_wide(ext_shape_pick(dual, mode[i], nc));
+    shape[i] = ext_shape_id(dual, mode[i], nc, b->P);
     if (shape[i] == kWideShape) ++n_wide, wide_max = std::max(wide_max, ext_wide_scratch(J.qlen, J.tlen));
     foot[i] = (live && mode[i] != 0) ? (((int64_t)(J.qlen + J.tlen - 1) * nc * 16 + 15) & ~(int64_t)15) : 0;
     if (foot[i] > c->tb_budget)
@@ -389,7 +399,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   std::vector<int64_t> tbo(n);
   std::vector<int32_t> ord(n);
   int64_t ordp = 0;
-  const int nshp = kNumExtShapes + 1;  // the instantiated shapes and the block-wide kernel
+  const int nshp = kNumShapeIds;  // both lane widths' shapes and the block-wide kernel
   const int nbins = 3 * nshp;
   std::vector<int32_t> bcount(nbins), bpos(nbins);
   for (int i = 0; i < n;) {
@@ -800,10 +810,16 @@ extern "C" int ksw2g_ext_shape_info(int shape, int *g, int *k) {
   return 0;
 }
 extern "C" int ksw2g_ext_set_shape(int dual, int mode, int lo, int hi, int shape) {
-  if (shape < 0 || shape >= kNumExtShapes || mode < 0 || mode > 2) return set_err(KSW2G_E_ARG, "bad shape/mode");
+  if (shape < 0 || shape >= 2 * kNumExtShapes || mode < 0 || mode > 2) return set_err(KSW2G_E_ARG, "bad shape/mode");
   ext_shape_set_pref(dual, mode, lo, hi, shape);
   return 0;
 }
+extern "C" int ksw2g_ext_set_family(int family) {
+  if (family < -1 || family > 1) return set_err(KSW2G_E_ARG, "lane width must be -1 (tuned), 0 (bytes) or 1 (16-bit)");
+  g_family.store(family);
+  return 0;
+}
+extern "C" int ksw2g_ext_get_family(void) { return g_family.load(); }
 
 // ---------------------------------------------------------------- per-call drop-in
 // Allocation of ez->cigar and of the ksw_ll_qinit block follows the caller's
@@ -872,7 +888,7 @@ static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen
   ksw2g_ctx *c = thread_ctx();
   const int mode = ext_mode(flag);
   const int nc = ext_ncol(qlen, tlen, w);
-  const int shape = ext_shape_or_wide(ext_shape_pick(dual, mode, nc));
+  const int shape = ext_shape_id(dual, mode, nc, P);
   const int64_t ncig = mode ? (int64_t)qlen + tlen + 1 : 0;
   const int64_t foot = mode ? (int64_t)(qlen + tlen - 1) * nc * 16 : 0;
   const size_t o_job = 32, o_tbo = o_job + 48, o_bt = o_tbo + 16, o_res = o_bt + 16;

@@ -42,6 +42,13 @@ inline void derive_ext_params(int dual, int8_t m, const int8_t *mat, int8_t q, i
   if (m * m <= 256) memcpy(P.mat, mat, m * m);
 }
 
+// The 16-bit-lane kernels (ext16_dp.cuh) reproduce every byte operation of the reference with
+// its wrap-around, except x = max(a, 0) - (q+e), which they compute without wrapping: exact
+// when the gap costs after the extd2 swap are non-negative and q+e, q2+e2 <= 128.
+inline bool ext16_params_ok(const ksw2g_ext_params &P) {
+  return P.q >= 0 && P.e >= 0 && P.q2 >= 0 && P.e2 >= 0 && P.q + P.e <= 128 && P.q2 + P.e2 <= 128;
+}
+
 // the reference's n_col_: 16-byte blocks of one traceback row (ksw2_extz2_sse.c:64-68)
 inline int ext_ncol(int qlen, int tlen, int w) {
   if (w < 0) w = tlen > qlen ? tlen : qlen;

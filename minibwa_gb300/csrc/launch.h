@@ -17,9 +17,9 @@ extern const ExtShape kExtShapes[kNumExtShapes];
 
 // Smallest instantiated shape index able to hold n_col_ blocks, or -1.
 int ext_shape_for(int n_col);
-// Shape index preferred for n_col_ by the autotuner table (falls back to ext_shape_for).
-int ext_shape_pick(int dual, int mode, int n_col);
-void ext_shape_set_pref(int dual, int mode, int n_col_lo, int n_col_hi, int shape);
+// Autotuner preference for n_col_: a shape code, where codes kNumExtShapes + s select the
+// 16-bit-lane kernel of shape s (ksw2g_ext_set_shape).
+void ext_shape_set_pref(int dual, int mode, int n_col_lo, int n_col_hi, int code);
 
 struct ExtLaunch {
   const ksw2g_job *jobs;
@@ -39,11 +39,24 @@ struct ExtLaunch {
 // Bands wider than the widest thread-group shape run on the block-wide kernel
 // (ext_wide.cuh); bins and launches use this virtual shape index for them.
 constexpr int kWideShape = KSW2G_NUM_SHAPES;
-inline int ext_shape_or_wide(int s) { return s < 0 ? kWideShape : s; }
+
 cudaError_t launch_ext_wide(const ksw2g_ext_params &P, const ExtLaunch &L, cudaStream_t st);
 int64_t ext_wide_scratch(int qlen, int tlen);
 
-// Launch the DP kernel of (dual, mode, shape) as a persistent grid.
+// The 16-bit-lane (DPX) kernels of the same (G, K) shapes have the shape ids kExt16Base + s.
+constexpr int kExt16Base = KSW2G_NUM_SHAPES + 1;
+constexpr int kNumShapeIds = 2 * KSW2G_NUM_SHAPES + 1;
+cudaError_t launch_ext16_dp_z2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                               cudaStream_t st);
+cudaError_t launch_ext16_dp_d2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                               cudaStream_t st);
+// Shape id of a job of n_col_ blocks under scoring P: the autotuner's preference (or the
+// smallest byte-lane shape that holds the band), the lane width forced by
+// ksw2g_ext_set_family if any, 16-bit lanes only where ext16_params_ok; kWideShape for
+// bands wider than every shape.
+int ext_shape_id(int dual, int mode, int n_col, const ksw2g_ext_params &P);
+
+// Launch the DP kernel of (dual, mode, shape id) as a persistent grid.
 cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,
                           int max_blocks, cudaStream_t st);
 cudaError_t launch_ext_bt(const ksw2g_job *jobs, const int32_t *order, int n_jobs, const ksw2g_bt *bts,

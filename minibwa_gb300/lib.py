@@ -109,6 +109,9 @@ def load_library():
         "ksw2g_ext_num_shapes": (i32, []),
         "ksw2g_ext_shape_info": (i32, [i32, C.POINTER(i32), C.POINTER(i32)]),
         "ksw2g_ext_set_shape": (i32, [i32, i32, i32, i32, i32]),
+        "ksw2g_ext_set_family": (i32, [i32]),
+        "ksw2g_ext_get_family": (i32, []),
+        "ksw2g_debug_fail_device_alloc": (None, [i32]),
         "ksw2g_probe_int32_peak": (i32, [i32, C.POINTER(C.c_double)]),
         "ksw2g_batch_set_timing": (i32, [vp, i32]),
         "ksw2g_batch_kernel_ms": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(i32),
@@ -313,6 +316,15 @@ class Context:
         _check(self.L.ksw2g_ll_batch(self.h, size, m, _ptr(mat), gapo, gape, len(jobs), _ptr(jobs), _ptr(qbuf),
                                      len(qbuf), _ptr(tbuf), len(tbuf), _ptr(res)))
         return res
+
+
+def set_ext_family(family):
+    """Lane width of extension batches prepared from now on: 1 = 16-bit lanes (DPX), 0 = byte
+    lanes, -1 = the shape preferences decide.  Returns the previous setting."""
+    L = load_library()
+    prev = L.ksw2g_ext_get_family()
+    _check(L.ksw2g_ext_set_family(int(family)))
+    return prev
 
 
 def probe_int32_peak(device=0):

@@ -223,6 +223,23 @@ inline uint32_t __viaddmin_s16x2(uint32_t a, uint32_t b, uint32_t c) {
 inline uint32_t __vimax3_s16x2(uint32_t a, uint32_t b, uint32_t c) {
   return emu::map16(a, b, c, [](int x, int y, int z) { return std::max(x, std::max(y, z)); });
 }
+// unsigned halves
+namespace emu {
+template <class F>
+inline uint32_t map16u(uint32_t a, uint32_t b, uint32_t c, F f) {
+  return (uint32_t)(uint16_t)f(a & 0xffffu, b & 0xffffu, c & 0xffffu) |
+         ((uint32_t)(uint16_t)f(a >> 16, b >> 16, c >> 16) << 16);
+}
+}  // namespace emu
+inline uint32_t __vimax3_u16x2(uint32_t a, uint32_t b, uint32_t c) {
+  return emu::map16u(a, b, c, [](uint32_t x, uint32_t y, uint32_t z) { return std::max(x, std::max(y, z)); });
+}
+inline uint32_t __vmaxu2(uint32_t a, uint32_t b) {
+  return emu::map16u(a, b, 0, [](uint32_t x, uint32_t y, uint32_t) { return std::max(x, y); });
+}
+inline uint32_t __vminu2(uint32_t a, uint32_t b) {
+  return emu::map16u(a, b, 0, [](uint32_t x, uint32_t y, uint32_t) { return std::min(x, y); });
+}
 template <typename T>
 inline T __ldg(const T *p) { return *p; }
 inline int atomicAdd(int *p, int v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }

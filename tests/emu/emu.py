@@ -42,7 +42,7 @@ def lib():
         _L = C.CDLL(LIB)
         vp, i = C.c_void_p, C.c_int
         _L.emu_ext.restype = i
-        _L.emu_ext.argtypes = [i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, C.c_longlong, i]
+        _L.emu_ext.argtypes = [i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, C.c_longlong, i, i]
         _L.emu_ll.restype = i
         _L.emu_ll.argtypes = [i, i, i, vp, vp, vp, i, i, i, vp, vp, vp, i, i]
         _L.emu_derive_params.restype = None
@@ -93,8 +93,9 @@ def shape_for(nc):
     return -1
 
 
-def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=None, shape=None):
-    """Run one batch (one flag/mode for all jobs) through the emulated kernels.
+def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=None, shape=None, family=0):
+    """Run one batch (one flag/mode for all jobs) through the emulated kernels (family 0: byte
+    lanes, ext_dp_kernel; 1: 16-bit lanes, ext16_dp_kernel).
     Returns (EXT_RESULT array, list of CIGAR lists)."""
     L = lib()
     n = len(qs)
@@ -126,7 +127,7 @@ def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=N
     cap = sum(len(a) + len(b) + 1 for a, b in zip(qs, ts)) + 16
     cig = np.zeros(cap, np.uint32)
     rc = L.emu_ext(int(dual), mode, shape, P.ctypes.data, n, jobs.ctypes.data, arena.ctypes.data, res.ctypes.data,
-                   bts.ctypes.data, tb.ctypes.data, tb_off.ctypes.data, cig.ctypes.data, cap, threads)
+                   bts.ctypes.data, tb.ctypes.data, tb_off.ctypes.data, cig.ctypes.data, cap, threads, family)
     if rc != 0:
         raise RuntimeError(f"emu_ext rc={rc}")
     cigars = [cig[r["cigar_off"]:r["cigar_off"] + r["n_cigar"]].tolist() if r["n_cigar"] > 0 else [] for r in res]

@@ -18,6 +18,7 @@ LaneState g_lane_state[1024];
 
 #include "../../minibwa_gb300/csrc/ext_bt.cuh"
 #include "../../minibwa_gb300/csrc/ext_dp.cuh"
+#include "../../minibwa_gb300/csrc/ext16_dp.cuh"
 #include "../../minibwa_gb300/csrc/ext_wide.cuh"
 #include "../../minibwa_gb300/csrc/host_common.h"
 #include "../../minibwa_gb300/csrc/ll.cuh"
@@ -72,6 +73,10 @@ typedef void (*ext_fn)(const ksw2g_job *, const int32_t *, int, const uint8_t *,
                       {ext_dp_kernel<1, 0, G, K>, ext_dp_kernel<1, 1, G, K>, ext_dp_kernel<1, 2, G, K>}},
 static const ext_fn kTab[KSW2G_NUM_SHAPES][2][3] = {KSW2G_SHAPES(ROW)};
 #undef ROW
+#define ROW(i, G, K) {{ext16_dp_kernel<0, 0, G, K>, ext16_dp_kernel<0, 1, G, K>, ext16_dp_kernel<0, 2, G, K>}, \
+                      {ext16_dp_kernel<1, 0, G, K>, ext16_dp_kernel<1, 1, G, K>, ext16_dp_kernel<1, 2, G, K>}},
+static const ext_fn kTab16[KSW2G_NUM_SHAPES][2][3] = {KSW2G_SHAPES(ROW)};
+#undef ROW
 #define SH(i, G, K) {G, K},
 static const int kShape[KSW2G_NUM_SHAPES][2] = {KSW2G_SHAPES(SH)};
 #undef SH
@@ -91,7 +96,7 @@ void emu_derive_params(int dual, int m, const int8_t *mat, int q, int e, int q2,
 // as the device arena is (32 zero bytes around every sequence).
 int emu_ext(int dual, int mode, int shape, const ksw2g_ext_params *P, int n, const ksw2g_job *jobs,
             const uint8_t *arena, ksw2g_ext_result *res, ksw2g_bt *bts, uint8_t *tb_pool, const int64_t *tb_off,
-            uint32_t *cigar, long long cap, int threads) {
+            uint32_t *cigar, long long cap, int threads, int family) {
   if (shape < 0 || shape > KSW2G_NUM_SHAPES) return -1;
   int counter = 0;
   const ksw2g_ext_params Pc = *P;
@@ -104,7 +109,7 @@ int emu_ext(int dual, int mode, int shape, const ksw2g_ext_params *P, int n, con
       ext_wide_kernel(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter, sp, stride);
     });
   } else {
-    const ext_fn f = kTab[shape][dual][mode];
+    const ext_fn f = family ? kTab16[shape][dual][mode] : kTab[shape][dual][mode];
     run_block(threads, [&] { f(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter); });
   }
   if (mode != 0) {

@@ -30,6 +30,17 @@ def test_emulated_kernels_match_golden_extension(emu, golden):
         assert cig[0] == c["cigar"], i
 
 
+def test_emulated_16bit_kernels_match_golden_extension(emu, golden):
+    """The 16-bit-lane DPX kernels (ext16_dp.cuh) on the golden cases, every fourth one."""
+    cases = list(golden_ext_cases(golden))
+    for i, c in enumerate(cases[1::4]):
+        res, cig = emu.ext(c["dual"], c["m"], c["mat"], c["q"], c["e"], c["q2"], c["e2"], [c["query"]], [c["target"]],
+                           c["w"], c["zdrop"], c["end_bonus"], c["flag"], family=1)
+        got = {f: int(res[0][f]) for f in EXT_FIELDS}
+        assert got == c["out"], (i, got, c["out"])
+        assert cig[0] == c["cigar"], i
+
+
 def test_emulated_kernels_match_golden_ll(emu, golden):
     cases = list(golden_ll_cases(golden))
     for i, c in enumerate(cases[::3]):
