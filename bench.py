@@ -77,6 +77,9 @@ def parse():
     ap.add_argument("--pairs", type=int, default=None, help="override the workload's unit count")
     ap.add_argument("--cpu-sample", type=int, default=None, help="units in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline workload only (by default a cfg1 run also measures cfg2, cfg3 and one "
+                         "serving point)")
     ap.add_argument("--lanes", type=int, default=-1, choices=[-1, 0, 1],
                     help="extension DP lane width: -1 the library's choice, 0 bytes, 1 16-bit (DPX)")
     return ap.parse_args()
@@ -461,24 +464,14 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def main():
-    args = parse()
-    rank, world = dist_init(args)
-    if args.impl == "reference":
-        run_reference(args, rank, world)
-        return
-    if args.workload == "rescue":
-        run_rescue(args, rank, world)
-        return
+def measure(args, w, ctx, dev, rank, world, steps, warmup, int_peak, with_cpu, sample):
+    """One workload: resident-input device timing, the DP kernel's roofline, end-to-end timing
+    through the C ABI one-shot calls, and (rank 0, N=1) the CPU baseline and parity on a
+    sample.  Returns the JSON fields of the workload."""
     import torch
-    from minibwa_gb300 import Context, Graph
+    from minibwa_gb300 import Graph
     from minibwa_gb300 import lib as K
-    dev = int(os.environ.get("LOCAL_RANK", 0))
-    torch.cuda.set_device(dev)
     L = K.load_library()
-    K.set_ext_family(args.lanes)
-    w = Workload(args.workload, args, rank)
-    ctx = Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
 
     # ---------------- value: resident inputs, device timing
@@ -491,7 +484,7 @@ def main():
         else:
             batches[0].run()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     ctx.sync()
     results = [b.fetch() for b in batches]
@@ -504,13 +497,13 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             step()
         e1.record(stream)
         ctx.sync()
     torch.cuda.synchronize()
     barrier(world)
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1) / steps
     launches_per_step = graph.launches if graph is not None else batches[0].launches
     ms_max = allmax(ms, world)
     tot = allsum(w.n, world)
@@ -518,16 +511,15 @@ def main():
     tot_cells = sum(cells)
 
     # ---------------- roofline of the dominant kernel (the DP kernel)
-    int_peak = K.probe_int32_peak(dev)
     kinds = w.kernel_kinds()
     ops = sum(c * OPS_PER_CELL[k] for c, k in zip(cells, kinds))
     n_dp = 1
     if graph is None:
         dp_ms, bt_ms, n_dp, n_bt = batches[0].kernel_ms()
-        n_dp = max(1, n_dp // args.steps)
-        dp_ms_step = dp_ms / args.steps
+        n_dp = max(1, n_dp // steps)
+        dp_ms_step = dp_ms / steps
         kernel_note = (f"DP kernel: {n_dp} launches per step, busy {dp_ms_step:.2f} ms per step "
-                       f"(backtrack {bt_ms / args.steps:.2f} ms); CUDA events around each launch, the "
+                       f"(backtrack {bt_ms / steps:.2f} ms); CUDA events around each launch, the "
                        f"union of their intervals (waves alternate between two streams)")
     else:
         dp_ms_step = ms  # branches overlap inside the graph: the whole graph is the timed unit
@@ -555,6 +547,10 @@ def main():
             tb = int((r["n_diag"].astype(np.int64) * ncol * 16).sum())
             alg_bytes += tb + 2 * int(jq.sum() + jt.sum()) + 4 * int(r["n_cigar"].sum()) + 64 * len(s)
     achieved_gbs = alg_bytes / (ms * 1e-3) / 1e9
+    if graph is not None:
+        graph.close()
+    for b in batches:
+        b.free()
 
     # ---------------- e2e through the C ABI one-shot calls with pinned host buffers
     def pinned(a):
@@ -588,15 +584,15 @@ def main():
             if rc != 0:
                 raise RuntimeError(L.ksw2g_last_error().decode())
 
-    for _ in range(max(1, min(args.warmup, 2))):
+    for _ in range(max(1, min(warmup, 2))):
         e2e_step()
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = allmax((time.perf_counter() - t0) / args.steps, world)
+    e2e_s = allmax((time.perf_counter() - t0) / steps, world)
     barrier(world)
     e2e_value = tot / e2e_s
     # the e2e results equal the resident-run results
@@ -608,43 +604,114 @@ def main():
         h2d += len(s.qbuf) + len(s.tbuf) + s.jobs.nbytes
         d2h += r.nbytes + 4 * int(u.value)
 
-    cb = parity = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb, _, outs = cpu_baseline(w, args.cpu_sample or DEFAULT_SAMPLE[args.workload])
-        parity = parity_vs_cpu(w, results, outs, cb["kind"])
+    out = {
+        "value": value, "unit": w.unit, "ms_per_step": ms_max, "steps": steps, "warmup": warmup,
+        "gcups": tot_cells / (ms * 1e-3) / 1e9, "cells_per_step": tot_cells, "bytes_per_step": alg_bytes,
+        "gpu_launches": launches_per_step * steps,
+        "roofline": {"bound": "int", "achieved": achieved / 1e12, "peak": int_peak / 1e12, "unit": "Tops/s",
+                     "frac": achieved / int_peak, "traffic": traffic,
+                     "ops_per_cell": {k: OPS_PER_CELL[k] for k in sorted(set(kinds))},
+                     "kernel": kernel_note,
+                     "peak_source": "measured in-bench: IADD3+LOP3 chains on every SM (MEASURED_PEAKS.json "
+                                    "has no integer figure)"},
+        "roofline_hbm": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm_peak, "algorithmic_bytes_per_step": alg_bytes,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": e2e_s * 1e3},
+        "clocks": clk.summary(),
+    }
+    if with_cpu and rank == 0 and world == 1:
+        cb, _, outs = cpu_baseline(w, sample)
+        out["cpu_baseline"] = cb
+        out["parity_vs_cpu"] = parity_vs_cpu(w, results, outs, cb["kind"])
+    return out
 
+
+def serving_point(frac=0.8, duration=3.0):
+    """Config 4 at one offered load: the continuous-batching engine's p50 / p99 latency and served
+    rate at `frac` of its measured peak (every job checked against the same job run alone), and
+    the reference CPU implementation's rate on a sample of the same mix."""
+    from minibwa_gb300 import serving
+    from oracle import oracle as O
+    out = serving.sweep(duration=duration, fracs=(frac,), percall_threads=0, check=True, log=open(os.devnull, "w"))
+    row = out["rates"][0]
+    line = {"metric": "served jobs/s at %d%% of peak, p50/p99 latency" % round(frac * 100),
+            "value": row["served_jobs_s"], "unit": "jobs/s", "p50_ms": row["p50_ms"], "p99_ms": row["p99_ms"],
+            "max_ms": row["max_ms"], "offered_jobs_s": row["offered_jobs_s"], "peak_jobs_s": out["peak_jobs_s"],
+            "requests": row["requests"], "duration_s": duration,
+            "mismatches_vs_alone": out["mismatches_vs_alone"],
+            "mix": "70% extz2 150 nt w=25, 20% extd2 log-normal 1-10 kb w=500, 10% ksw_ll i16; request batches "
+                   "of 1-4096 jobs, Poisson arrivals; 8 slots, 40 GB traceback budget"}
+    # CPU: the reference's functions over a sample of the three pools in the mix's proportions
+    sets = serving.JobSets(n_short=7000, n_long=400, n_ll=1000)
+    kind = "reference" if O.have_ref() else "port"
+    which = "ref" if kind == "reference" else "orc"
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    for p in sets.pools[:2]:
+        O.ext_batch(which, p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf, threads)
+    p = sets.pools[2]
+    O.ll_batch(which, p.size, 5, p.mat, p.gapo, p.gape, p.jobs, p.qbuf, p.tbuf, threads)
+    dt = time.perf_counter() - t0
+    n = sum(len(p) for p in sets.pools)
+    line["cpu_baseline"] = {"value": n / dt, "unit": "jobs/s", "cores": threads, "kind": kind,
+                            "sample": f"{n} jobs of the mix (7000 extz2, 400 long extd2, 1000 ksw_ll), "
+                                      f"{threads} threads, {dt:.2f} s wall"}
+    return line
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if args.workload == "rescue":
+        run_rescue(args, rank, world)
+        return
+    import torch
+    from minibwa_gb300 import Context
+    from minibwa_gb300 import lib as K
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    K.load_library()
+    K.set_ext_family(args.lanes)
+    int_peak = K.probe_int32_peak(dev)
+    ctx = Context(dev)
+    w = Workload(args.workload, args, rank)
+    m = measure(args, w, ctx, dev, rank, world, args.steps, args.warmup, int_peak, not args.no_cpu_baseline,
+                args.cpu_sample or DEFAULT_SAMPLE[args.workload])
+    del w
+    extra = {}
+    if args.workload == "cfg1" and not args.no_extras and world == 1:
+        # the other configurations, measured in the same run with fixed short step counts
+        for name in ("cfg2", "cfg3"):
+            wx = Workload(name, argparse.Namespace(pairs=None), rank)
+            mx = measure(args, wx, ctx, dev, rank, world, 3, 1, int_peak, not args.no_cpu_baseline,
+                         DEFAULT_SAMPLE[name])
+            mx["metric"] = wx.metric
+            mx["config"] = workload_config(name, wx.n, world)
+            extra[name] = mx
+            del wx
+        extra["cfg4"] = serving_point()
     if rank == 0:
         line = {
-            "metric": w.metric, "value": value, "unit": w.unit, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int16" if w.ll else "int8",
+            "metric": Workload(args.workload, args, rank, sizes_only=True).metric, "value": m["value"],
+            "unit": m["unit"], "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int16" if args.workload == "cfg3" else "int8",
             "data": "synthetic (seeded splitmix64, no public dataset)",
-            "config": workload_config(args.workload, w.n, world),
-            "bytes_per_step": alg_bytes,
-            "gcups": tot_cells / (ms * 1e-3) / 1e9,
-            "cells_per_step": tot_cells,
-            "gpu_launches": launches_per_step * args.steps,
-            "roofline": {"bound": "int", "achieved": achieved / 1e12, "peak": int_peak / 1e12, "unit": "Tops/s",
-                         "frac": achieved / int_peak, "traffic": traffic,
-                         "ops_per_cell": {k: OPS_PER_CELL[k] for k in sorted(set(kinds))},
-                         "kernel": kernel_note,
-                         "peak_source": "measured in-bench: IADD3+LOP3 chains on every SM (MEASURED_PEAKS.json "
-                                        "has no integer figure)"},
-            "roofline_hbm": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                             "frac": achieved_gbs / hbm_peak, "algorithmic_bytes_per_step": alg_bytes,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
-            "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": e2e_s * 1e3},
-            "clocks": clk.summary(),
+            "config": workload_config(args.workload, sum(Workload(args.workload, args, rank,
+                                                                  sizes_only=True).set_sizes), world),
         }
-        if cb:
-            line["cpu_baseline"] = cb
-            line["parity_vs_cpu"] = parity
+        for k in ("bytes_per_step", "gcups", "cells_per_step", "gpu_launches", "roofline", "roofline_hbm", "e2e",
+                  "clocks", "cpu_baseline", "parity_vs_cpu"):
+            if k in m:
+                line[k] = m[k]
+        if extra:
+            line["extra"] = extra
         print(json.dumps(line), flush=True)
-    if graph is not None:
-        graph.close()
-    for b in batches:
-        b.free()
     ctx.close()
 
 

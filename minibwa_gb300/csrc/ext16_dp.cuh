@@ -304,10 +304,8 @@ ext16_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ 
               const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | (tq & 0x04040404u);
               const uint32_t sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
               bad |= tq | (tq + 0x03030303u);
-              const int lo = i == 0 ? st0 - p0 : 0, hi = fend - p0;
-              const uint32_t wm = lo > 3 || hi < 0 ? 0u
-                                  : (lo > 0 ? 0xffffffffu << (8 * lo) : 0xffffffffu) &
-                                        (hi < 3 ? 0xffffffffu >> (8 * (3 - hi)) : 0xffffffffu);
+              // slots above 0 start above st0 (the window starts at st0's 16-cell block)
+              const uint32_t wm = i == 0 ? lanes_from(st0 - p0) & lanes_upto(fend - p0) : lanes_upto(fend - p0);
               S[i] = (S[i] & ~wm) | (sn & wm);
             }
           }
@@ -341,9 +339,7 @@ ext16_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ 
                     sn |= (v ^ 0x80u) << (8 * b);
                   }
                 }
-                const int lo = st0 - p0, hi = fend - p0;
-                const uint32_t wm = (lo > 0 ? 0xffffffffu << (8 * lo) : 0xffffffffu) &
-                                    (hi < 3 ? 0xffffffffu >> (8 * (3 - hi)) : 0xffffffffu);
+                const uint32_t wm = lanes_from(st0 - p0) & lanes_upto(fend - p0);
                 S[i] = (S[i] & ~wm) | (sn & wm);
               }
             }

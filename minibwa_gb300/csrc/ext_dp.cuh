@@ -65,6 +65,14 @@ __device__ __forceinline__ void shift4(T (&a)[K], T fill, int k, unsigned gm) {
 __device__ __forceinline__ uint32_t ld_tw(const uint8_t *tp, int p, int tlen) {
   return p < tlen ? __ldg((const uint32_t *)(tp + p)) : 0u;
 }
+// Byte lanes j of a word with from <= j <= to set to 0xff, the others 0 (from, to relative to
+// the word's first cell; the funnel shifts clamp their counts at 32, so any range works).
+__device__ __forceinline__ uint32_t lanes_upto(int to) {
+  return __funnelshift_rc(0xffffffffu, 0u, (uint32_t)max(24 - 8 * to, 0));
+}
+__device__ __forceinline__ uint32_t lanes_from(int from) {
+  return __funnelshift_lc(0u, 0xffffffffu, (uint32_t)max(8 * from, 0));
+}
 // query bytes of four consecutive cells: lane j = query[hi - j], 0 outside [0, qlen)
 __device__ __forceinline__ uint32_t ld_qw(const uint8_t *qp, int hi, int qlen) {
   uint32_t w = 0;
@@ -327,10 +335,8 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | (tq & 0x04040404u);
               const uint32_t sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
               bad |= tq | (tq + 0x03030303u);  // bits 3-7 of a lane set iff t | q >= 5
-              const int lo = i == 0 ? st0 - p0 : 0, hi = fend - p0;
-              const uint32_t wm = lo > 3 || hi < 0 ? 0u
-                                  : (lo > 0 ? 0xffffffffu << (8 * lo) : 0xffffffffu) &
-                                        (hi < 3 ? 0xffffffffu >> (8 * (3 - hi)) : 0xffffffffu);
+              // slots above 0 start above st0 (the window starts at st0's 16-cell block)
+              const uint32_t wm = i == 0 ? lanes_from(st0 - p0) & lanes_upto(fend - p0) : lanes_upto(fend - p0);
               S[i] = (S[i] & ~wm) | (sn & wm);
             }
           }
@@ -364,9 +370,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
                     sn |= v << (8 * b);
                   }
                 }
-                const int lo = st0 - p0, hi = fend - p0;
-                const uint32_t wm = (lo > 0 ? 0xffffffffu << (8 * lo) : 0xffffffffu) &
-                                    (hi < 3 ? 0xffffffffu >> (8 * (3 - hi)) : 0xffffffffu);
+                const uint32_t wm = lanes_from(st0 - p0) & lanes_upto(fend - p0);
                 S[i] = (S[i] & ~wm) | (sn & wm);
               }
             }

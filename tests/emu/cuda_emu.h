@@ -240,6 +240,15 @@ inline uint32_t __vmaxu2(uint32_t a, uint32_t b) {
 inline uint32_t __vminu2(uint32_t a, uint32_t b) {
   return emu::map16u(a, b, 0, [](uint32_t x, uint32_t y, uint32_t) { return std::min(x, y); });
 }
+// funnel shifts with the count clamped at 32
+inline uint32_t __funnelshift_rc(uint32_t lo, uint32_t hi, uint32_t s) {
+  const uint64_t v = ((uint64_t)hi << 32) | lo;
+  return (uint32_t)(v >> (s > 32 ? 32 : s));
+}
+inline uint32_t __funnelshift_lc(uint32_t lo, uint32_t hi, uint32_t s) {
+  const uint64_t v = ((uint64_t)hi << 32) | lo;
+  return (uint32_t)((v << (s > 32 ? 32 : s)) >> 32);
+}
 template <typename T>
 inline T __ldg(const T *p) { return *p; }
 inline int atomicAdd(int *p, int v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }
