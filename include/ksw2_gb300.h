@@ -158,6 +158,59 @@ int ksw2g_align_pairs(ksw2g_ctx_t *ctx, const ksw2g_align_opt_t *opt, const int8
 					  int64_t tbuf_len, ksw2g_ext_result_t *res, uint32_t *cigar, int64_t cigar_cap,
 					  int64_t *cigar_used);
 
+/* ---- whole chains of mb_align1 (align.c:548-757), gap fills issued speculatively ----
+ * For every hit (chain of anchors) the call derives the DP jobs mb_align1 runs: the left
+ * extension, the gap fill between consecutive anchors (align.c:668-740) and the right
+ * extension, with the anchor trimming of short-read mode (mb_max_stretch, align.c:522-546)
+ * or long-read mode (mm_fix_bad_ends, mm_filter_bad_seeds(_alt), align.c:392-520).  Every
+ * job of every chain goes to the device at once, the gap fills in their first, approximate
+ * z-drop pass; the reference's z-drop test on their CIGARs (mm_test_zdrop, align.c:26-68,
+ * with its inversion check on the device) selects the second, exact pass; then each chain is
+ * assembled in order as mb_align1 does: the first gap fill that z-drops ends the chain and
+ * cancels the jobs behind it (align.c:698-720), splitting the hit when the anchors behind
+ * carry enough matches.  Results are mb_align1's, up to the call of mb_update_extra
+ * (align.c:753), which stays with the caller. */
+typedef struct {          /* mb_anchor_t (mbpriv.h:26-32) */
+	int32_t sid;          /* tid << 1 | rev */
+	int32_t len;          /* anchor length */
+	int32_t qpos;         /* query coordinate of the anchor's last base */
+	uint32_t flag;        /* MB_SEED_LONG_JOIN 0x1, MB_SEED_IGNORE 0x2 */
+	int64_t tpos;         /* contig coordinate of the anchor's last base */
+} ksw2g_anchor_t;
+typedef struct {          /* one hit: the fields of mb_hit_t that mb_align1 reads */
+	int32_t as, cnt;      /* anchors[as .. as+cnt) of the anchor array */
+	int32_t mlen, score;  /* r->mlen, r->score */
+	int32_t qoff, qlen;   /* the read in qbuf, in the orientation aligned (seq[rev]) */
+	int32_t meth;         /* methylation mode as mb_align1 receives it (flipped for rev strands) */
+	int32_t split_inv;    /* r->split_inv */
+} ksw2g_chain_t;
+typedef struct {          /* the mb_opt_t fields mb_align1 reads */
+	int32_t a, b, b_ts, b_ambi, q, e, q2, e2;
+	int32_t bw, bw_long, max_gap, end_bonus, zdrop, zdrop_inv;
+	int32_t min_ksw_len, min_len, min_chain_score, min_dp_max;
+	int32_t long_reads;   /* MB_F_LONG */
+	int32_t adaptive;     /* MB_F_ADAP: reads longer than max_sr_len align as long reads */
+	int32_t max_sr_len;
+	int32_t meth;         /* MB_F_METH */
+	int64_t max_sw_mat;
+} ksw2g_chain_opt_t;
+typedef struct {
+	int64_t ts, te;       /* r->ts, r->te */
+	int32_t qs, qe;       /* r->qs, r->qe (on the read's forward strand, as mb_align1 sets them) */
+	int32_t dp_score;     /* r->p->dp_score */
+	int32_t n_cigar;      /* r->p->n_cigar; the CIGAR is at cigar + cigar_off */
+	int64_t cigar_off;
+	int32_t cnt, score;   /* r->cnt, r->score after a split */
+	int32_t split_n;      /* > 0: the hit was split by mb_split_hit(r, r2, split_n, ...) */
+	int32_t split_inv2;   /* r2->split_inv of that split */
+	int32_t n_dp;         /* DP jobs whose results the chain used */
+	int32_t n_dp_issued;  /* DP jobs issued for it (the speculative ones included) */
+} ksw2g_chain_result_t;
+int ksw2g_align_chains(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, const ksw2g_chain_opt_t *opt, int n_chains,
+					   const ksw2g_chain_t *chains, const ksw2g_anchor_t *anchors, int64_t n_anchors,
+					   const uint8_t *qbuf, int64_t qbuf_len, ksw2g_chain_result_t *res, uint32_t *cigar,
+					   int64_t cigar_cap, int64_t *cigar_used);
+
 /* ---- mate rescue over the resident reference (pe.c:209-372) ----
  * One candidate is one (read, window) pair of mb_matesw_core: the window
  * [ts, te) on contig tid computed from the insert-size statistics and clamped

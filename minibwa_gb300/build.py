@@ -62,6 +62,7 @@ def build(verbose=False, force=False):
         ("ref.cu", "ref.o", []),
         ("rescue.cu", "rescue.o", []),
         ("align_pairs.cu", "align_pairs.o", []),
+        ("align_chains.cu", "align_chains.o", []),
     ]
     hdrs = _headers()
     procs, objs = [], []

@@ -185,6 +185,7 @@ namespace ksw2g {
 cudaError_t launch_ref_gather(int n, const int32_t *tid, const int64_t *st, const int32_t *len, const int32_t *flags,
                               const int64_t *dst_off, uint8_t *arena, const ksw2g_ref *R, cudaStream_t stream);
 int ref_check_window(const ksw2g_ref *R, int64_t tid, int64_t st, int64_t len);
+int64_t ref_ctg_len(const ksw2g_ref *R, int64_t tid);  // -1 for a bad contig id
 }  // namespace ksw2g
 
 // Upload + pack the sequences and build the device job table and the wave plan

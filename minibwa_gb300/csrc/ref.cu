@@ -96,6 +96,10 @@ cudaError_t launch_ref_gather(int n, const int32_t *tid, const int64_t *st, cons
   return cudaGetLastError();
 }
 
+int64_t ref_ctg_len(const ksw2g_ref *R, int64_t tid) {
+  return tid >= 0 && tid < R->n_ctg ? (int64_t)R->h_len[tid] : -1;
+}
+
 int ref_check_window(const ksw2g_ref *R, int64_t tid, int64_t st, int64_t len) {
   if (tid < 0 || tid >= R->n_ctg) return report_error(KSW2G_E_ARG, "reference window: contig id out of range");
   if (st < 0 || len < 0 || (uint64_t)(st + len) > R->h_len[tid])

@@ -425,3 +425,160 @@ def rescue_workload(n, ctg_len=(40_000_000, 25_000_000, 15_000_000), spec=None, 
     if rc != 0:
         raise RuntimeError(f"synth_rescue failed ({rc})")
     return ref, jobs, qbuf[:used.value].copy()
+
+
+# minibwa's option presets the chain cases are aligned with (options.c:53-83): "sr"/"adap" and "lr"
+CHAIN_OPT_SR = dict(a=2, b=8, b_ts=0, b_ambi=1, q=12, e=2, q2=23, e2=1, bw=100, bw_long=20000, max_gap=100,
+                    end_bonus=10, zdrop=80, zdrop_inv=80, min_ksw_len=20, min_len=19, min_chain_score=25,
+                    min_dp_max=30, long_reads=0, adaptive=1, max_sr_len=325, meth=0, max_sw_mat=100000000)
+CHAIN_OPT_LR = dict(CHAIN_OPT_SR, bw=500, max_gap=5000, end_bonus=-1, zdrop=400, zdrop_inv=240, min_ksw_len=200,
+                    min_chain_score=40, min_dp_max=50, long_reads=1, adaptive=0)
+
+
+class ChainCases:
+    """Hits (chains of exact-match anchors) of simulated reads over a Reference2b, shaped like the
+    chains minibwa hands to mb_align1: for each read, the sequence in the orientation aligned
+    (seq[rev]) and its anchors -- the maximal runs of at least min_len bases that match the
+    reference on one diagonal, ordered along the read -- with mlen and a chaining score.
+    Reads carry substitutions and short indels, and each draws one event (`kind`):
+      0 none; 1 a block of random bases of unchanged length (a gap fill that z-drops);
+      2 a chimeric junction to a region downstream on the contig; 3 one long insertion or
+      deletion; 4 an inverted segment (the inversion test of the z-drop check); 5 two long gaps,
+      opposite (mm_filter_bad_seeds) or in one direction (mm_filter_bad_seeds_alt); 6 a mid-size
+      indel near either end (mm_fix_bad_ends); 7 a read at a contig's start or end.
+    Bisulfite reads (meth=True) read C as T (mode 1) or G as A (mode 2) on their forward strand;
+    some hits carry split_inv (the z-drop of their left extension uses zdrop_inv)."""
+
+    N_KINDS = 8
+
+    def __init__(self, ref, n, long_reads=False, seed=SEED + 70, min_len=19, meth=False, p_split_inv=0.2):
+        rng = np.random.default_rng(seed)
+        g = ref.decoded()
+        self.ref = ref
+        anchors, chains, reads = [], [], []
+        self.fwd, self.rc, self.kind = [], [], []
+        qoff = 0
+        big = (lambda lo, hi: int(rng.integers(lo * 5, hi * 5))) if long_reads else (lambda lo, hi: int(rng.integers(lo, hi)))
+        while len(chains) < n:
+            k = int(rng.integers(0, len(ref.ctg_len)))
+            clen, c0 = int(ref.ctg_len[k]), int(ref.ctg_off[k])
+            L = int(rng.integers(1000, 6000)) if long_reads else int(rng.integers(100, 251))
+            kind = len(chains) % self.N_KINDS
+            if clen < 4 * L + 20000:
+                continue
+            if kind == 7:
+                st = int(rng.integers(0, 40)) if rng.random() < 0.5 else clen - L - int(rng.integers(0, 40))
+            else:
+                st = int(rng.integers(0, clen - 2 * L - 12000))
+            mt = int(rng.integers(1, 3)) if meth and rng.random() < 0.7 else 0
+            sub, ind = (0.05, 0.02) if long_reads else (0.02, 0.005)
+            at = int(rng.integers(L // 4, 3 * L // 4))
+            ev = []  # (read position, event) to apply
+            if kind == 1:
+                ev = [(at, ("junk", big(20, 80)))]
+            elif kind == 2:
+                ev = [(at, ("jump", big(60, 1600)))]
+            elif kind == 3:
+                ev = [(at, ("ins" if rng.random() < 0.5 else "del", big(30, 120)))]
+            elif kind == 4:
+                ev = [(at, ("inv", big(40, 200)))]
+            elif kind == 5:
+                l1 = big(30, 120)
+                same = rng.random() < 0.5
+                l2 = big(30, 120) if same else l1 + int(rng.integers(-10, 11))
+                op1 = "ins" if rng.random() < 0.5 else "del"
+                op2 = op1 if same else ("del" if op1 == "ins" else "ins")
+                ev = [(at, (op1, l1)), (at + int(rng.integers(20, 60)) * (5 if long_reads else 1), (op2, max(l2, 1)))]
+            elif kind == 6:
+                p6 = int(rng.integers(25, 90)) if rng.random() < 0.5 else L - int(rng.integers(25, 90))
+                ev = [(p6, ("ins" if rng.random() < 0.5 else "del", int(rng.integers(15, 60))))]
+            seq, pos = [], []  # the read in the aligned orientation and its reference position (-1: inserted)
+            t = st
+            while len(seq) < L and t < clen - 1:
+                if ev and len(seq) >= ev[0][0]:
+                    op, ln = ev.pop(0)[1]
+                    if op == "junk":
+                        seq += [int(x) for x in rng.integers(0, 4, ln)]
+                        pos += [-1] * ln
+                        t += ln
+                    elif op == "jump" or op == "del":
+                        t += ln
+                    elif op == "ins":
+                        seq += [int(x) for x in rng.integers(0, 4, ln)]
+                        pos += [-1] * ln
+                    elif op == "inv":
+                        ln = min(ln, clen - 1 - t)
+                        piece = g[c0 + t:c0 + t + ln]
+                        seq += [int(x) for x in _revcomp(piece)]
+                        pos += [-1] * ln
+                        t += ln
+                    continue
+                u = rng.random()
+                if u < ind / 2:
+                    t += int(rng.integers(1, 4))
+                    continue
+                if u < ind:
+                    for _ in range(int(rng.integers(1, 4))):
+                        seq.append(int(rng.integers(0, 4))), pos.append(-1)
+                    continue
+                b = int(g[c0 + t])
+                if b < 4 and rng.random() < sub:
+                    b = (b + int(rng.integers(1, 4))) % 4
+                if mt == 1 and b == 1 and rng.random() < 0.95:
+                    b = 3
+                elif mt == 2 and b == 2 and rng.random() < 0.95:
+                    b = 0
+                seq.append(b), pos.append(t)
+                t += 1
+            s = np.array(seq, np.uint8)
+            p = np.array(pos, np.int64)
+            if len(s) < 60:
+                continue
+            # maximal exact runs on one diagonal (bisulfite pairs match through the conversion)
+            ok = p >= 0
+            gb = np.where(ok, g[c0 + np.maximum(p, 0)], 255)
+            eq = ok & ((s == gb) | ((mt == 1) & (gb == 1) & (s == 3)) | ((mt == 2) & (gb == 2) & (s == 0)))
+            runs, i = [], 0
+            while i < len(s):
+                if not eq[i]:
+                    i += 1
+                    continue
+                j = i
+                while j + 1 < len(s) and eq[j + 1] and p[j + 1] == p[j] + 1:
+                    j += 1
+                if j - i + 1 >= min_len:
+                    runs.append((i, j))
+                i = j + 1
+            if not runs:
+                continue
+            rev = int(rng.random() < 0.5)
+            mt_read = (3 - mt if mt else 0) if rev else mt  # the mode of the read's own forward strand
+            a0 = len(anchors)
+            for i, j in runs:
+                anchors.append((k << 1 | rev, j - i + 1, j, 0, int(p[j])))
+            cnt = len(runs)
+            tp = np.array([x[4] for x in anchors[a0:]], np.int64)
+            qp = np.array([x[2] for x in anchors[a0:]], np.int64)
+            lens = np.array([x[1] for x in anchors[a0:]], np.int64)
+            mlen = int(lens[0])
+            for i in range(1, cnt):  # mb_cal_mblen (map-algo.c:133-150)
+                tl, ql, sp = int(tp[i] - tp[i - 1]), int(qp[i] - qp[i - 1]), int(lens[i])
+                mlen += sp if (tl > sp and ql > sp) else min(tl, ql)
+            split_inv = int(rng.random() < p_split_inv)
+            chains.append((a0, cnt, mlen, int(lens.sum()), qoff, len(s), mt_read, split_inv))
+            reads.append(s)
+            fwd = _revcomp(s) if rev else s
+            self.fwd.append(fwd), self.rc.append(_revcomp(fwd)), self.kind.append(kind)
+            qoff += len(s)
+        self.anchors = np.array(anchors, dtype=[("sid", "<i4"), ("len", "<i4"), ("qpos", "<i4"), ("flag", "<u4"),
+                                                ("tpos", "<i8")])
+        self.chains = np.array(chains, dtype=[(x, "<i4") for x in ("as", "cnt", "mlen", "score", "qoff", "qlen",
+                                                                     "meth", "split_inv")])
+        self.qbuf = np.concatenate(reads)
+
+    def __len__(self):
+        return len(self.chains)
+
+    def read(self, i):
+        c = self.chains[i]
+        return self.qbuf[c["qoff"]:c["qoff"] + c["qlen"]]

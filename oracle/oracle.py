@@ -515,3 +515,350 @@ def align_pair(opt, mat, query, target, w, end_bonus, zdrop, flag):
     dual = not (q == q2 and e == e2)
     ez, _ = extz(int(dual), qs, ts, 5, mat, q, e, q2, e2, w, zdrop * a, end_bonus, flag)
     return {k: ez[k] for k in ALIGN_OUT + ("cigar",)}
+
+
+CHAIN_OPT = ("a", "b", "b_ts", "b_ambi", "q", "e", "q2", "e2", "bw", "bw_long", "max_gap", "end_bonus", "zdrop",
+             "zdrop_inv", "min_ksw_len", "min_len", "min_chain_score", "min_dp_max", "long_reads", "adaptive",
+             "max_sr_len", "meth", "max_sw_mat")
+ALIGN1_OUT = ("ts", "te", "qs", "qe", "dp_score", "n_cigar", "cnt", "score", "r2_cnt", "r2_as", "r2_split_inv",
+              "r2_score")
+
+
+def ref_align1(ref, opt, anchors, chain, seq_fwd, seq_rc):
+    """The reference's own mb_align1 (align.c:548-760) on one hit through _ref/libmbpe.so, with
+    mb_update_extra left out; `anchors` is the whole anchor array (mb_align1 filters a copy of
+    the hit's range in place), `chain` one ksw2g_chain_t-shaped record."""
+    L = refpe_lib()
+    if not hasattr(L, "_refal1"):
+        L.refal_align1.restype = C.c_int
+        L.refal_align1.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
+                                   C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                   C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                   C.c_int]
+        L._refal1 = True
+    keep, args = _l2b_args(ref)
+    optv = np.array([int(opt[k]) for k in CHAIN_OPT], np.int64)
+    a = np.ascontiguousarray(anchors)
+    ai = np.ascontiguousarray(np.stack([a["sid"], a["len"], a["qpos"], a["flag"].astype(np.int32)], 1), np.int32)
+    at = np.ascontiguousarray(a["tpos"], np.int64)
+    f = np.ascontiguousarray(seq_fwd, np.uint8).copy()
+    r = np.ascontiguousarray(seq_rc, np.uint8).copy()
+    out = np.zeros(len(ALIGN1_OUT), np.int64)
+    cig = np.zeros(2 * len(f) + 64 + 4 * int(chain["cnt"]), np.uint32)
+    rc = L.refal_align1(*args, _p(optv), len(f), _p(f), _p(r), int(chain["meth"]), len(a), _p(ai), _p(at),
+                        int(chain["as"]), int(chain["cnt"]), int(chain["mlen"]), int(chain["score"]),
+                        int(chain["split_inv"]), _p(out), _p(cig), len(cig))
+    if rc:
+        raise RuntimeError("CIGAR buffer too small")
+    d = {k: int(v) for k, v in zip(ALIGN1_OUT, out)}
+    d["cigar"] = [int(x) for x in cig[:d["n_cigar"]]]
+    return d
+
+
+def _max_stretch(a):
+    """mb_max_stretch (align.c:522-546) over the hit's anchors a[0..cnt)."""
+    if len(a) < 2:
+        return 0, len(a)
+    best, best_i, best_len, score, ln = -1, -1, 0, int(a[0]["len"]), 1
+    for i in range(1, len(a)):
+        lr, lq = int(a[i]["tpos"] - a[i - 1]["tpos"]), int(a[i]["qpos"] - a[i - 1]["qpos"])
+        if lq == lr:
+            score += min(lq, int(a[i]["len"]))
+            ln += 1
+        else:
+            if score > best:
+                best, best_len, best_i = score, ln, i - ln
+            score, ln = int(a[i]["len"]), 1
+    if score > best:
+        best, best_len, best_i = score, ln, len(a) - ln
+    return best_i, best_len
+
+
+def _gap(a, i):
+    return int(a[i]["qpos"] - a[i - 1]["qpos"]) - int(a[i]["tpos"] - a[i - 1]["tpos"])
+
+
+def _fix_bad_ends(a, mlen, bw, min_match):
+    """mm_fix_bad_ends (align.c:486-520)."""
+    cnt = len(a)
+    if cnt < 3:
+        return 0, cnt
+    as1 = 0
+    m = l = int(a[0]["len"])
+    for i in range(1, cnt - 1):
+        if a[i]["flag"] & 1:
+            break
+        lr, lq, span = int(a[i]["tpos"] - a[i - 1]["tpos"]), int(a[i]["qpos"] - a[i - 1]["qpos"]), int(a[i]["len"])
+        mn, mx = min(lr, lq), max(lr, lq)
+        if mx - mn > l >> 1:
+            as1 = i
+        l += mn
+        m += min(mn, span)
+        if l >= bw << 1 or (m >= min_match and m >= bw) or m >= mlen >> 1:
+            break
+    cnt1 = cnt - as1
+    m = l = int(a[cnt - 1]["len"])
+    for i in range(cnt - 2, as1, -1):
+        if a[i + 1]["flag"] & 1:
+            break
+        lr = int(a[i + 1]["tpos"] - a[i]["tpos"] - a[i + 1]["len"] + a[i]["len"])
+        lq = int(a[i + 1]["qpos"] - a[i]["qpos"] - a[i + 1]["len"] + a[i]["len"])
+        mn, mx, span = min(lr, lq), max(lr, lq), int(a[i]["len"])
+        if mx - mn > l >> 1:
+            cnt1 = i + 1 - as1
+        l += mn
+        m += min(mn, span)
+        if l >= bw << 1 or (m >= min_match and m >= bw) or m >= mlen >> 1:
+            break
+    return as1, cnt1
+
+
+def _long_gaps(b, min_gap):
+    k = [i for i in range(1, len(b)) if abs(_gap(b, i)) > min_gap]
+    return k if len(k) > 1 else []
+
+
+def _filter_bad_seeds(b, min_gap, diff_thres, max_ext_len, max_ext_cnt):
+    """mm_filter_bad_seeds (align.c:411-447) on the view b = a[as1:as1+cnt1] (flags set in place)."""
+    K = _long_gaps(b, min_gap)
+    n, mx, st, en, k = len(K), 0, -1, -1, 0
+    if not K:
+        return
+    while True:
+        if k == n or k >= en:
+            if en > 0:
+                for i in range(K[st], K[en]):
+                    b[i]["flag"] |= 2
+            mx, st, en = 0, -1, -1
+            if k == n:
+                break
+        i = K[k]
+        n_ins = n_del = max_diff = 0
+        max_diff_l = -1
+        g = _gap(b, i)
+        n_ins, n_del = (g, 0) if g > 0 else (0, -g)
+        qs, ts = int(b[i - 1]["qpos"]), int(b[i - 1]["tpos"])
+        for l in range(k + 1, min(n, k + max_ext_cnt + 1)):
+            j = K[l]
+            if int(b[j]["qpos"] - b[j]["len"]) - qs > max_ext_len or int(b[j]["tpos"] - b[j]["len"]) - ts > max_ext_len:
+                break
+            g = _gap(b, j)
+            if g > 0:
+                n_ins += g
+            else:
+                n_del -= g
+            diff = n_ins + n_del - abs(n_ins - n_del)
+            if max_diff < diff:
+                max_diff, max_diff_l = diff, l
+        if max_diff > diff_thres and max_diff > mx:
+            mx, st, en = max_diff, k, max_diff_l
+        k += 1
+
+
+def _filter_bad_seeds_alt(b, min_gap, max_ext):
+    """mm_filter_bad_seeds_alt (align.c:449-484) on the view b."""
+    K = _long_gaps(b, min_gap)
+    n, k = len(K), 0
+    while k < n:
+        i = K[k]
+        gap1 = abs(_gap(b, i))
+        te1, qe1, left = int(b[i]["tpos"]), int(b[i]["qpos"]), int(b[i]["len"])
+        l = k + 1
+        while l < n:
+            j = K[l]
+            if int(b[j]["qpos"]) - qe1 > max_ext or int(b[j]["tpos"]) - te1 > max_ext:
+                break
+            gap2 = abs(_gap(b, j))
+            m = min(int(b[j - 1]["tpos"]) - te1 + left, int(b[j - 1]["qpos"]) - qe1 + left)
+            if m > gap1 + gap2:
+                break
+            te1, qe1, left, gap1 = int(b[j]["tpos"]), int(b[j]["qpos"]), int(b[j]["len"]), gap2
+            l += 1
+        if l > k + 1:
+            for j in range(K[k], K[l - 1]):
+                b[j]["flag"] |= 2
+            b[K[l - 1]]["flag"] |= 1
+        k = l
+
+
+def _cal_mlen(a):
+    """mb_cal_mblen (map-algo.c:133-150), its first value."""
+    if len(a) == 0:
+        return 0
+    mlen = int(a[0]["len"])
+    for i in range(1, len(a)):
+        sp, tl, ql = int(a[i]["len"]), int(np.int32(a[i]["tpos"]) - np.int32(a[i - 1]["tpos"])), int(a[i]["qpos"] - a[i - 1]["qpos"])
+        mlen += sp if tl > sp and ql > sp else min(tl, ql)
+    return mlen
+
+
+def _test_zdrop(opt, qseq, tseq, cigar, mat, is_sr):
+    """mm_test_zdrop (align.c:26-68)."""
+    score, mx, mi, mj, i, j, mz = 0, -(1 << 31), -1, -1, 0, 0, 0
+    pos = [[-1, -1], [-1, -1]]
+
+    def upd(s, ii, jj):
+        nonlocal mx, mi, mj, mz
+        if s < mx:
+            z = mx - s - abs((ii - mi) - (jj - mj)) * opt["e"]
+            if z > mz:
+                mz, pos[0][0], pos[0][1], pos[1][0], pos[1][1] = z, mi, ii, mj, jj
+        else:
+            mx, mi, mj = s, ii, jj
+    for c in cigar:
+        op, ln = c & 0xf, c >> 4
+        if op == 0:
+            for l in range(ln):
+                score += int(mat[int(tseq[i + l]) * 5 + int(qseq[j + l])])
+                upd(score, i + l, j + l)
+            i += ln
+            j += ln
+        elif op in (1, 2, 3):
+            score -= opt["q"] + opt["e"] * ln
+            if op == 1:
+                j += ln
+            else:
+                i += ln
+            upd(score, i, j)
+    q_len, t_len = pos[1][1] - pos[1][0], pos[0][1] - pos[0][0]
+    if not is_sr and mz > opt["zdrop_inv"] and q_len < opt["max_gap"] and t_len < opt["max_gap"]:
+        q2 = np.array([4 if qseq[pos[1][1] - x - 1] >= 4 else 3 - qseq[pos[1][1] - x - 1] for x in range(q_len)],
+                      np.uint8)
+        r, _ = ll(2, q2, tseq[pos[0][0]:pos[0][0] + t_len], 5, mat, opt["q"], opt["e"], 0)
+        if r["score"] >= opt["min_chain_score"] * opt["a"] and r["score"] >= opt["min_dp_max"] * opt["a"]:
+            return 2
+    return 1 if mz > opt["zdrop"] else 0
+
+
+def _append(cg, add):
+    """mb_append_cigar (align.c:300-314)."""
+    if not add:
+        return
+    if cg and (cg[-1] & 0xf) == (add[0] & 0xf):
+        cg[-1] += add[0] >> 4 << 4
+        cg.extend(add[1:])
+    else:
+        cg.extend(add)
+
+
+def align1(ref, opt, anchors, chain, seq):
+    """mb_align1 (align.c:548-757) restated over the oracle's mb_align_pair and ksw_ll, up to
+    mb_update_extra: `seq` is the read in the orientation aligned (seq[rev]), `anchors` the
+    whole anchor array.  Returns the dict ref_align1 returns."""
+    opt = {k: int(v) for k, v in opt.items()}
+    a = np.array(anchors[int(chain["as"]):int(chain["as"]) + int(chain["cnt"])], copy=True)
+    qseq = np.ascontiguousarray(seq, np.uint8)
+    qlen, cnt = len(qseq), int(chain["cnt"])
+    rev, tid = int(a[0]["sid"]) & 1, int(a[0]["sid"]) >> 1
+    ctg_len = int(ref.ctg_len[tid])
+    mt = int(chain["meth"])
+    mt = meth_rev(mt) if rev else mt
+    is_sr = not (opt["long_reads"] or (opt["adaptive"] and qlen > opt["max_sr_len"]))
+    max_back = 0 if is_sr else 10
+    mat = gen_nt4_mat(opt["a"], opt["b"], opt["b_ts"], opt["b_ambi"], mt)
+    bw = int(opt["bw"] * 1.5 + 1.)
+    bw_long = max(int(opt["bw_long"] * 1.5 + 1.), bw) if not is_sr else bw
+    if is_sr:
+        as1, cnt1 = _max_stretch(a)
+    else:
+        as1, cnt1 = _fix_bad_ends(a, int(chain["mlen"]), opt["bw"], opt["min_chain_score"] * 2)
+        _filter_bad_seeds(a[as1:as1 + cnt1], 10, 40, opt["max_gap"] >> 1, 10)
+        _filter_bad_seeds_alt(a[as1:as1 + cnt1], 30, opt["max_gap"] >> 1)
+    A = lambda i: (int(a[i]["tpos"]), int(a[i]["qpos"]), int(a[i]["len"]), int(a[i]["flag"]))  # noqa: E731
+    tp, qp, ln, _ = A(as1)
+    ts, qs = tp + 1 - ln + min(ln >> 1, max_back), qp + 1 - ln + min(ln >> 1, max_back)
+    tp, qp, ln, _ = A(as1 + cnt1 - 1)
+    te, qe = tp + 1 - min(ln >> 1, max_back), qp + 1 - min(ln >> 1, max_back)
+    ea = lambda l, bonus: l + ((l * opt["a"] + bonus - opt["q"]) // opt["e"] if l * opt["a"] + bonus > opt["q"] else 0)  # noqa: E731
+    if is_sr:
+        qs0, qe0 = 0, qlen
+        ts0 = max(ts - ea(qs, opt["end_bonus"]), 0)
+        te0 = min(te + ea(qlen - qe, opt["end_bonus"]), ctg_len)
+    else:
+        ts0, qs0 = max(A(0)[0] + 1 - A(0)[2], 0), A(0)[1] + 1 - A(0)[2]
+        if qs > 0 and ts > 0:
+            l = min(qs, opt["max_gap"])
+            qs0 = min(qs0, max(0, qs - l))
+            l = min(ea(l, 0), opt["max_gap"], ts)
+            ts0 = min(ts0, max(0, ts - l), ts)
+        else:
+            ts0, qs0 = ts, qs
+        te0, qe0 = A(cnt - 1)[0] + 1, A(cnt - 1)[1] + 1
+        if qe < qlen and te < ctg_len:
+            l = min(qlen - qe, opt["max_gap"])
+            qe0 = max(qe0, min(qlen, qe + l))
+            l = min(ea(l, 0), opt["max_gap"], ctg_len - te)
+            te0 = max(te0, min(ctg_len, te + l))
+        else:
+            te0, qe0 = te, qe
+    tgt = lambda s, e: l2b_getseq(ref, tid, s, e - s)  # noqa: E731
+    cg, dp, dropped = [], 0, False
+    out = dict(r2_cnt=0, r2_as=0, r2_split_inv=0, r2_score=0, cnt=cnt, score=int(chain["score"]))
+    if qs > 0 and ts > 0:
+        ez = align_pair(opt, mat, qseq[qs0:qs][::-1], tgt(ts0, ts)[::-1], bw, opt["end_bonus"],
+                        opt["zdrop_inv"] if chain["split_inv"] else opt["zdrop"], 0x40 | 0x02 | 0x80)
+        if ez["n_cigar"] > 0:
+            _append(cg, ez["cigar"])
+            dp += ez["mqe"] if ez["reach_end"] else ez["max"]
+        ts1 = ts - (ez["mqe_t"] + 1 if ez["reach_end"] else ez["max_t"] + 1)
+        qs1 = qs - (qs - qs0 if ez["reach_end"] else ez["max_q"] + 1)
+    else:
+        ts1, qs1 = ts, qs
+    tp, qp, ln, _ = A(as1)
+    te = te1 = tp + 1 - min(ln >> 1, max_back)
+    qe = qe1 = qp + 1 - min(ln >> 1, max_back)
+    _append(cg, [(te - ts) << 4])
+    dp += opt["a"] * (te - ts)
+    ts, qs = te, qe
+    for i in range(1, cnt1):
+        tp, qp, ln, fl = A(as1 + i)
+        if (fl & 2) and i != cnt1 - 1:
+            continue
+        te1, qe1 = tp + 1 - min(ln >> 1, max_back), qp + 1 - min(ln >> 1, max_back)
+        if not (i == cnt1 - 1 or (fl & 1) or (qe1 - qs >= opt["min_ksw_len"] and te1 - ts >= opt["min_ksw_len"])):
+            continue
+        d1 = 0
+        if ln > opt["min_len"] * 2:
+            d1 = min(te1 - (tp + 1 - ln), qe1 - qs, te1 - ts) - opt["min_len"]
+            d1 = 0 if d1 < opt["min_len"] else d1
+        te, qe = te1 - d1, qe1 - d1
+        bw1 = max(qe - qs, te - ts) if fl & 1 else bw_long
+        qg, tg = qseq[qs:qe], tgt(ts, te)
+        ez = align_pair(opt, mat, qg, tg, bw1, -1, opt["zdrop"], 0x08)  # first pass: approximate maximum
+        code = _test_zdrop(opt, qg, tg, ez["cigar"], mat, is_sr)
+        if code:
+            ez = align_pair(opt, mat, qg, tg, bw1, -1, opt["zdrop_inv"] if code == 2 else opt["zdrop"], 0)
+        if ez["n_cigar"] > 0:
+            _append(cg, ez["cigar"])
+        if ez["zdropped"]:
+            j = i - 1
+            while j >= 0 and int(a[as1 + j]["tpos"]) > ts + ez["max_t"]:
+                j -= 1
+            j = max(j, 0)
+            dropped = True
+            dp += ez["max"]
+            te1, qe1 = ts + ez["max_t"] + 1, qs + ez["max_q"] + 1
+            if _cal_mlen(a[as1 + j + 1:as1 + cnt1]) >= opt["min_chain_score"]:
+                n = as1 + j + 1  # mb_split_hit (map-algo.c:247-264)
+                if 0 < n < cnt:
+                    c2 = cnt - n
+                    s2 = int(float(np.float32(np.float32(chain["score"]) * (np.float32(c2) / np.float32(cnt)))) + .499)
+                    out.update(r2_cnt=c2, r2_as=int(chain["as"]) + n, r2_score=s2, cnt=cnt - c2,
+                               score=int(chain["score"]) - s2, r2_split_inv=int(code == 2))
+            break
+        dp += ez["score"]
+        if d1 > 0:
+            _append(cg, [d1 << 4])
+            dp += opt["a"] * d1
+            te, qe = te1, qe1
+        ts, qs = te, qe
+    if not dropped and qe < qe0 and te < te0:
+        ez = align_pair(opt, mat, qseq[qe:qe0], tgt(te, te0), bw, opt["end_bonus"], opt["zdrop"], 0x40)
+        if ez["n_cigar"] > 0:
+            _append(cg, ez["cigar"])
+            dp += ez["mqe"] if ez["reach_end"] else ez["max"]
+        te1 = te + (ez["mqe_t"] + 1 if ez["reach_end"] else ez["max_t"] + 1)
+        qe1 = qe + (qe0 - qe if ez["reach_end"] else ez["max_q"] + 1)
+    out.update(ts=ts1, te=te1, dp_score=dp, n_cigar=len(cg), cigar=cg)
+    out.update(qs=qlen - qe1 if rev else qs1, qe=qlen - qs1 if rev else qe1)
+    return out

@@ -1,0 +1,82 @@
+"""ksw2g_align_chains on the device: every hit's result -- coordinates, dp_score, CIGAR and the
+z-drop split -- equals the reference's own mb_align1 through the golden fixture, and the
+oracle's restatement on fresh seeds."""
+import numpy as np
+import pytest
+
+from test_chains import chain_sets, expected, load_chains_golden, read_of
+
+pytestmark = pytest.mark.gpu
+
+
+def as_align1(chain, r, cig):
+    """A CHAIN_RESULT record in the shape of the reference harness's output."""
+    d = dict(ts=int(r["ts"]), te=int(r["te"]), qs=int(r["qs"]), qe=int(r["qe"]), dp_score=int(r["dp_score"]),
+             n_cigar=int(r["n_cigar"]), cnt=int(r["cnt"]), score=int(r["score"]), r2_cnt=0, r2_as=0,
+             r2_split_inv=0, r2_score=0)
+    if r["split_n"] > 0:
+        d.update(r2_cnt=int(chain["cnt"]) - int(r["split_n"]), r2_as=int(chain["as"]) + int(r["split_n"]),
+                 r2_split_inv=int(r["split_inv2"]), r2_score=int(chain["score"]) - int(r["score"]))
+    d["cigar"] = cig[r["cigar_off"]:r["cigar_off"] + r["n_cigar"]].tolist() if r["n_cigar"] else []
+    return d
+
+
+@pytest.fixture(scope="module")
+def dev(built):
+    from minibwa_gb300 import Context
+    ctx = Context(0)
+    yield ctx
+    ctx.close()
+
+
+def test_chains_golden(dev):
+    from minibwa_gb300.lib import Reference
+    z = load_chains_golden()
+    ref = Reference(dev, z["pac"], z["ctg_off"], z["ctg_len"], z["ambi"])
+    for name, opt, idx in chain_sets(z):
+        ch = z["chains"][idx.start:idx.stop]
+        res, cig = ref.align_chains(opt, ch, z["anchors"], z["qbuf"])
+        for k, i in enumerate(idx):
+            got = as_align1(ch[k], res[k], cig)
+            assert got == expected(z, i), (name, i)
+            assert res[k]["n_dp"] <= res[k]["n_dp_issued"]
+    ref.close()
+
+
+def test_chains_oracle_fresh_seeds(dev):
+    from oracle import oracle as O
+    from minibwa_gb300 import synth
+    from minibwa_gb300.lib import Reference
+    R = synth.Reference2b([400000, 250000, 120000], n_runs=12, seed=310)
+    ref = Reference(dev, R.pac, R.ctg_off, R.ctg_len, R.ambi)
+    for lr, n, opt, meth in ((False, 1200, synth.CHAIN_OPT_SR, False), (True, 48, synth.CHAIN_OPT_LR, False),
+                             (False, 300, dict(synth.CHAIN_OPT_SR, meth=1, b_ts=4), True),
+                             (True, 24, dict(synth.CHAIN_OPT_LR, meth=1), True)):
+        cs = synth.ChainCases(R, n, long_reads=lr, seed=311 + n, meth=meth)
+        res, cig = ref.align_chains(opt, cs.chains, cs.anchors, cs.qbuf)
+        for i in range(len(cs)):
+            exp = O.align1(R, opt, cs.anchors, cs.chains[i], cs.read(i))
+            assert as_align1(cs.chains[i], res[i], cig) == exp, (lr, meth, i, cs.kind[i])
+    ref.close()
+
+
+def test_chains_edges(dev):
+    from minibwa_gb300.lib import CHAIN, Reference
+    z = load_chains_golden()
+    ref = Reference(dev, z["pac"], z["ctg_off"], z["ctg_len"], z["ambi"])
+    opt = next(chain_sets(z))[1]
+    res, cig = ref.align_chains(opt, np.zeros(0, CHAIN), z["anchors"], z["qbuf"])
+    assert len(res) == 0 and len(cig) == 0
+    ch = z["chains"][:3].copy()
+    ch[1]["cnt"] = 0  # mb_align1 returns at once for a hit without anchors
+    res, cig = ref.align_chains(opt, ch, z["anchors"], z["qbuf"])
+    assert res[1]["n_cigar"] == 0 and res[1]["cigar_off"] == -1 and res[1]["n_dp_issued"] == 0
+    for k in (0, 2):
+        assert as_align1(ch[k], res[k], cig) == expected(z, k)
+    bad = z["chains"][:2].copy()
+    bad[1]["as"] = len(z["anchors"])  # anchors out of range: refused before any device work
+    with pytest.raises(RuntimeError):
+        ref.align_chains(opt, bad, z["anchors"], z["qbuf"])
+    with pytest.raises(RuntimeError):  # CIGAR buffer too small
+        ref.align_chains(opt, z["chains"][:4], z["anchors"], z["qbuf"], cigar_cap=1)
+    ref.close()
