@@ -51,10 +51,12 @@ OPS_PER_CELL = {
 }
 # DRAM bytes per nominal cell of the DP kernel, from ncu (dram__bytes_read.sum + dram__bytes_write.sum
 # of one captured launch / its cells), scaled to the workload's launches by their cell counts.
-# extd2: 1,038,595,072 B over 674,520,661 cells (ext_dp_kernel<1,1,16,2>, 20,000 config-1 pairs);
+# extd2: 188,659,200 + 791,366,144 B over 674,520,661 cells (ext_dp_kernel<1,1,8,4>, 20,000 config-1 pairs);
+# extz2: 129,133,568 + 261,759,488 B over 146,499,977 cells (ext_dp_kernel<0,1,4,3>, 20,000 config-0 pairs);
 # ll_i16: 111,992,832 B over 11,259,234,900 cells (ll_dpx_kernel<2,20>, 100,000 config-3 jobs).
-# Both grow with the cells a launch processes (traceback rows and sequences), so they scale.
-DRAM_BYTES_PER_CELL = {"extd2": 1038595072 / 674520661, "extz2": None, "ll_i16": 111992832 / 11259234900}
+# All grow with the cells a launch processes (traceback rows and sequences), so they scale.
+DRAM_BYTES_PER_CELL = {"extd2": (188659200 + 791366144) / 674520661, "extz2": (129133568 + 261759488) / 146499977,
+                       "ll_i16": 111992832 / 11259234900}
 
 WORKLOADS = {
     "cfg1": "cfg1: 1M extd2 extension pairs, 100-300 nt, w=100, CIGAR",

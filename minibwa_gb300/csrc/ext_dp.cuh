@@ -73,7 +73,8 @@ __device__ __forceinline__ uint32_t lanes_upto(int to) {
 __device__ __forceinline__ uint32_t lanes_from(int from) {
   return __funnelshift_lc(0u, 0xffffffffu, (uint32_t)max(8 * from, 0));
 }
-// query bytes of four consecutive cells: lane j = query[hi - j], 0 outside [0, qlen)
+// query bytes of four consecutive cells: lane j = query[hi - j], 0 outside [0, qlen) (the
+// 16-bit kernel carries them from anti-diagonal to anti-diagonal)
 __device__ __forceinline__ uint32_t ld_qw(const uint8_t *qp, int hi, int qlen) {
   uint32_t w = 0;
 #pragma unroll
@@ -89,14 +90,11 @@ __device__ __forceinline__ uint32_t ld_qw(const uint8_t *qp, int hi, int qlen) {
 #ifndef KSW2G_EXT_MINB4
 #define KSW2G_EXT_MINB4 4  // resident blocks per SM asked of shapes with K <= 4
 #endif
-#ifndef KSW2G_EXT_MINB8
-#define KSW2G_EXT_MINB8 2  // resident blocks per SM asked of shapes with K > 5
-#endif
 // resident blocks per SM asked of a shape: two-word shapes fit five (extd2) or six (extz2)
 // blocks of 128 threads without spilling
 template <int VAR, int K>
 constexpr int ext_min_blocks() {
-  return K <= 2 ? (VAR ? 5 : 6) : K <= 4 ? KSW2G_EXT_MINB4 : K <= 5 ? 3 : KSW2G_EXT_MINB8;
+  return K <= 2 ? (VAR ? 5 : 6) : K <= 4 ? KSW2G_EXT_MINB4 : K <= 5 ? 3 : 2;
 }
 template <int VAR, int MODE, int G, int K>
 __global__ void __launch_bounds__(128, ext_min_blocks<VAR, K>())
@@ -129,10 +127,6 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
 
   // per-slot state
   uint32_t U[K], V[K], X[K], Y[K], X2[K], Y2[K], S[K + 1], TW[K + 1];
-  // query bytes of the cells of every unit on this anti-diagonal (lane j of unit i holds
-  // query[r - t] of cell t = base + 4*(k + G*i) + j); they move one cell right per
-  // anti-diagonal, so each unit takes one byte from its left neighbour instead of loading
-  uint32_t QW[K];
   int32_t H0[K], H1[K], H2[K], H3[K];
 
   // per-group state (identical in every thread of the group)
@@ -192,8 +186,6 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         }
 #pragma unroll
         for (int i = 0; i <= K; ++i) S[i] = s_init4, TW[i] = ld_tw(tp, 4 * (k + G * i), tlen);
-#pragma unroll
-        for (int i = 0; i < K; ++i) QW[i] = 0u;  // anti-diagonal -1: every query index is negative
       }
     }
     if (__all_sync(0xffffffffu, !active)) break;
@@ -231,16 +223,12 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           }
           shift4<G, K + 1>(S, s_init4, k, gm);
           shift4<G, K + 1>(TW, 0u, k, gm);
-          shift4<G, K>(QW, 0u, k, gm);
           shift4<G, K>(H0, (int32_t)KSW2G_NEG_INF, k, gm);
           shift4<G, K>(H1, (int32_t)KSW2G_NEG_INF, k, gm);
           shift4<G, K>(H2, (int32_t)KSW2G_NEG_INF, k, gm);
           shift4<G, K>(H3, (int32_t)KSW2G_NEG_INF, k, gm);
           wb = stb;
-          if (k >= G - 4) {
-            TW[K] = ld_tw(tp, (wb << 4) + 4 * (k + G * K), tlen);
-            QW[K - 1] = ld_qw(qp, r - 1 - ((wb << 4) + 4 * (k + G * (K - 1))), qlen);  // the last anti-diagonal's
-          }
+          if (k >= G - 4) TW[K] = ld_tw(tp, (wb << 4) + 4 * (k + G * K), tlen);
           x1 = xr, v1 = vr, x21 = x2r;  // (r-1, st-1) was computed on the last anti-diagonal
         } else {
           x1 = initb, v1 = initb, x21 = init2b;
@@ -277,31 +265,6 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             if (D2) Y2[i] = e ? (Y2[i] & keep) | (init2b << sh) : Y2[i];
           }
         }
-        // last bytes of x, v, x2 and of the query window of every word, packed, and handed to
-        // the next word's owner; the first word takes the boundary bytes and the query byte
-        // entering the window
-        uint32_t rv[K];
-        {
-          uint32_t pk[K];
-#pragma unroll
-          for (int i = 0; i < K; ++i) {
-            pk[i] = __byte_perm(X[i], V[i], 0x0073);
-            if (D2) pk[i] = __byte_perm(pk[i], X2[i], 0x0710);
-            pk[i] = __byte_perm(pk[i], QW[i], 0x7210);
-          }
-#pragma unroll
-          for (int i = 0; i < K; ++i) {
-            const uint32_t send = (k == G - 1) ? (i > 0 ? pk[i > 0 ? i - 1 : 0] : 0u) : pk[i];
-            rv[i] = __shfl_sync(gm, send, (k - 1) & (G - 1), G);
-          }
-          if (k == 0) {
-            const int qi = r - base;
-            const uint32_t qin = qi >= 0 && qi < qlen ? (uint32_t)__ldg(qp + qi) : 0u;
-            rv[0] = x1 | (v1 << 8) | (x21 << 16) | (qin << 24);
-          }
-#pragma unroll
-          for (int i = 0; i < K; ++i) QW[i] = __byte_perm(rv[i], QW[i], 0x6543);
-        }
         // ---- substitution scores written by the 16-byte stores from st0 (ksw2_extz2_sse.c:117-136) ----
         {
           const bool generic = flag & KSW2G_GENERIC_SC;
@@ -316,17 +279,14 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
 #pragma unroll
           for (int i = 0; i <= K; ++i) {
             const int p0 = base + 4 * (k + G * i);
-            // Slots 0..K-1 run without a branch (a word outside [st0, fend] gets a zero byte
-            // mask); the extra slot K is mostly outside, keeps the branch and loads its query.
+            // Slots 0..K-1 run without a branch: a word outside [st0, fend] reads the query
+            // at an index clamped into the range the words inside read, and its byte mask is 0.
+            // The extra slot K is mostly outside and keeps the branch.
             if (i < K || (p0 + 3 >= st0 && p0 <= fend)) {
-              uint32_t Qw;
-              if (i < K) {
-                Qw = QW[i];
-              } else {
-                const int idx0 = max(r - p0 - 3, r - fend - 3);
-                const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
-                Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
-              }
+              // words of slots 1.. start above st0 (the window starts at st0's 16-cell block)
+              const int idx0 = i == 0 ? min(max(r - p0 - 3, r - fend - 3), r - st0) : max(r - p0 - 3, r - fend - 3);
+              const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
+              const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
               const uint32_t Tw = TW[i];
               // lanes with t | q <= 4 (codes 0-3, or N = 4 against 0 or N): the lane index
               // (t ^ q) & 3 | (t | q) & 4 is 0 for a match, 1-3 for a mismatch and 4 for N, and
@@ -335,7 +295,6 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
               const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | (tq & 0x04040404u);
               const uint32_t sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
               bad |= tq | (tq + 0x03030303u);  // bits 3-7 of a lane set iff t | q >= 5
-              // slots above 0 start above st0 (the window starts at st0's 16-cell block)
               const uint32_t wm = i == 0 ? lanes_from(st0 - p0) & lanes_upto(fend - p0) : lanes_upto(fend - p0);
               S[i] = (S[i] & ~wm) | (sn & wm);
             }
@@ -345,14 +304,9 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             for (int i = 0; i <= K; ++i) {
               const int p0 = base + 4 * (k + G * i);
               if (p0 + 3 >= st0 && p0 <= fend) {
-                uint32_t Qw;
-                if (i < K) {
-                  Qw = QW[i];
-                } else {
-                  const int idx0 = r - p0 - 3;
-                  const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
-                  Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
-                }
+                const int idx0 = r - p0 - 3;
+                const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
+                const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
                 const uint32_t Tw = TW[i];
                 uint32_t sn;
                 if (!generic) {
@@ -381,6 +335,22 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
         const uint32_t extx = (!D2 && (x1 & 0x80)) ? 0xffffff00u : 0u;  // sign-extended _mm_cvtsi32_si128
         const uint32_t extv = (!D2 && (v1 & 0x80)) ? 0xffffff00u : 0u;
         uint32_t *row = CIG ? (uint32_t *)(tb + (size_t)r * ncol16) : nullptr;
+        // last bytes of x, v, x2 of every word, packed, and handed to the next word's owner
+        uint32_t rv[K];
+        {
+          uint32_t pk[K];
+#pragma unroll
+          for (int i = 0; i < K; ++i) {
+            pk[i] = __byte_perm(X[i], V[i], 0x0073);
+            if (D2) pk[i] = __byte_perm(pk[i], X2[i], 0x0710);
+          }
+#pragma unroll
+          for (int i = 0; i < K; ++i) {
+            const uint32_t send = (k == G - 1) ? (i > 0 ? pk[i > 0 ? i - 1 : 0] : 0u) : pk[i];
+            rv[i] = __shfl_sync(gm, send, (k - 1) & (G - 1), G);
+          }
+          if (k == 0) rv[0] = x1 | (v1 << 8) | (x21 << 16);
+        }
 #pragma unroll
         for (int i = 0; i < K; ++i) {
           const int wi = k + G * i;
