@@ -178,11 +178,15 @@ typedef struct {          /* mb_anchor_t (mbpriv.h:26-32) */
 	int64_t tpos;         /* contig coordinate of the anchor's last base */
 } ksw2g_anchor_t;
 typedef struct {          /* one hit: the fields of mb_hit_t that mb_align1 reads */
-	int32_t as, cnt;      /* anchors[as .. as+cnt) of the anchor array */
+	int64_t as;           /* anchors[as .. as+cnt) of the anchor array */
+	int64_t qoff;         /* the read in qbuf, in the orientation aligned (seq[rev]) */
+	int32_t cnt;
 	int32_t mlen, score;  /* r->mlen, r->score */
-	int32_t qoff, qlen;   /* the read in qbuf, in the orientation aligned (seq[rev]) */
-	int32_t meth;         /* methylation mode as mb_align1 receives it (flipped for rev strands) */
+	int32_t qlen;
+	int32_t meth;         /* the read's methylation mode as mb_align1 receives it (flipped for rev strands) */
 	int32_t split_inv;    /* r->split_inv */
+	int32_t opt;          /* index of the hit's option set (mb_opt_adap varies them with the read length) */
+	int32_t pad;
 } ksw2g_chain_t;
 typedef struct {          /* the mb_opt_t fields mb_align1 reads */
 	int32_t a, b, b_ts, b_ambi, q, e, q2, e2;
@@ -206,8 +210,12 @@ typedef struct {
 	int32_t n_dp;         /* DP jobs whose results the chain used */
 	int32_t n_dp_issued;  /* DP jobs issued for it (the speculative ones included) */
 } ksw2g_chain_result_t;
-int ksw2g_align_chains(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, const ksw2g_chain_opt_t *opt, int n_chains,
-					   const ksw2g_chain_t *chains, const ksw2g_anchor_t *anchors, int64_t n_anchors,
+/* opts: n_opts option sets that agree in their scores (a, b, b_ts, b_ambi, q, e, q2, e2, meth,
+ * max_sw_mat).  As mb_align1 does, the call sets MB_SEED_IGNORE / MB_SEED_LONG_JOIN in the
+ * flags of the anchors of long-read hits; a hit split off by a z-drop is aligned by a later
+ * call over the anchors so flagged.  CIGARs go to cigar[cigar_off ..] in hit order. */
+int ksw2g_align_chains(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int n_opts, const ksw2g_chain_opt_t *opts,
+					   int n_chains, const ksw2g_chain_t *chains, ksw2g_anchor_t *anchors, int64_t n_anchors,
 					   const uint8_t *qbuf, int64_t qbuf_len, ksw2g_chain_result_t *res, uint32_t *cigar,
 					   int64_t cigar_cap, int64_t *cigar_used);
 

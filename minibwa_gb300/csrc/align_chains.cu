@@ -252,6 +252,7 @@ struct Job {
 };
 
 struct ChainWork {
+  const ksw2g_chain_opt_t *o = nullptr;  // the hit's options
   int as1 = 0, cnt1 = 0, is_sr = 1, rev = 0, mt = 0;
   int64_t tid = 0, ts0 = 0, te0 = 0;
   int32_t qs0 = 0, qe0 = 0;
@@ -266,16 +267,24 @@ struct ChainWork {
 
 }  // namespace
 
-extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const ksw2g_chain_opt_t *opt, int n,
-                                  const ksw2g_chain_t *chains, const ksw2g_anchor_t *anchors, int64_t n_anchors,
+// the scores every option set of one call must share: they fix the matrix and the DP batches
+bool same_scoring(const ksw2g_chain_opt_t &x, const ksw2g_chain_opt_t &y) {
+  return x.a == y.a && x.b == y.b && x.b_ts == y.b_ts && x.b_ambi == y.b_ambi && x.q == y.q && x.e == y.e &&
+         x.q2 == y.q2 && x.e2 == y.e2 && x.meth == y.meth && x.max_sw_mat == y.max_sw_mat;
+}
+
+extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_opts, const ksw2g_chain_opt_t *opts,
+                                  int n, const ksw2g_chain_t *chains, ksw2g_anchor_t *anchors, int64_t n_anchors,
                                   const uint8_t *qbuf, int64_t qbuf_len, ksw2g_chain_result_t *res, uint32_t *cigar,
                                   int64_t cigar_cap, int64_t *cigar_used) {
-  if (!c || !ref || !opt || n < 0 || n_anchors < 0 || (n > 0 && (!chains || !res || !qbuf)))
+  if (!c || !ref || n < 0 || n_anchors < 0 || n_opts <= 0 || !opts || (n > 0 && (!chains || !res || !qbuf || !anchors)))
     return report_error(KSW2G_E_ARG, "align_chains: bad arguments");
   if (cigar_used) *cigar_used = 0;
   if (n == 0) return 0;
-  const ksw2g_chain_opt_t &o = *opt;
-  if (o.e <= 0 || o.e2 <= 0 || o.a <= 0) return report_error(KSW2G_E_ARG, "align_chains: a, e and e2 must be positive");
+  const ksw2g_chain_opt_t &S = opts[0];  // scoring
+  if (S.e <= 0 || S.e2 <= 0 || S.a <= 0) return report_error(KSW2G_E_ARG, "align_chains: a, e and e2 must be positive");
+  for (int k = 1; k < n_opts; ++k)
+    if (!same_scoring(S, opts[k])) return report_error(KSW2G_E_ARG, "align_chains: option sets differ in scoring");
   int rc;
   std::vector<ChainWork> W(n);
   int64_t tbuf_len = 0;
@@ -287,8 +296,10 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     res[ci].cigar_off = -1, res[ci].cnt = h.cnt, res[ci].score = h.score;
     if (h.cnt <= 0) continue;
     if (h.as < 0 || h.as + (int64_t)h.cnt > n_anchors || h.qoff < 0 || h.qlen < 0 || h.qoff + (int64_t)h.qlen > qbuf_len ||
-        h.meth < 0 || h.meth > 2)
+        h.meth < 0 || h.meth > 2 || h.opt < 0 || h.opt >= n_opts)
       return report_error(KSW2G_E_ARG, "align_chains: chain out of bounds");
+    const ksw2g_chain_opt_t &o = opts[h.opt];
+    cw.o = &o;
     cw.a.assign(anchors + h.as, anchors + h.as + h.cnt);
     ksw2g_anchor_t *a = cw.a.data();  // indices relative to the hit's first anchor
     const int qlen = h.qlen;
@@ -311,6 +322,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
       fix_bad_ends(a, 0, h.cnt, h.mlen, o.bw, o.min_chain_score * 2, cw.as1, cw.cnt1);
       filter_bad_seeds(a, cw.as1, cw.cnt1, 10, 40, o.max_gap >> 1, 10);
       filter_bad_seeds_alt(a, cw.as1, cw.cnt1, 30, o.max_gap >> 1);
+      for (int k = 0; k < h.cnt; ++k) anchors[h.as + k].flag = a[k].flag;  // mb_align1 filters the caller's anchors
     }
     const ksw2g_anchor_t &f = a[cw.as1], &g = a[cw.as1 + cw.cnt1 - 1];
     int64_t ts = f.tpos + 1 - f.len + min32(f.len >> 1, max_back);
@@ -466,7 +478,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     }
   }
   // ---- one mb_align_pair batch per (pass, methylation mode); left extensions run on reversed sequences
-  ksw2g_align_opt_t ao{o.a, o.b, o.b_ts, o.b_ambi, o.q, o.e, o.q2, o.e2, o.meth ? 1 : 0, 0, o.max_sw_mat};
+  ksw2g_align_opt_t ao{S.a, S.b, S.b_ts, S.b_ambi, S.q, S.e, S.q2, S.e2, S.meth ? 1 : 0, 0, S.max_sw_mat};
   struct Out {
     std::vector<ksw2g_ext_result_t> res;
     std::vector<uint32_t> cig;
@@ -493,7 +505,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
             qb.insert(qb.end(), qsrc, qsrc + ql), tb.insert(tb.end(), tsrc, tsrc + tl);
           }
           int zd = j.zdrop, fl = j.flag;
-          if (p == 1) zd = j.zcode == 2 ? o.zdrop_inv : o.zdrop, fl = 0;  // second pass: exact maximum (align.c:693)
+          if (p == 1) zd = j.zcode == 2 ? cw.o->zdrop_inv : cw.o->zdrop, fl = 0;  // exact maximum (align.c:693)
           (p == 0 ? j.pass1 : j.pass2) = (int)jobs.size();
           jobs.push_back(ksw2g_job_t{qo, to, ql, tl, j.w, zd, j.end_bonus, fl});
           cap += ql + tl + 1;
@@ -506,7 +518,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
       if (qb.empty()) qb.push_back(0);  // every window empty: the batch still takes a valid buffer
       if (tb.empty()) tb.push_back(0);
       int8_t mat[25];
-      gen_mat(mat, o.a, o.b, o.b_ts, o.b_ambi, mt);
+      gen_mat(mat, S.a, S.b, S.b_ts, S.b_ambi, mt);
       int64_t used = 0;
       const int r = ksw2g_align_pairs(c, &ao, mat, (int)jobs.size(), jobs.data(), qb.data(), (int64_t)qb.size(),
                                       tb.data(), (int64_t)tb.size(), out.res.data(), out.cig.data(),
@@ -529,15 +541,16 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     std::vector<Inv> inv[3];
     for (int ci = 0; ci < n; ++ci) {
       ChainWork &cw = W[ci];
+      const ksw2g_chain_opt_t &o = *cw.o;
       int8_t mat[25];
-      gen_mat(mat, o.a, o.b, o.b_ts, o.b_ambi, cw.mt);
+      gen_mat(mat, S.a, S.b, S.b_ts, S.b_ambi, cw.mt);
       for (size_t ji = 0; ji < cw.jobs.size(); ++ji) {
         Job &j = cw.jobs[ji];
         if (j.kind != 1) continue;
         const ksw2g_ext_result_t &E = pass[0][cw.mt].res[j.pass1];
         const uint8_t *qs = qbuf + chains[ci].qoff + j.qs, *ts = tbuf.data() + cw.win_off + (j.ts - cw.ts0);
         int pos[2][2];
-        const int32_t mz = cigar_zdrop(o, qs, ts, pass[0][cw.mt].cig.data() + (E.n_cigar > 0 ? E.cigar_off : 0),
+        const int32_t mz = cigar_zdrop(S, qs, ts, pass[0][cw.mt].cig.data() + (E.n_cigar > 0 ? E.cigar_off : 0),
                                        E.n_cigar > 0 ? E.n_cigar : 0, mat, pos);
         j.zcode = mz > o.zdrop ? 1 : 0;
         const int q_len = pos[1][1] - pos[1][0], t_len = pos[0][1] - pos[0][0];
@@ -555,7 +568,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     for (int mt = 0; mt < 3; ++mt) {
       if (inv[mt].empty()) continue;
       int8_t mat[25];
-      gen_mat(mat, o.a, o.b, o.b_ts, o.b_ambi, mt);
+      gen_mat(mat, S.a, S.b, S.b_ts, S.b_ambi, mt);
       std::vector<ksw2g_ll_job_t> lj;
       std::vector<uint8_t> qb, tb;
       for (const Inv &v : inv[mt]) {
@@ -566,11 +579,12 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
       std::vector<ksw2g_ll_result_t> lr(lj.size());
       if (qb.empty()) qb.push_back(0);
       if (tb.empty()) tb.push_back(0);
-      if ((rc = ksw2g_ll_batch(c, 2, 5, mat, o.q, o.e, (int)lj.size(), lj.data(), qb.data(), (int64_t)qb.size(),
+      if ((rc = ksw2g_ll_batch(c, 2, 5, mat, S.q, S.e, (int)lj.size(), lj.data(), qb.data(), (int64_t)qb.size(),
                                tb.data(), (int64_t)tb.size(), lr.data())))
         return rc;
       for (size_t k = 0; k < lj.size(); ++k) {  // ksw_ll_i16's score (align.c:63-65)
         const int32_t s = lr[k].score;
+        const ksw2g_chain_opt_t &o = *W[inv[mt][k].ci].o;
         if (s >= o.min_chain_score * o.a && s >= o.min_dp_max * o.a) W[inv[mt][k].ci].jobs[inv[mt][k].ji].zcode = 2;
       }
     }
@@ -583,6 +597,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     ChainWork &cw = W[ci];
     ksw2g_chain_result_t &R = res[ci];
     if (h.cnt <= 0) continue;
+    const ksw2g_chain_opt_t &o = *cw.o;
     std::vector<uint32_t> cg;
     int32_t dp_score = 0;
     int n_dp = 0;

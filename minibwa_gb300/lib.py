@@ -52,7 +52,8 @@ assert RESCUE_OPT.itemsize == 44 and RESCUE_JOB.itemsize == 48 and RESCUE_RESULT
 
 # ksw2g_anchor_t / ksw2g_chain_t / ksw2g_chain_opt_t / ksw2g_chain_result_t (include/ksw2_gb300.h)
 ANCHOR = np.dtype([("sid", "<i4"), ("len", "<i4"), ("qpos", "<i4"), ("flag", "<u4"), ("tpos", "<i8")])
-CHAIN = np.dtype([(k, "<i4") for k in ("as", "cnt", "mlen", "score", "qoff", "qlen", "meth", "split_inv")])
+CHAIN = np.dtype([("as", "<i8"), ("qoff", "<i8")] + [(k, "<i4") for k in ("cnt", "mlen", "score", "qlen", "meth",
+                                                                          "split_inv", "opt", "pad")])
 CHAIN_OPT = np.dtype([(k, "<i4") for k in ("a", "b", "b_ts", "b_ambi", "q", "e", "q2", "e2", "bw", "bw_long",
                                              "max_gap", "end_bonus", "zdrop", "zdrop_inv", "min_ksw_len", "min_len",
                                              "min_chain_score", "min_dp_max", "long_reads", "adaptive", "max_sr_len",
@@ -138,7 +139,7 @@ def load_library():
         "ksw2g_ll_batch_ref": (i32, [vp, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp, u8p, i64, vp]),
         "ksw2g_rescue_batch": (i32, [vp, vp, vp, i32, vp, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_rescue_last_stats": (i32, [vp, vp, vp]),
-        "ksw2g_align_chains": (i32, [vp, vp, vp, i32, vp, vp, i64, u8p, i64, vp, vp, i64, C.POINTER(i64)]),
+        "ksw2g_align_chains": (i32, [vp, vp, i32, vp, i32, vp, vp, i64, u8p, i64, vp, vp, i64, C.POINTER(i64)]),
         "ksw2g_align_pairs": (i32, [vp, vp, vp, i32, vp, u8p, i64, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_graph_create": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
         "ksw2g_graph_launch": (i32, [vp, vp]),
@@ -479,25 +480,31 @@ class Reference:
                                          _ptr(res), _ptr(cig), cap, C.byref(used)))
         return res, cig[:used.value]
 
-    def align_chains(self, opt, chains, anchors, qbuf, cigar_cap=None):
-        """mb_align1 over many hits at once (ksw2g_align_chains): opt a dict or CHAIN_OPT record,
-        chains a CHAIN array indexing anchors (ANCHOR) and qbuf (each read in the orientation it
-        aligns in).  Returns (CHAIN_RESULT array, CIGAR words)."""
-        if isinstance(opt, dict):
-            o = np.zeros(1, CHAIN_OPT)
+    def align_chains(self, opts, chains, anchors, qbuf, cigar_cap=None):
+        """mb_align1 over many hits at once (ksw2g_align_chains): opts one option set (a dict or
+        CHAIN_OPT record) or a list of them that chains["opt"] indexes, chains records with the
+        CHAIN fields (extra fields are ignored, missing ones are 0) indexing anchors (ANCHOR; their
+        flags are updated in place when it is an ANCHOR array) and qbuf (each read in the
+        orientation it aligns in).  Returns (CHAIN_RESULT array, CIGAR words)."""
+        if isinstance(opts, dict) or (isinstance(opts, np.ndarray) and opts.dtype == CHAIN_OPT and opts.ndim == 0):
+            opts = [opts]
+        o = np.zeros(len(opts), CHAIN_OPT)
+        for i, x in enumerate(opts):
             for k in CHAIN_OPT.names:
-                o[k] = opt[k]
-            opt = o
-        opt = np.ascontiguousarray(opt, CHAIN_OPT)
-        chains = np.ascontiguousarray(chains, CHAIN)
-        anchors = np.ascontiguousarray(anchors, ANCHOR)
+                o[i][k] = x[k]
+        ch = np.zeros(len(chains), CHAIN)
+        for k in CHAIN.names:
+            if chains.dtype.names and k in chains.dtype.names:
+                ch[k] = chains[k]
+        if not (isinstance(anchors, np.ndarray) and anchors.dtype == ANCHOR and anchors.flags.c_contiguous):
+            anchors = np.ascontiguousarray(anchors, ANCHOR)
         qbuf = _u8(qbuf)
-        res = np.zeros(len(chains), CHAIN_RESULT)
+        res = np.zeros(len(ch), CHAIN_RESULT)
         if cigar_cap is None:
-            cigar_cap = int(2 * chains["qlen"].astype(np.int64).sum() + 4 * chains["cnt"].astype(np.int64).sum()) + 64
+            cigar_cap = int(2 * ch["qlen"].astype(np.int64).sum() + 4 * ch["cnt"].astype(np.int64).sum()) + 64
         cig = np.zeros(max(int(cigar_cap), 1), np.uint32)
         used = C.c_int64()
-        _check(self.L.ksw2g_align_chains(self.ctx.h, self.h, _ptr(opt), len(chains), _ptr(chains), _ptr(anchors),
+        _check(self.L.ksw2g_align_chains(self.ctx.h, self.h, len(o), _ptr(o), len(ch), _ptr(ch), _ptr(anchors),
                                          len(anchors), _ptr(qbuf), len(qbuf), _ptr(res), _ptr(cig), int(cigar_cap),
                                          C.byref(used)))
         return res, cig[:used.value]

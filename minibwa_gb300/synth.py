@@ -582,3 +582,127 @@ class ChainCases:
     def read(self, i):
         c = self.chains[i]
         return self.qbuf[c["qoff"]:c["qoff"] + c["qlen"]]
+
+
+# ---- genomes and reads for whole-mapper runs (FASTA in, SAM out)
+
+_ACGTN = np.frombuffer(b"ACGTN", np.uint8)
+
+
+def _mutate_fast(rng, s, sub, indel):
+    """Substitutions at rate sub, then indels of 1-3 bases at rate indel (half insertions),
+    without a per-base Python loop."""
+    s = s.copy()
+    m = rng.random(len(s)) < sub
+    s[m] = (s[m] + rng.integers(1, 4, int(m.sum()))).astype(np.uint8) % 4
+    ev = np.nonzero(rng.random(len(s)) < indel)[0]
+    if len(ev) == 0:
+        return s
+    keep = np.ones(len(s), bool)
+    ins_at, ins = [], []
+    for p in ev:
+        ln = int(rng.integers(1, 4))
+        if rng.random() < 0.5:
+            keep[p:p + ln] = False
+        else:
+            ins_at.append(p), ins.append(rng.integers(0, 4, ln).astype(np.uint8))
+    if ins:
+        s = np.insert(s, np.repeat(ins_at, [len(x) for x in ins]), np.concatenate(ins))
+        keep = np.insert(keep, np.repeat(ins_at, [len(x) for x in ins]), True)
+    return s[keep]
+
+
+def mapper_genome(ctg_len=(2_000_000, 1_200_000, 800_000), seed=SEED + 80, n_repeats=300, n_runs=20):
+    """Contigs of random bases with near-copies of segments (300 of 200-3000 bases, 2%
+    diverged) and runs of N; returns a list of (name, uint8 codes 0-4)."""
+    rng = np.random.default_rng(seed)
+    ctgs = [rng.integers(0, 4, n).astype(np.uint8) for n in ctg_len]
+    for _ in range(n_repeats):
+        a, b = (int(x) for x in rng.integers(0, len(ctgs), 2))
+        ln = int(rng.integers(200, 3000))
+        sa, sb = int(rng.integers(0, len(ctgs[a]) - ln)), int(rng.integers(0, len(ctgs[b]) - ln))
+        seg = _mutate_fast(rng, ctgs[a][sa:sa + ln], 0.02, 0.0)
+        ctgs[b][sb:sb + ln] = seg[:ln]
+    for _ in range(n_runs):
+        k = int(rng.integers(0, len(ctgs)))
+        ln, st = int(rng.integers(1, 400)), int(rng.integers(0, len(ctgs[k]) - 400))
+        ctgs[k][st:st + ln] = 4
+    return [(f"ctg{k + 1}", c) for k, c in enumerate(ctgs)]
+
+
+def write_fasta(fn, seqs, width=0):
+    with open(fn, "w") as f:
+        for name, s in seqs:
+            f.write(f">{name}\n{_ACGTN[s].tobytes().decode()}\n")
+
+
+def mapper_pairs(genome, n, rl=150, ins_mean=350, ins_sd=50, seed=SEED + 81, sub=0.015, indel=0.002,
+                 p_noisy=0.08, p_junk=0.04, p_chimera=0.03):
+    """n read pairs (FR orientation) from the genome: substitutions and short indels, some mates
+    noisy (12% substitutions: mate rescue), some with a random tail (z-drop) or a chimeric
+    second half.  Returns (reads 1, reads 2) as lists of (name, codes)."""
+    rng = np.random.default_rng(seed)
+    lens = np.array([len(c) for _, c in genome], np.float64)
+    r1, r2 = [], []
+    while len(r1) < n:
+        k = int(rng.choice(len(genome), p=lens / lens.sum()))
+        g = genome[k][1]
+        ins = max(rl + 20, int(rng.normal(ins_mean, ins_sd)))
+        if len(g) < ins + 200:
+            continue
+        st = int(rng.integers(0, len(g) - ins - 50))
+        frag = g[st:st + ins + 40]
+        if rng.random() < 0.5:
+            frag = _revcomp(frag)
+        a = _mutate_fast(rng, frag[:rl + 20], sub, indel)[:rl]
+        b = _revcomp(_mutate_fast(rng, frag[ins - rl - 20:ins], sub, indel)[-rl:])
+        u = rng.random()
+        if u < p_noisy:
+            b = _mutate_fast(rng, b, 0.12, 0.0)
+        elif u < p_noisy + p_junk:
+            t = int(rng.integers(20, 70))
+            a = np.concatenate([a[:rl - t], rng.integers(0, 4, t).astype(np.uint8)])
+        elif u < p_noisy + p_junk + p_chimera:
+            k2 = int(rng.integers(0, len(genome)))
+            g2 = genome[k2][1]
+            s2 = int(rng.integers(0, len(g2) - rl))
+            a = np.concatenate([a[:rl // 2], g2[s2:s2 + rl - rl // 2]])
+        if len(a) < 30 or len(b) < 30:
+            continue
+        nm = f"p{len(r1)}"
+        r1.append((nm + "/1", a)), r2.append((nm + "/2", b))
+    return r1, r2
+
+
+def mapper_long_reads(genome, n, lo=1000, hi=8000, seed=SEED + 82, sub=0.05, indel=0.03, p_inv=0.15, p_junk=0.1,
+                      p_chimera=0.05):
+    """n long reads: 5% substitutions and 3% indels, some with an inverted segment (the
+    inversion check), a random block (a z-drop inside the chain) or a chimeric junction."""
+    rng = np.random.default_rng(seed)
+    lens = np.array([len(c) for _, c in genome], np.float64)
+    out = []
+    while len(out) < n:
+        k = int(rng.choice(len(genome), p=lens / lens.sum()))
+        g = genome[k][1]
+        L = int(rng.integers(lo, hi))
+        if len(g) < L + 100:
+            continue
+        st = int(rng.integers(0, len(g) - L))
+        s = g[st:st + L].copy()
+        u = rng.random()
+        if u < p_inv:
+            a, ln = int(rng.integers(L // 4, L // 2)), int(rng.integers(150, min(1500, L // 3)))
+            s[a:a + ln] = _revcomp(s[a:a + ln])
+        elif u < p_inv + p_junk:
+            a, ln = int(rng.integers(L // 4, L // 2)), int(rng.integers(100, 600))
+            s[a:a + ln] = rng.integers(0, 4, len(s[a:a + ln]))
+        elif u < p_inv + p_junk + p_chimera:
+            k2 = int(rng.integers(0, len(genome)))
+            g2 = genome[k2][1]
+            s2 = int(rng.integers(0, len(g2) - L // 2))
+            s = np.concatenate([s[:L // 2], g2[s2:s2 + L // 2]])
+        s = _mutate_fast(rng, s, sub, indel)
+        if rng.random() < 0.5:
+            s = _revcomp(s)
+        out.append((f"l{len(out)}", s))
+    return out

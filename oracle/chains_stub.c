@@ -1,0 +1,122 @@
+/* chains_stub.c -- ksw2g_align_chains computed by the reference's own mb_align1 on the CPU
+ * (TEST INFRASTRUCTURE ONLY).
+ *
+ * The batched minibwa (minibwa_gb300/mapper) calls five functions of libksw2gpu.so:
+ * ksw2g_ctx_create, ksw2g_ref_create, ksw2g_ref_destroy, ksw2g_align_chains and
+ * ksw2g_last_error.  This file provides them over the reference's align.c (included as
+ * _ref/align_noextra.c, mb_update_extra at the end of mb_align1 left out, as the device entry
+ * point leaves it to its caller): each hit goes through mb_align1 as mb_align_skeleton would
+ * call it.  Linked with the reference's ksw2 sources in place of libksw2gpu.so (make
+ * mbgstub), the batched mapper then runs without a GPU, so the host side of the batched
+ * pipeline -- deferral, rounds of split-off hits, the finishing pass -- can be checked for
+ * byte-identical SAM on any machine that has the reference tree.  The device entry point
+ * itself is pinned to mb_align1 separately (tests/test_gpu_chains.py). */
+#include <stdlib.h>
+#include <string.h>
+
+#include "align_noextra.c"
+#include "ksw2_gb300.h"
+
+struct ksw2g_ctx { int device; };
+struct ksw2g_ref { l2b_t l2b; };
+
+const char *ksw2g_last_error(void) { return "chains stub"; }
+
+int ksw2g_ctx_create(int device, ksw2g_ctx_t **ctx)
+{
+	*ctx = (ksw2g_ctx_t*)calloc(1, sizeof(ksw2g_ctx_t));
+	(*ctx)->device = device;
+	return 0;
+}
+
+int ksw2g_ref_create(ksw2g_ctx_t *ctx, int64_t n_ctg, const uint64_t *ctg_off, const uint64_t *ctg_len,
+                     const uint64_t *pac, int64_t n_pac, int64_t n_ambi, const uint64_t *ambi, ksw2g_ref_t **ref)
+{
+	ksw2g_ref_t *r = (ksw2g_ref_t*)calloc(1, sizeof(ksw2g_ref_t));
+	int64_t k;
+	(void)ctx;
+	r->l2b.n_ctg = r->l2b.m_ctg = n_ctg;
+	r->l2b.ctg = (l2b_ctg_t*)calloc(n_ctg + 1, sizeof(l2b_ctg_t));
+	for (k = 0; k < n_ctg; ++k)
+		r->l2b.ctg[k].off = ctg_off[k], r->l2b.ctg[k].len = ctg_len[k], r->l2b.tot_len += ctg_len[k];
+	r->l2b.pac = (uint64_t*)pac, r->l2b.n_pac = r->l2b.m_pac = n_pac;
+	r->l2b.n_ambi = r->l2b.m_ambi = n_ambi, r->l2b.ambi = (l2b_intv_t*)ambi;
+	*ref = r;
+	return 0;
+}
+
+void ksw2g_ref_destroy(ksw2g_ref_t *ref)
+{
+	if (ref) free(ref->l2b.ctg), free(ref);
+}
+
+static void stub_opt(const ksw2g_chain_opt_t *c, mb_opt_t *o)
+{
+	memset(o, 0, sizeof(*o));
+	o->a = c->a, o->b = c->b, o->b_ts = c->b_ts, o->b_ambi = c->b_ambi;
+	o->q = c->q, o->e = c->e, o->q2 = c->q2, o->e2 = c->e2;
+	o->bw = c->bw, o->bw_long = c->bw_long, o->max_gap = c->max_gap, o->end_bonus = c->end_bonus;
+	o->zdrop = c->zdrop, o->zdrop_inv = c->zdrop_inv, o->min_ksw_len = c->min_ksw_len, o->min_len = c->min_len;
+	o->min_chain_score = c->min_chain_score, o->min_dp_max = c->min_dp_max;
+	if (c->long_reads) o->flag |= MB_F_LONG;
+	if (c->adaptive) o->flag |= MB_F_ADAP;
+	o->max_sr_len = c->max_sr_len;
+	if (c->meth) o->flag |= MB_F_METH;
+	o->max_sw_mat = c->max_sw_mat;
+}
+
+int ksw2g_align_chains(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int n_opts, const ksw2g_chain_opt_t *opts,
+                       int n_chains, const ksw2g_chain_t *chains, ksw2g_anchor_t *anchors, int64_t n_anchors,
+                       const uint8_t *qbuf, int64_t qbuf_len, ksw2g_chain_result_t *res, uint32_t *cigar,
+                       int64_t cigar_cap, int64_t *cigar_used)
+{
+	mb_idx_t mi;
+	mb_anchor_t *a;
+	ksw_extz_t ez;
+	int64_t k, used = 0;
+	int i;
+	(void)ctx, (void)qbuf_len;
+	memset(&mi, 0, sizeof mi);
+	mi.l2b = (l2b_t*)&ref->l2b;
+	a = (mb_anchor_t*)calloc(n_anchors + 1, sizeof(mb_anchor_t));
+	for (k = 0; k < n_anchors; ++k) {
+		a[k].sid = anchors[k].sid, a[k].len = anchors[k].len, a[k].qpos = anchors[k].qpos;
+		a[k].flag = anchors[k].flag & 0x7fffffffu, a[k].flt = anchors[k].flag >> 31, a[k].tpos = anchors[k].tpos;
+	}
+	memset(&ez, 0, sizeof ez);
+	for (i = 0; i < n_chains; ++i) {
+		const ksw2g_chain_t *h = &chains[i];
+		ksw2g_chain_result_t *R = &res[i];
+		mb_opt_t opt;
+		mb_hit_t r, r2;
+		uint8_t *qseq0[2];
+		int rev;
+		if (h->opt < 0 || h->opt >= n_opts) return KSW2G_E_ARG;
+		stub_opt(&opts[h->opt], &opt);
+		memset(&r, 0, sizeof r), memset(&r2, 0, sizeof r2), memset(R, 0, sizeof(*R));
+		R->cigar_off = -1, R->cnt = h->cnt, R->score = h->score;
+		if (h->cnt <= 0) continue;
+		rev = a[h->as].sid & 1;
+		qseq0[rev] = (uint8_t*)qbuf + h->qoff; // the other orientation is not read with mb_update_extra left out
+		qseq0[!rev] = (uint8_t*)qbuf + h->qoff;
+		r.as = (int32_t)h->as, r.cnt = h->cnt, r.mlen = h->mlen, r.score = h->score, r.split_inv = h->split_inv;
+		r.tid = a[h->as].sid >> 1, r.rev = rev;
+		mb_align1(0, &opt, &mi, h->qlen, qseq0, (l2b_meth_t)h->meth, &r, &r2, (int)n_anchors, a, &ez);
+		R->ts = r.ts, R->te = r.te, R->qs = r.qs, R->qe = r.qe, R->cnt = r.cnt, R->score = r.score;
+		if (r2.cnt > 0) R->split_n = r2.as - (int32_t)h->as, R->split_inv2 = r2.split_inv;
+		if (r.p) {
+			R->dp_score = r.p->dp_score, R->n_cigar = r.p->n_cigar;
+			if (cigar) {
+				if (used + r.p->n_cigar > cigar_cap) { free(r.p), free(a), free(ez.cigar); return KSW2G_E_CAPACITY; }
+				memcpy(cigar + used, r.p->cigar, (size_t)r.p->n_cigar * 4);
+				R->cigar_off = used;
+			}
+			used += r.p->n_cigar;
+			free(r.p);
+		}
+	}
+	for (k = 0; k < n_anchors; ++k) anchors[k].flag = a[k].flag | (uint32_t)a[k].flt << 31;
+	free(a), free(ez.cigar);
+	if (cigar_used) *cigar_used = used;
+	return 0;
+}

@@ -97,6 +97,19 @@ def build_minibwa(gpulib_dir):
     return {k: os.path.join(HERE, "_ref", "minibwa_" + k) for k in ("stock", "gpu", "stock_km", "gpu_km")}
 
 
+def build_mbgstub():
+    """Compile the batched minibwa against _ref/libmbgstub.so (ksw2g_align_chains by the
+    reference's own mb_align1 on the CPU) and the stock minibwa; needs a reference tree.
+    Returns the paths of both (libc builds)."""
+    t = ref_tree()
+    if not t:
+        raise RuntimeError("no reference tree: set KSW2_REF_TREE or stage one (make -C oracle stage REF=...)")
+    j = f"-j{os.cpu_count() or 4}"
+    subprocess.check_call(["make", "-s", "-C", HERE, j, "mbgstub", "_ref/minibwa_stock", f"REF={t}"])
+    return dict(stock=os.path.join(HERE, "_ref", "minibwa_stock"),
+                batch=os.path.join(HERE, "_ref", "mbgstub", "minibwa_batch"))
+
+
 def have_ref():
     return os.path.exists(LIB_REF)
 

@@ -35,7 +35,7 @@ def test_chains_golden(dev):
     ref = Reference(dev, z["pac"], z["ctg_off"], z["ctg_len"], z["ambi"])
     for name, opt, idx in chain_sets(z):
         ch = z["chains"][idx.start:idx.stop]
-        res, cig = ref.align_chains(opt, ch, z["anchors"], z["qbuf"])
+        res, cig = ref.align_chains(opt, ch, z["anchors"].copy(), z["qbuf"])
         for k, i in enumerate(idx):
             got = as_align1(ch[k], res[k], cig)
             assert got == expected(z, i), (name, i)
@@ -53,10 +53,33 @@ def test_chains_oracle_fresh_seeds(dev):
                              (False, 300, dict(synth.CHAIN_OPT_SR, meth=1, b_ts=4), True),
                              (True, 24, dict(synth.CHAIN_OPT_LR, meth=1), True)):
         cs = synth.ChainCases(R, n, long_reads=lr, seed=311 + n, meth=meth)
-        res, cig = ref.align_chains(opt, cs.chains, cs.anchors, cs.qbuf)
+        res, cig = ref.align_chains(opt, cs.chains, cs.anchors.copy(), cs.qbuf)
         for i in range(len(cs)):
             exp = O.align1(R, opt, cs.anchors, cs.chains[i], cs.read(i))
             assert as_align1(cs.chains[i], res[i], cig) == exp, (lr, meth, i, cs.kind[i])
+    ref.close()
+
+
+def test_chains_several_option_sets(dev):
+    """One call over hits of three option sets that share their scores (short-read preset,
+    long-read preset, long reads under the short-read preset's adaptive switch)."""
+    from minibwa_gb300.lib import CHAIN, Reference
+    z = load_chains_golden()
+    ref = Reference(dev, z["pac"], z["ctg_off"], z["ctg_len"], z["ambi"])
+    sets = [s for s in chain_sets(z) if s[0] != "sr_meth"]
+    opts = [s[1] for s in sets]
+    idx = np.concatenate([np.arange(s[2].start, s[2].stop) for s in sets])
+    ch = np.zeros(len(idx), CHAIN)
+    for k in ("as", "qoff", "cnt", "mlen", "score", "qlen", "meth", "split_inv"):
+        ch[k] = z["chains"][k][idx]
+    ch["opt"] = np.concatenate([np.full(len(s[2]), i) for i, s in enumerate(sets)])
+    perm = np.random.default_rng(5).permutation(len(ch))  # hits of the sets interleaved
+    res, cig = ref.align_chains(opts, ch[perm], z["anchors"].copy(), z["qbuf"])
+    for k, p in enumerate(perm):
+        assert as_align1(ch[p], res[k], cig) == expected(z, int(idx[p])), int(idx[p])
+    meth_opt = next(s[1] for s in chain_sets(z) if s[0] == "sr_meth")
+    with pytest.raises(RuntimeError):  # option sets with other scores in one call
+        ref.align_chains([opts[0], meth_opt], ch[:2], z["anchors"].copy(), z["qbuf"])
     ref.close()
 
 
@@ -65,18 +88,18 @@ def test_chains_edges(dev):
     z = load_chains_golden()
     ref = Reference(dev, z["pac"], z["ctg_off"], z["ctg_len"], z["ambi"])
     opt = next(chain_sets(z))[1]
-    res, cig = ref.align_chains(opt, np.zeros(0, CHAIN), z["anchors"], z["qbuf"])
+    res, cig = ref.align_chains(opt, np.zeros(0, CHAIN), z["anchors"].copy(), z["qbuf"])
     assert len(res) == 0 and len(cig) == 0
     ch = z["chains"][:3].copy()
     ch[1]["cnt"] = 0  # mb_align1 returns at once for a hit without anchors
-    res, cig = ref.align_chains(opt, ch, z["anchors"], z["qbuf"])
+    res, cig = ref.align_chains(opt, ch, z["anchors"].copy(), z["qbuf"])
     assert res[1]["n_cigar"] == 0 and res[1]["cigar_off"] == -1 and res[1]["n_dp_issued"] == 0
     for k in (0, 2):
         assert as_align1(ch[k], res[k], cig) == expected(z, k)
     bad = z["chains"][:2].copy()
     bad[1]["as"] = len(z["anchors"])  # anchors out of range: refused before any device work
     with pytest.raises(RuntimeError):
-        ref.align_chains(opt, bad, z["anchors"], z["qbuf"])
+        ref.align_chains(opt, bad, z["anchors"].copy(), z["qbuf"])
     with pytest.raises(RuntimeError):  # CIGAR buffer too small
-        ref.align_chains(opt, z["chains"][:4], z["anchors"], z["qbuf"], cigar_cap=1)
+        ref.align_chains(opt, z["chains"][:4], z["anchors"].copy(), z["qbuf"], cigar_cap=1)
     ref.close()
