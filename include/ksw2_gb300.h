@@ -218,6 +218,11 @@ int ksw2g_align_chains(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int n_opts, con
 					   int n_chains, const ksw2g_chain_t *chains, ksw2g_anchor_t *anchors, int64_t n_anchors,
 					   const uint8_t *qbuf, int64_t qbuf_len, ksw2g_chain_result_t *res, uint32_t *cigar,
 					   int64_t cigar_cap, int64_t *cigar_used);
+/* The context's last ksw2g_align_chains call: host wall time of its stages in ms[6] (deriving
+ * the jobs, gathering the windows, the first pass, the z-drop tests with the inversion checks,
+ * the second pass, assembly) and counts[4] (hits, first-pass jobs, second-pass jobs, inversion
+ * checks). */
+int ksw2g_align_chains_last_stats(const ksw2g_ctx_t *ctx, double *ms, int64_t *counts);
 
 /* ---- mate rescue over the resident reference (pe.c:209-372) ----
  * One candidate is one (read, window) pair of mb_matesw_core: the window

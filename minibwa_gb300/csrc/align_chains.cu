@@ -17,12 +17,15 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
+#include <memory>
 #include <vector>
 
 #include "../../include/ksw2.h"
 #include "../../include/ksw2_gb300.h"
 #include "batch.h"
 #include "host_common.h"
+#include "host_parallel.h"
 
 using namespace ksw2g;
 
@@ -32,6 +35,10 @@ constexpr uint32_t kSeedLongJoin = 0x1, kSeedIgnore = 0x2;  // MB_SEED_* (mbpriv
 constexpr uint32_t kOpM = 0, kOpI = 1, kOpD = 2, kOpN = 3;    // MB_CIGAR_* (minibwa.h:27-30)
 
 inline int32_t min32(int32_t a, int32_t b) { return a < b ? a : b; }
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 // ksw_gen_nt4_mat (ksw2.h:199-219)
 void gen_mat(int8_t *mat, int a, int b, int b_ts, int b_ambi, int mt) {
@@ -286,18 +293,26 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
   for (int k = 1; k < n_opts; ++k)
     if (!same_scoring(S, opts[k])) return report_error(KSW2G_E_ARG, "align_chains: option sets differ in scoring");
   int rc;
+  double t0 = now_ms(), t1;
+  for (double &x : c->ch_ms) x = 0;
+  for (int64_t &x : c->ch_n) x = 0;
+  c->ch_n[0] = n;
   std::vector<ChainWork> W(n);
   int64_t tbuf_len = 0;
-  // ---- jobs of every chain, as mb_align1 would issue them if no gap fill z-dropped
-  for (int ci = 0; ci < n; ++ci) {
+  // ---- jobs of every chain, as mb_align1 would issue them if no gap fill z-dropped; chains in
+  // parallel, each on its own copy of its anchors (chains of one call must not share anchors)
+  std::vector<int> bad(n, 0);
+  std::vector<const char *> why(n, nullptr);
+  auto derive = [&](int ci) -> int {
+    auto fail = [&](const char *msg) { why[ci] = msg; return KSW2G_E_ARG; };
     const ksw2g_chain_t &h = chains[ci];
     ChainWork &cw = W[ci];
     res[ci] = ksw2g_chain_result_t{};
     res[ci].cigar_off = -1, res[ci].cnt = h.cnt, res[ci].score = h.score;
-    if (h.cnt <= 0) continue;
+    if (h.cnt <= 0) return 0;
     if (h.as < 0 || h.as + (int64_t)h.cnt > n_anchors || h.qoff < 0 || h.qlen < 0 || h.qoff + (int64_t)h.qlen > qbuf_len ||
         h.meth < 0 || h.meth > 2 || h.opt < 0 || h.opt >= n_opts)
-      return report_error(KSW2G_E_ARG, "align_chains: chain out of bounds");
+      return fail("align_chains: chain out of bounds");
     const ksw2g_chain_opt_t &o = opts[h.opt];
     cw.o = &o;
     cw.a.assign(anchors + h.as, anchors + h.as + h.cnt);
@@ -315,14 +330,13 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
       if (bw_long < bw) bw_long = bw;
     }
     const int64_t ctg_len = ref_ctg_len(ref, cw.tid);
-    if (ctg_len < 0) return report_error(KSW2G_E_ARG, "align_chains: anchor contig out of range");
+    if (ctg_len < 0) return fail("align_chains: anchor contig out of range");
     if (cw.is_sr) {
       max_stretch(a, 0, h.cnt, cw.as1, cw.cnt1);
     } else {
       fix_bad_ends(a, 0, h.cnt, h.mlen, o.bw, o.min_chain_score * 2, cw.as1, cw.cnt1);
       filter_bad_seeds(a, cw.as1, cw.cnt1, 10, 40, o.max_gap >> 1, 10);
       filter_bad_seeds_alt(a, cw.as1, cw.cnt1, 30, o.max_gap >> 1);
-      for (int k = 0; k < h.cnt; ++k) anchors[h.as + k].flag = a[k].flag;  // mb_align1 filters the caller's anchors
     }
     const ksw2g_anchor_t &f = a[cw.as1], &g = a[cw.as1 + cw.cnt1 - 1];
     int64_t ts = f.tpos + 1 - f.len + min32(f.len >> 1, max_back);
@@ -342,7 +356,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
       cw.ts0 = a[0].tpos + 1 - a[0].len;
       cw.qs0 = a[0].qpos + 1 - a[0].len;
       if (cw.ts0 < 0) cw.ts0 = 0;
-      if (cw.qs0 < 0) return report_error(KSW2G_E_ARG, "align_chains: anchor starts before the read");
+      if (cw.qs0 < 0) return fail("align_chains: anchor starts before the read");
       int64_t ts1 = 0;
       int32_t qs1 = 0;
       if (qs > 0 && ts > 0) {
@@ -376,7 +390,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
       }
     }
     if (!(cw.te0 > cw.ts0) || cw.qs0 < 0 || cw.qe0 > qlen || cw.te0 > ctg_len)
-      return report_error(KSW2G_E_ARG, "align_chains: anchors outside the read or the contig");
+      return fail("align_chains: anchors outside the read or the contig");
     // left extension (align.c:647-659)
     if (qs > 0 && ts > 0) {
       Job j{};
@@ -389,7 +403,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
     // the first anchor's exact match (align.c:663-671)
     te = f.tpos + 1 - min32(f.len >> 1, max_back);
     qe = f.qpos + 1 - min32(f.len >> 1, max_back);
-    if (te - ts != qe - qs || te < ts) return report_error(KSW2G_E_ARG, "align_chains: first anchor is not a match");
+    if (te - ts != qe - qs || te < ts) return fail("align_chains: first anchor is not a match");
     cw.te_first = te, cw.qe_first = qe;
     ts = te, qs = qe;
     int64_t te1 = te;
@@ -416,7 +430,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
         j.kind = 1, j.anchor = i, j.ts = ts, j.te = te, j.qs = qs, j.qe = qe;
         j.w = bw1, j.end_bonus = -1, j.zdrop = o.zdrop, j.flag = KSW_EZ_APPROX_MAX;
         j.d1 = d1, j.te1 = te1, j.qe1 = qe1;
-        if (te < ts || qe < qs) return report_error(KSW2G_E_ARG, "align_chains: anchors out of order");
+        if (te < ts || qe < qs) return fail("align_chains: anchors out of order");
         cw.jobs.push_back(j);
         if (d1 > 0) te = te1, qe = qe1;
         ts = te, qs = qe;
@@ -430,10 +444,23 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
       j.w = bw, j.end_bonus = o.end_bonus, j.zdrop = o.zdrop, j.flag = KSW_EZ_EXTZ_ONLY;
       cw.jobs.push_back(j);
     }
+    return 0;
+  };
+  parallel_for(n, 256, [&](int64_t lo, int64_t hi) {
+    for (int64_t ci = lo; ci < hi; ++ci) bad[ci] = derive((int)ci);
+  });
+  for (int ci = 0; ci < n; ++ci) {
+    if (bad[ci]) return report_error(bad[ci], why[ci]);
+    const ksw2g_chain_t &h = chains[ci];
+    ChainWork &cw = W[ci];
+    if (h.cnt <= 0) continue;
+    if (!cw.is_sr)  // mb_align1 filters the caller's anchors (align.c:571-573)
+      for (int k = 0; k < h.cnt; ++k) anchors[h.as + k].flag = cw.a[k].flag;
     if ((rc = ref_check_window(ref, cw.tid, cw.ts0, cw.te0 - cw.ts0))) return rc;
     cw.win_off = tbuf_len;
     tbuf_len += cw.te0 - cw.ts0;
   }
+  t1 = now_ms(), c->ch_ms[0] = t1 - t0, t0 = t1;
   // ---- the target windows, decoded from the resident reference and brought to the host
   std::vector<uint8_t> tbuf((size_t)std::max<int64_t>(tbuf_len, 1));
   {
@@ -469,14 +496,16 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
           cudaStreamSynchronize(c->st) != cudaSuccess)
         return report_error(KSW2G_E_CUDA, "align_chains: window gather failed");
       darena.release(), dmeta.release();
-      int k = 0;
-      for (int ci = 0; ci < n; ++ci)
-        if (W[ci].te0 > W[ci].ts0 && chains[ci].cnt > 0) {
-          memcpy(tbuf.data() + W[ci].win_off, harena.data() + dst[k], (size_t)len[k]);
-          ++k;
-        }
+      std::vector<int> wk(n, -1);  // window of each chain
+      for (int ci = 0, k = 0; ci < n; ++ci)
+        if (W[ci].te0 > W[ci].ts0 && chains[ci].cnt > 0) wk[ci] = k++;
+      parallel_for(n, 1024, [&](int64_t lo, int64_t hi) {
+        for (int64_t ci = lo; ci < hi; ++ci)
+          if (wk[ci] >= 0) memcpy(tbuf.data() + W[ci].win_off, harena.data() + dst[wk[ci]], (size_t)len[wk[ci]]);
+      });
     }
   }
+  t1 = now_ms(), c->ch_ms[1] = t1 - t0, t0 = t1;
   // ---- one mb_align_pair batch per (pass, methylation mode); left extensions run on reversed sequences
   ksw2g_align_opt_t ao{S.a, S.b, S.b_ts, S.b_ambi, S.q, S.e, S.q2, S.e2, S.meth ? 1 : 0, 0, S.max_sw_mat};
   struct Out {
@@ -486,43 +515,53 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
   Out pass[2][3];
   auto run_pass = [&](int p) -> int {
     for (int mt = 0; mt < 3; ++mt) {
+      // job records and buffer offsets in chain order, then the sequences copied over the threads
       std::vector<ksw2g_job_t> jobs;
-      std::vector<uint8_t> qb, tb;
-      int64_t cap = 0;
+      int64_t qn = 0, tn = 0, cap = 0;
       for (int ci = 0; ci < n; ++ci) {
         ChainWork &cw = W[ci];
         if (cw.mt != mt) continue;
-        const uint8_t *q = qbuf + chains[ci].qoff, *t = tbuf.data() + cw.win_off;
         for (Job &j : cw.jobs) {
           if (p == 1 && !(j.kind == 1 && j.zcode != 0)) continue;
           const int32_t ql = j.qe - j.qs, tl = (int32_t)(j.te - j.ts);
-          const int64_t qo = (int64_t)qb.size(), to = (int64_t)tb.size();
-          const uint8_t *qsrc = q + j.qs, *tsrc = t + (j.ts - cw.ts0);
-          if (j.kind == 0) {  // mb_seq_rev of both (align.c:650-652)
-            for (int32_t x = ql - 1; x >= 0; --x) qb.push_back(qsrc[x]);
-            for (int32_t x = tl - 1; x >= 0; --x) tb.push_back(tsrc[x]);
-          } else {
-            qb.insert(qb.end(), qsrc, qsrc + ql), tb.insert(tb.end(), tsrc, tsrc + tl);
-          }
           int zd = j.zdrop, fl = j.flag;
           if (p == 1) zd = j.zcode == 2 ? cw.o->zdrop_inv : cw.o->zdrop, fl = 0;  // exact maximum (align.c:693)
           (p == 0 ? j.pass1 : j.pass2) = (int)jobs.size();
-          jobs.push_back(ksw2g_job_t{qo, to, ql, tl, j.w, zd, j.end_bonus, fl});
-          cap += ql + tl + 1;
+          jobs.push_back(ksw2g_job_t{qn, tn, ql, tl, j.w, zd, j.end_bonus, fl});
+          qn += ql, tn += tl, cap += ql + tl + 1;
         }
       }
+      c->ch_n[1 + p] += (int64_t)jobs.size();
       Out &out = pass[p][mt];
       out.res.assign(jobs.size(), ksw2g_ext_result_t{});
       out.cig.assign((size_t)cap + 16, 0);
       if (jobs.empty()) continue;
-      if (qb.empty()) qb.push_back(0);  // every window empty: the batch still takes a valid buffer
-      if (tb.empty()) tb.push_back(0);
+      std::unique_ptr<uint8_t[]> qb(new uint8_t[qn + 1]), tb(new uint8_t[tn + 1]);
+      parallel_for(n, 512, [&](int64_t lo, int64_t hi) {
+        for (int64_t ci = lo; ci < hi; ++ci) {
+          const ChainWork &cw = W[ci];
+          if (cw.mt != mt) continue;
+          const uint8_t *q = qbuf + chains[ci].qoff, *t = tbuf.data() + cw.win_off;
+          for (const Job &j : cw.jobs) {
+            const int idx = p == 0 ? j.pass1 : j.pass2;
+            if (idx < 0) continue;
+            const ksw2g_job_t &J = jobs[idx];
+            const uint8_t *qsrc = q + j.qs, *tsrc = t + (j.ts - cw.ts0);
+            uint8_t *qd = qb.get() + J.qoff, *td = tb.get() + J.toff;
+            if (j.kind == 0) {  // mb_seq_rev of both (align.c:650-652)
+              for (int32_t x = 0; x < J.qlen; ++x) qd[x] = qsrc[J.qlen - 1 - x];
+              for (int32_t x = 0; x < J.tlen; ++x) td[x] = tsrc[J.tlen - 1 - x];
+            } else {
+              memcpy(qd, qsrc, (size_t)J.qlen), memcpy(td, tsrc, (size_t)J.tlen);
+            }
+          }
+        }
+      });
       int8_t mat[25];
       gen_mat(mat, S.a, S.b, S.b_ts, S.b_ambi, mt);
       int64_t used = 0;
-      const int r = ksw2g_align_pairs(c, &ao, mat, (int)jobs.size(), jobs.data(), qb.data(), (int64_t)qb.size(),
-                                      tb.data(), (int64_t)tb.size(), out.res.data(), out.cig.data(),
-                                      (int64_t)out.cig.size(), &used);
+      const int r = ksw2g_align_pairs(c, &ao, mat, (int)jobs.size(), jobs.data(), qb.get(), qn + 1, tb.get(), tn + 1,
+                                      out.res.data(), out.cig.data(), (int64_t)out.cig.size(), &used);
       if (r) return r;
     }
     return 0;
@@ -530,6 +569,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
   for (ChainWork &cw : W)
     for (Job &j : cw.jobs) j.pass1 = j.pass2 = -1, j.zcode = 0;
   if ((rc = run_pass(0))) return rc;
+  t1 = now_ms(), c->ch_ms[2] = t1 - t0, t0 = t1;
   // ---- mm_test_zdrop on the first pass of every gap fill; the inversion checks as one ksw_ll batch per mode
   {
     struct Inv {
@@ -538,9 +578,11 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
       int64_t toff_t;  // offset of the target piece in tbuf
       std::vector<uint8_t> q;
     };
-    std::vector<Inv> inv[3];
-    for (int ci = 0; ci < n; ++ci) {
+    std::vector<std::vector<Inv>> invc(n);  // per chain, then gathered in chain order
+    parallel_for(n, 512, [&](int64_t lo, int64_t hi) {
+     for (int64_t ci = lo; ci < hi; ++ci) {
       ChainWork &cw = W[ci];
+      if (cw.jobs.empty()) continue;
       const ksw2g_chain_opt_t &o = *cw.o;
       int8_t mat[25];
       gen_mat(mat, S.a, S.b, S.b_ts, S.b_ambi, cw.mt);
@@ -555,16 +597,20 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
         j.zcode = mz > o.zdrop ? 1 : 0;
         const int q_len = pos[1][1] - pos[1][0], t_len = pos[0][1] - pos[0][0];
         if (!cw.is_sr && mz > o.zdrop_inv && q_len < o.max_gap && t_len < o.max_gap) {
-          Inv v{ci, (int)ji, t_len, cw.win_off + (j.ts - cw.ts0) + pos[0][0], {}};
+          Inv v{(int)ci, (int)ji, t_len, cw.win_off + (j.ts - cw.ts0) + pos[0][0], {}};
           v.q.resize((size_t)std::max(q_len, 0));
           for (int x = 0; x < q_len; ++x) {  // reverse complement of the dropped query stretch (align.c:55-58)
             const int b = qs[pos[1][1] - x - 1];
             v.q[x] = (uint8_t)(b >= 4 ? 4 : 3 - b);
           }
-          inv[cw.mt].push_back(std::move(v));
+          invc[ci].push_back(std::move(v));
         }
       }
-    }
+     }
+    });
+    std::vector<Inv> inv[3];
+    for (int ci = 0; ci < n; ++ci)
+      for (Inv &v : invc[ci]) inv[W[ci].mt].push_back(std::move(v));
     for (int mt = 0; mt < 3; ++mt) {
       if (inv[mt].empty()) continue;
       int8_t mat[25];
@@ -577,6 +623,7 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
         tb.insert(tb.end(), tbuf.data() + v.toff_t, tbuf.data() + v.toff_t + std::max(v.tlen, 0));
       }
       std::vector<ksw2g_ll_result_t> lr(lj.size());
+      c->ch_n[3] += (int64_t)lj.size();
       if (qb.empty()) qb.push_back(0);
       if (tb.empty()) tb.push_back(0);
       if ((rc = ksw2g_ll_batch(c, 2, 5, mat, S.q, S.e, (int)lj.size(), lj.data(), qb.data(), (int64_t)qb.size(),
@@ -589,16 +636,19 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
       }
     }
   }
+  t1 = now_ms(), c->ch_ms[3] = t1 - t0, t0 = t1;
   if ((rc = run_pass(1))) return rc;
-  // ---- assemble every chain in order (align.c:647-757)
-  int64_t used = 0;
-  for (int ci = 0; ci < n; ++ci) {
+  t1 = now_ms(), c->ch_ms[4] = t1 - t0, t0 = t1;
+  // ---- assemble every chain in order (align.c:647-757), chains over the threads
+  std::vector<std::vector<uint32_t>> cgs(n);
+  parallel_for(n, 512, [&](int64_t lo, int64_t hi) {
+   for (int64_t ci = lo; ci < hi; ++ci) {
     const ksw2g_chain_t &h = chains[ci];
     ChainWork &cw = W[ci];
     ksw2g_chain_result_t &R = res[ci];
     if (h.cnt <= 0) continue;
     const ksw2g_chain_opt_t &o = *cw.o;
-    std::vector<uint32_t> cg;
+    std::vector<uint32_t> &cg = cgs[ci];
     int32_t dp_score = 0;
     int n_dp = 0;
     size_t ji = 0;
@@ -676,14 +726,33 @@ extern "C" int ksw2g_align_chains(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, int n_
     R.n_dp = n_dp;
     R.n_dp_issued = 0;
     for (const Job &j : cw.jobs) R.n_dp_issued += j.pass2 >= 0 ? 2 : 1;
+   }
+  });
+  int64_t used = 0;
+  for (int ci = 0; ci < n; ++ci) {
+    if (chains[ci].cnt <= 0) continue;
     if (cigar) {
-      if (used + (int64_t)cg.size() > cigar_cap)
+      if (used + (int64_t)cgs[ci].size() > cigar_cap)
         return report_error(KSW2G_E_CAPACITY, "align_chains: CIGAR buffer too small");
-      memcpy(cigar + used, cg.data(), cg.size() * 4);
-      R.cigar_off = used;
+      res[ci].cigar_off = used;
     }
-    used += (int64_t)cg.size();
+    used += (int64_t)cgs[ci].size();
   }
+  if (cigar)
+    parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
+      for (int64_t ci = lo; ci < hi; ++ci)
+        if (res[ci].cigar_off >= 0) memcpy(cigar + res[ci].cigar_off, cgs[ci].data(), cgs[ci].size() * 4);
+    });
   if (cigar_used) *cigar_used = used;
+  c->ch_ms[5] = now_ms() - t0;
+  return 0;
+}
+
+extern "C" int ksw2g_align_chains_last_stats(const ksw2g_ctx_t *c, double *ms, int64_t *counts) {
+  if (!c) return report_error(KSW2G_E_ARG, "align_chains: null ctx");
+  for (int k = 0; k < 6; ++k)
+    if (ms) ms[k] = c->ch_ms[k];
+  for (int k = 0; k < 4; ++k)
+    if (counts) counts[k] = c->ch_n[k];
   return 0;
 }

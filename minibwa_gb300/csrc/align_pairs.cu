@@ -19,6 +19,7 @@
 #include "../../include/ksw2.h"
 #include "../../include/ksw2_gb300.h"
 #include "batch.h"
+#include "host_parallel.h"
 
 using namespace ksw2g;
 
@@ -55,63 +56,75 @@ extern "C" int ksw2g_align_pairs(ksw2g_ctx_t *c, const ksw2g_align_opt_t *opt, c
   const ksw2g_align_opt_t &o = *opt;
   const bool dual = !(o.q == o.q2 && o.e == o.e2);
   const int extra_flag = ((o.b_ts != 0 && o.b != o.b_ts) || o.meth) ? KSW_EZ_GENERIC_SC : 0;
-  std::vector<ksw2g_job_t> dp;
-  std::vector<int> dp_idx;
-  std::vector<uint8_t> shortcut(n, 0);  // 1: ungapped CIGAR of qlen M, 2: no CIGAR
+  std::vector<uint8_t> shortcut(n, 0);  // 1: ungapped CIGAR of qlen M, 2: no CIGAR, 3: DP, 4: out of bounds
+  std::vector<int32_t> band(n, 0);       // the DP band after the shrink of short pairs
   int64_t used = 0;
-  for (int i = 0; i < n; ++i) {
-    const ksw2g_job_t &J = jobs[i];
-    if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
-        J.toff + J.tlen > tbuf_len || (J.qlen > 0 && !qbuf) || (J.tlen > 0 && !tbuf))
-      return report_error(KSW2G_E_ARG, "align_pairs: pair out of buffer bounds");
-    const uint8_t *qs = qbuf + J.qoff, *ts = tbuf + J.toff;
-    const int flag = J.flag | extra_flag;
-    int w = J.w;
-    int32_t n_mm = -1;
-    ksw2g_ext_result_t &R = res[i];
-    reset_extz(R);
-    if ((flag & KSW_EZ_EXTZ_ONLY) && J.tlen >= J.qlen) {  // ungapped extension (align.c:335-349)
-      int32_t score = 0, mx = 0;
-      for (int j = 0; j < J.qlen; ++j) {
-        const int8_t s = mat[ts[j] * 5 + qs[j]];
-        score += s;
-        n_mm += (ts[j] > 3 || qs[j] > 3 || s < 0);
-        if (mx < score) mx = score, R.max_q = R.max_t = j;
+  // the shortcuts, the band shrink and the memory cap, pair by pair over the host threads
+  parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) {
+      const ksw2g_job_t &J = jobs[i];
+      if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
+          J.toff + J.tlen > tbuf_len || (J.qlen > 0 && !qbuf) || (J.tlen > 0 && !tbuf)) {
+        shortcut[i] = 4;
+        continue;
       }
-      R.score = score, R.max = mx;
-      if (n_mm <= 2) {
-        R.mqe = score, R.mqe_t = J.qlen - 1;
-        if (R.mqe + J.end_bonus >= R.max) {
-          R.reach_end = 1;
+      const uint8_t *qs = qbuf + J.qoff, *ts = tbuf + J.toff;
+      const int flag = J.flag | extra_flag;
+      int w = J.w;
+      int32_t n_mm = -1;
+      ksw2g_ext_result_t &R = res[i];
+      reset_extz(R);
+      if ((flag & KSW_EZ_EXTZ_ONLY) && J.tlen >= J.qlen) {  // ungapped extension (align.c:335-349)
+        int32_t score = 0, mx = 0;
+        for (int j = 0; j < J.qlen; ++j) {
+          const int8_t s = mat[ts[j] * 5 + qs[j]];
+          score += s;
+          n_mm += (ts[j] > 3 || qs[j] > 3 || s < 0);
+          if (mx < score) mx = score, R.max_q = R.max_t = j;
+        }
+        R.score = score, R.max = mx;
+        if (n_mm <= 2) {
+          R.mqe = score, R.mqe_t = J.qlen - 1;
+          if (R.mqe + J.end_bonus >= R.max) {
+            R.reach_end = 1;
+            shortcut[i] = 1;
+            continue;
+          }
+        }
+      } else if (J.qlen == J.tlen && !(flag & KSW_EZ_EXTZ_ONLY)) {  // ungapped alignment (align.c:350-360)
+        const int32_t max_gapped = (J.qlen - 2) * o.a - 2 * (o.q + o.e);
+        int32_t score = 0;
+        for (int j = 0; j < J.qlen; ++j) {
+          const int8_t s = mat[ts[j] * 5 + qs[j]];
+          score += s;
+          n_mm += (ts[j] > 3 || qs[j] > 3 || s < 0);
+        }
+        R.score = score;
+        if (n_mm <= 3 || score > max_gapped) {
           shortcut[i] = 1;
           continue;
         }
       }
-    } else if (J.qlen == J.tlen && !(flag & KSW_EZ_EXTZ_ONLY)) {  // ungapped alignment (align.c:350-360)
-      const int32_t max_gapped = (J.qlen - 2) * o.a - 2 * (o.q + o.e);
-      int32_t score = 0;
-      for (int j = 0; j < J.qlen; ++j) {
-        const int8_t s = mat[ts[j] * 5 + qs[j]];
-        score += s;
-        n_mm += (ts[j] > 3 || qs[j] > 3 || s < 0);
+      if (n_mm >= 0 && (J.qlen < J.tlen ? J.qlen : J.tlen) < kMaxBwAdjLen) {  // align.c:362-366
+        const int32_t max_bw = max_bw_from_mm(o, n_mm);
+        if (w > max_bw + 4) w = max_bw + 4;
       }
-      R.score = score;
-      if (n_mm <= 3 || score > max_gapped) {
-        shortcut[i] = 1;
+      if (o.max_sw_mat > 0 && (int64_t)J.tlen * J.qlen > o.max_sw_mat) {  // align.c:368-370
+        reset_extz(R);
+        R.zdropped = 1;
+        shortcut[i] = 2;
         continue;
       }
+      band[i] = w, shortcut[i] = 3;
     }
-    if (n_mm >= 0 && (J.qlen < J.tlen ? J.qlen : J.tlen) < kMaxBwAdjLen) {  // align.c:362-366
-      const int32_t max_bw = max_bw_from_mm(o, n_mm);
-      if (w > max_bw + 4) w = max_bw + 4;
-    }
-    if (o.max_sw_mat > 0 && (int64_t)J.tlen * J.qlen > o.max_sw_mat) {  // align.c:368-370
-      reset_extz(R);
-      R.zdropped = 1;
-      shortcut[i] = 2;
-      continue;
-    }
-    dp.push_back(ksw2g_job_t{J.qoff, J.toff, J.qlen, J.tlen, w, J.zdrop * o.a, J.end_bonus, flag});
+  });
+  std::vector<ksw2g_job_t> dp;
+  std::vector<int> dp_idx;
+  for (int i = 0; i < n; ++i) {
+    if (shortcut[i] == 4) return report_error(KSW2G_E_ARG, "align_pairs: pair out of buffer bounds");
+    if (shortcut[i] != 3) continue;
+    const ksw2g_job_t &J = jobs[i];
+    dp.push_back(ksw2g_job_t{J.qoff, J.toff, J.qlen, J.tlen, band[i], J.zdrop * o.a, J.end_bonus, J.flag | extra_flag});
     dp_idx.push_back(i);
   }
   // DP of the remaining pairs: CIGARs land in the caller's buffer first, the shortcuts' runs after them

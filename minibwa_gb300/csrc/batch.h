@@ -104,6 +104,8 @@ struct ksw2g_ctx {
   ksw2g_batch *rs_ll[6] = {};                   // mate-rescue ksw_ll batches, one per (size, methylation)
   int rs_launches = 0;                          // kernels the last rescue call launched
   double rs_ms[3] = {0, 0, 0};                  // its stages' wall time: prefilter, ksw_ll, extz2
+  double ch_ms[6] = {};      // the last ksw2g_align_chains call's stages (host wall time)
+  int64_t ch_n[4] = {};      // its hits, first-pass jobs, second-pass jobs, inversion checks
   ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls
   // sub-contexts (own stream and traceback pool, half the budget each) that the
   // one-shot calls rotate their chunks through, so the host prepares the next chunks

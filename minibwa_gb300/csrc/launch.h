@@ -7,6 +7,13 @@
 
 namespace ksw2g {
 
+// Raises a kernel's dynamic shared-memory cap on the current device to at least `bytes` and
+// never lowers it.  The attribute belongs to the function, process-wide: a launch that set it
+// to its own need could lower it under a concurrent launch of the same kernel from another
+// thread (the per-call drop-in runs one stream per caller thread), which then fails with an
+// invalid argument.
+cudaError_t raise_smem_cap(const void *fn, size_t bytes);
+
 // Thread-group shapes instantiated for the extension DP kernel.  A pair with
 // n_col_ 16-byte blocks per anti-diagonal needs G*K >= 4*n_col_ words.
 struct ExtShape {

@@ -1,5 +1,9 @@
 // ll_kernels.cu -- instantiations and launcher of the striped local-alignment kernel.
 #include <cuda_runtime.h>
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 #include "launch.h"
 #include "ll.cuh"
 
@@ -31,6 +35,20 @@ static int wide_smem_cap() {
   }
   return cap;
 }
+cudaError_t raise_smem_cap(const void *fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> cap;  // (device, kernel) -> cap set so far
+  int d = 0;
+  cudaError_t e = cudaGetDevice(&d);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &c = cap[std::make_pair(d, fn)];
+  if (bytes <= c) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) c = bytes;
+  return e;
+}
+
 static size_t wide_smem_bytes(int size, int m, int slen) {
   const int lanes = size == 1 ? 16 : 8;
   return (size_t)(m + 3) * slen * lanes * sizeof(int16_t);
@@ -47,7 +65,7 @@ static cudaError_t launch_wide(int size, int slen_max, const LLLaunch &L, int ma
   const wide_fn fn = size == 1 ? ll_wide_kernel<1> : ll_wide_kernel<2>;
   const size_t smem = wide_smem_bytes(size, L.m, slen_max);
   if (smem > (size_t)wide_smem_cap()) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_cap((const void *)fn, smem);
   if (e != cudaSuccess) return e;
   const int lanes = size == 1 ? 16 : 8;
   int occ = 0, sms = 0, d = 0;
@@ -85,7 +103,7 @@ static cudaError_t launch_dpx(int size, int slen_max, const LLLaunch &L, int max
   const size_t smem = ll_dpx_smem_bytes(L.m, kSlenD[si], T);
   if (smem > 200 * 1024) return cudaSuccess;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_cap((const void *)fn, smem);
     if (e != cudaSuccess) return e;
   }
   int occ = 0, sms = 0, d = 0;
@@ -120,22 +138,24 @@ cudaError_t launch_ll(int size, int slen_max, const LLLaunch &L, int max_blocks,
   const ll_fn fn = kLL[size - 1][si];
   const int lanes = size == 1 ? 16 : 8, groups = 128 / lanes;
   const size_t smem = (size_t)groups * (L.m * kSlen[si] * lanes + 8) * sizeof(int16_t);
-  static int occ[2][4][17] = {};
-  static int sms = 0;
+  static std::atomic<int> occ[2][4][17] = {};  // computed once, by whichever thread comes first
+  static std::atomic<int> sms_seen{0};
   const int mi = L.m < 16 ? L.m : 16;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_cap((const void *)fn, smem);
     if (e != cudaSuccess) return e;
   }
-  if (!occ[size - 1][si][mi]) {
+  if (!occ[size - 1][si][mi].load(std::memory_order_relaxed)) {
     int o = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, 128, smem);
-    occ[size - 1][si][mi] = o > 0 ? o : 1;
+    occ[size - 1][si][mi].store(o > 0 ? o : 1, std::memory_order_relaxed);
   }
+  int sms = sms_seen.load(std::memory_order_relaxed);
   if (!sms) {
     int d = 0;
     cudaGetDevice(&d);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+    sms_seen.store(sms, std::memory_order_relaxed);
   }
   int blocks = (L.n_jobs + groups - 1) / groups;
   const int cap = sms * occ[size - 1][si][mi];

@@ -133,8 +133,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
                         (const int32_t *)(dm + o_fl), (const int64_t *)(dm + o_dst), c->rs_t.as<uint8_t>(), ref,
                         st) != cudaSuccess)
     return report_error(KSW2G_E_CUDA, "rescue: window gather failed");
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(ungap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (smem > 48 * 1024 && raise_smem_cap((const void *)ungap_kernel, smem) != cudaSuccess)
     return report_error(KSW2G_E_CUDA, "rescue: shared memory attribute");
   ungap_kernel<<<blocks, kUngapThreads, smem, st>>>(
       n, (const UngapJob *)(dm + o_uj), c->rs_q.as<uint8_t>(), c->rs_t.as<uint8_t>(), c->rs_res.as<UngapRes>(),

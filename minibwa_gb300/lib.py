@@ -139,6 +139,7 @@ def load_library():
         "ksw2g_ll_batch_ref": (i32, [vp, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp, u8p, i64, vp]),
         "ksw2g_rescue_batch": (i32, [vp, vp, vp, i32, vp, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_rescue_last_stats": (i32, [vp, vp, vp]),
+        "ksw2g_align_chains_last_stats": (i32, [vp, vp, vp]),
         "ksw2g_align_chains": (i32, [vp, vp, i32, vp, i32, vp, vp, i64, u8p, i64, vp, vp, i64, C.POINTER(i64)]),
         "ksw2g_align_pairs": (i32, [vp, vp, vp, i32, vp, u8p, i64, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_graph_create": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
@@ -508,6 +509,14 @@ class Reference:
                                          len(anchors), _ptr(qbuf), len(qbuf), _ptr(res), _ptr(cig), int(cigar_cap),
                                          C.byref(used)))
         return res, cig[:used.value]
+
+    def chains_stats(self):
+        """(stage ms [derive, gather, pass 1, z-drop tests, pass 2, assembly], counts [hits, pass-1
+        jobs, pass-2 jobs, inversion checks]) of the context's last align_chains call."""
+        ms = (C.c_double * 6)()
+        n = (C.c_int64 * 4)()
+        _check(self.L.ksw2g_align_chains_last_stats(self.ctx.h, ms, n))
+        return list(ms), list(n)
 
     def rescue_stats(self):
         """(kernel launches, [prefilter, ksw_ll, extz2] stage ms) of the context's last rescue call."""

@@ -11,8 +11,9 @@
  * on the worker thread as before; its alignment is deferred.  mbg_step_end then aligns the
  * hits of every read of the mini-batch at once through ksw2g_align_chains on the GPU (hits split
  * off by a z-drop in later rounds, as mb_align_skeleton reaches them), and finishes every read
- * on kt_for workers: mb_update_extra, the inversion check between split hits (mb_align1_inv),
- * hit filtering and sorting, and the rest of mb_map_sai.  Pairing and mate rescue follow in
+ * on kt_for workers: mb_update_extra, the inversion check between split hits (mb_align1_inv,
+ * its ksw_ll and mb_align_pair batched on the GPU for all reads), hit filtering and sorting,
+ * and the rest of mb_map_sai.  Pairing and mate rescue follow in
  * step 1 as before.  Output is byte-identical to the stock minibwa. */
 #ifndef MBG_H
 #define MBG_H
@@ -23,16 +24,11 @@
 extern "C" {
 #endif
 
-void mbg_step_begin(int64_t n_seq);
+void mbg_step_begin(const mb_idx_t *idx, int64_t n_seq);
 void mbg_map_sai_defer(const mb_opt_t *opt, const mb_idx_t *idx, int64_t qlen, const char *seq0, l2b_meth_t mt,
                        mb_sai_v *u, int64_t rid, mb_tbuf_t *b, const char *qname);
 void mbg_step_end(const mb_opt_t *opt, const mb_idx_t *idx, int n_thread, mb_tbuf_t **tbuf, int64_t n_seq,
                   mb_hit_t **hit, int32_t *n_hit);
-
-/* align.c's static mb_align1_inv (align.c:759-815), exported by mbg_align.c; the DP buffer
- * mb_align_skeleton shares between calls is local to each call here */
-int mbg_align1_inv(void *km, const mb_opt_t *opt, const mb_idx_t *mi, int qlen, uint8_t *qseq0[2], l2b_meth_t mt,
-                   const mb_hit_t *r1, const mb_hit_t *r2, mb_hit_t *r_inv);
 
 #ifdef __cplusplus
 }

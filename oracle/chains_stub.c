@@ -1,9 +1,10 @@
 /* chains_stub.c -- ksw2g_align_chains computed by the reference's own mb_align1 on the CPU
  * (TEST INFRASTRUCTURE ONLY).
  *
- * The batched minibwa (minibwa_gb300/mapper) calls five functions of libksw2gpu.so:
- * ksw2g_ctx_create, ksw2g_ref_create, ksw2g_ref_destroy, ksw2g_align_chains and
- * ksw2g_last_error.  This file provides them over the reference's align.c (included as
+ * The batched minibwa (minibwa_gb300/mapper) calls eight functions of libksw2gpu.so:
+ * ksw2g_ctx_create, ksw2g_ref_create, ksw2g_ref_destroy, ksw2g_align_chains (and its stats),
+ * ksw2g_ll_batch, ksw2g_align_pairs and ksw2g_last_error.  This file provides them over the
+ * reference's align.c (included as
  * _ref/align_noextra.c, mb_update_extra at the end of mb_align1 left out, as the device entry
  * point leaves it to its caller): each hit goes through mb_align1 as mb_align_skeleton would
  * call it.  Linked with the reference's ksw2 sources in place of libksw2gpu.so (make
@@ -21,6 +22,15 @@ struct ksw2g_ctx { int device; };
 struct ksw2g_ref { l2b_t l2b; };
 
 const char *ksw2g_last_error(void) { return "chains stub"; }
+
+int ksw2g_align_chains_last_stats(const ksw2g_ctx_t *ctx, double *ms, int64_t *counts)
+{
+	int k;
+	(void)ctx;
+	for (k = 0; k < 6; ++k) if (ms) ms[k] = 0;
+	for (k = 0; k < 4; ++k) if (counts) counts[k] = 0;
+	return 0;
+}
 
 int ksw2g_ctx_create(int device, ksw2g_ctx_t **ctx)
 {
@@ -117,6 +127,63 @@ int ksw2g_align_chains(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, int n_opts, con
 	}
 	for (k = 0; k < n_anchors; ++k) anchors[k].flag = a[k].flag | (uint32_t)a[k].flt << 31;
 	free(a), free(ez.cigar);
+	if (cigar_used) *cigar_used = used;
+	return 0;
+}
+
+/* ksw_ll_i16 (ksw2_ll_sse.c:335-341) per job, or its u8 core for size 1 */
+int ksw2g_ll_batch(ksw2g_ctx_t *ctx, int size, int m, const int8_t *mat, int gapo, int gape, int n_jobs,
+                   const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+                   int64_t tbuf_len, ksw2g_ll_result_t *res)
+{
+	int i;
+	(void)ctx, (void)qbuf_len, (void)tbuf_len;
+	for (i = 0; i < n_jobs; ++i) {
+		const ksw2g_ll_job_t *J = &jobs[i];
+		void *qp = ksw_ll_qinit(0, size, J->qlen, qbuf + J->qoff, m, mat);
+		ksw_llrst_t r = size == 1? ksw_ll_u8_core(qp, J->tlen, tbuf + J->toff, gapo, gape, J->xtra)
+		                          : ksw_ll_i16_core(qp, J->tlen, tbuf + J->toff, gapo, gape, J->xtra);
+		free(qp);
+		res[i].score = r.score, res[i].te = r.te, res[i].qe = r.qe, res[i].score2 = r.score2, res[i].te2 = r.te2;
+		res[i].rows = 0;
+	}
+	return 0;
+}
+
+/* mb_align_pair (align.c:329-390) per job */
+int ksw2g_align_pairs(ksw2g_ctx_t *ctx, const ksw2g_align_opt_t *ao, const int8_t *mat, int n_jobs,
+                      const ksw2g_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
+                      int64_t tbuf_len, ksw2g_ext_result_t *res, uint32_t *cigar, int64_t cigar_cap,
+                      int64_t *cigar_used)
+{
+	mb_opt_t opt;
+	ksw_extz_t ez;
+	int64_t used = 0;
+	int i;
+	(void)ctx, (void)qbuf_len, (void)tbuf_len;
+	memset(&opt, 0, sizeof opt);
+	opt.a = ao->a, opt.b = ao->b, opt.b_ts = ao->b_ts, opt.b_ambi = ao->b_ambi;
+	opt.q = ao->q, opt.e = ao->e, opt.q2 = ao->q2, opt.e2 = ao->e2;
+	if (ao->meth) opt.flag |= MB_F_METH;
+	opt.max_sw_mat = ao->max_sw_mat;
+	memset(&ez, 0, sizeof ez);
+	for (i = 0; i < n_jobs; ++i) {
+		const ksw2g_job_t *J = &jobs[i];
+		ksw2g_ext_result_t *R = &res[i];
+		mb_align_pair(0, &opt, J->qlen, qbuf + J->qoff, J->tlen, tbuf + J->toff, mat, J->w, J->end_bonus, J->zdrop,
+		              J->flag, &ez);
+		memset(R, 0, sizeof(*R));
+		R->score = ez.score, R->max = (int32_t)ez.max, R->max_q = ez.max_q, R->max_t = ez.max_t, R->mqe = ez.mqe;
+		R->mqe_t = ez.mqe_t, R->mte = ez.mte, R->mte_q = ez.mte_q, R->zdropped = ez.zdropped;
+		R->reach_end = ez.reach_end, R->n_cigar = ez.n_cigar;
+		if (ez.n_cigar > 0 && cigar) {
+			if (used + ez.n_cigar > cigar_cap) { free(ez.cigar); return KSW2G_E_CAPACITY; }
+			memcpy(cigar + used, ez.cigar, (size_t)ez.n_cigar * 4);
+			R->cigar_off = used;
+			used += ez.n_cigar;
+		}
+	}
+	free(ez.cigar);
 	if (cigar_used) *cigar_used = used;
 	return 0;
 }

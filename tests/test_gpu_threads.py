@@ -84,3 +84,34 @@ def test_batch_contexts_from_four_threads(built):
             ctx.close()
 
     _run_threads(4, work)
+
+
+def test_long_ll_queries_from_sixteen_threads(built):
+    """ksw_ll_i16 on queries of 520-4,000 nt (align.c's inversion check, up to max_gap) from 16
+    threads at once: the block-wide ksw_ll kernel takes a different amount of shared memory for
+    every query length, and a call must never lower the kernel's shared-memory cap under a
+    concurrent launch of another thread (that launch failed with an invalid argument)."""
+    import minibwa_gb300.lib as K
+    from oracle import oracle as O
+    rng = np.random.default_rng(77)
+    mat = K.gen_nt4_mat(2, 8, 0, 1)
+    cases = []
+    for _ in range(160):
+        ql, tl = int(rng.integers(520, 4000)), int(rng.integers(300, 4000))
+        q = rng.integers(0, 4, ql).astype(np.uint8)
+        t = rng.integers(0, 4, tl).astype(np.uint8)
+        if rng.random() < 0.5:  # a stretch of the query in the target
+            a, ln = int(rng.integers(0, ql // 2)), int(rng.integers(50, 300))
+            b = int(rng.integers(0, max(tl - ln, 1)))
+            piece = q[a:a + ln][: tl - b]
+            t[b:b + len(piece)] = piece
+        cases.append((q, t, O.ll(2, q, t, 5, mat, 12, 2, 0)[0]))
+    n_threads = 16
+
+    def work(t):
+        for q, tg, exp in cases[t::n_threads]:
+            qp = K.ksw_ll_qinit(2, q, 5, mat)
+            r = K.ksw_ll_i16_core(qp, tg, 12, 2, 0)
+            K.ll_free(qp)
+            assert dict(score=r.score, te=r.te, qe=r.qe, score2=r.score2, te2=r.te2) == exp
+    _run_threads(n_threads, work)
