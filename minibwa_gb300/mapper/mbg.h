@@ -13,12 +13,14 @@
  * off by a z-drop in later rounds, as mb_align_skeleton reaches them), and finishes every read
  * on kt_for workers: mb_update_extra, the inversion check between split hits (mb_align1_inv,
  * its ksw_ll and mb_align_pair batched on the GPU for all reads), hit filtering and sorting,
- * and the rest of mb_map_sai.  Pairing and mate rescue follow in
- * step 1 as before.  Output is byte-identical to the stock minibwa. */
+ * and the rest of mb_map_sai.  A third line replaces step 1's pairing loop by mbg_pair_step,
+ * which hands the mate-rescue windows of all pairs to the GPU at once and then runs mb_pair per
+ * pair as before.  Output is byte-identical to the stock minibwa. */
 #ifndef MBG_H
 #define MBG_H
 
 #include "mbpriv.h"
+#include "bseq.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -29,6 +31,10 @@ void mbg_map_sai_defer(const mb_opt_t *opt, const mb_idx_t *idx, int64_t qlen, c
                        mb_sai_v *u, int64_t rid, mb_tbuf_t *b, const char *qname);
 void mbg_step_end(const mb_opt_t *opt, const mb_idx_t *idx, int n_thread, mb_tbuf_t **tbuf, int64_t n_seq,
                   mb_hit_t **hit, int32_t *n_hit);
+/* step 1's pairing loop (kt_for over worker_for_pe) with the mate rescue of all pairs batched (mbg_pe.c) */
+void mbg_pair_step(const mb_opt_t *opt, const mb_idx_t *idx, int n_thread, mb_tbuf_t **tbuf, int64_t n_frag,
+                   const int32_t *seg_off, const int32_t *seg_cnt, const mb_bseq1_t *seq, int32_t *n_hit,
+                   mb_hit_t **hit, const mb_pestat_t *pes);
 
 #ifdef __cplusplus
 }

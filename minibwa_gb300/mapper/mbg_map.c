@@ -185,6 +185,15 @@ static void mbg_gpu_init(const mb_idx_t *idx)
 	g_l2b = l;
 }
 
+ksw2g_ctx_t *mbg_ctx(const mb_idx_t *idx)
+{ // the process's context and resident reference, for mbg_pe.c
+	if (g_init_running) pthread_join(g_init_tid, 0), g_init_running = 0;
+	mbg_gpu_init(idx);
+	return g_ctx;
+}
+
+ksw2g_ref_t *mbg_ref(void) { return g_ref; }
+
 static void mbg_chain_opt(const mb_opt_t *o, ksw2g_chain_opt_t *c)
 {
 	memset(c, 0, sizeof(*c));

@@ -1,9 +1,11 @@
 /* chains_stub.c -- ksw2g_align_chains computed by the reference's own mb_align1 on the CPU
  * (TEST INFRASTRUCTURE ONLY).
  *
- * The batched minibwa (minibwa_gb300/mapper) calls eight functions of libksw2gpu.so:
+ * The batched minibwa (minibwa_gb300/mapper) calls nine functions of libksw2gpu.so:
  * ksw2g_ctx_create, ksw2g_ref_create, ksw2g_ref_destroy, ksw2g_align_chains (and its stats),
- * ksw2g_ll_batch, ksw2g_align_pairs and ksw2g_last_error.  This file provides them over the
+ * ksw2g_ll_batch, ksw2g_align_pairs, ksw2g_rescue_batch and ksw2g_last_error.  This file
+ * provides them over the reference's own code -- mate rescue over the oracle's restatement of
+ * it (rescue_cpu.c), which is pinned to the reference's mb_matesw_core -- and the
  * reference's align.c (included as
  * _ref/align_noextra.c, mb_update_extra at the end of mb_align1 left out, as the device entry
  * point leaves it to its caller): each hit goes through mb_align1 as mb_align_skeleton would
@@ -17,9 +19,10 @@
 
 #include "align_noextra.c"
 #include "ksw2_gb300.h"
+#include "ksw2_oracle.h"
 
 struct ksw2g_ctx { int device; };
-struct ksw2g_ref { l2b_t l2b; };
+struct ksw2g_ref { l2b_t l2b; uint64_t *off; };
 
 const char *ksw2g_last_error(void) { return "chains stub"; }
 
@@ -47,8 +50,9 @@ int ksw2g_ref_create(ksw2g_ctx_t *ctx, int64_t n_ctg, const uint64_t *ctg_off, c
 	(void)ctx;
 	r->l2b.n_ctg = r->l2b.m_ctg = n_ctg;
 	r->l2b.ctg = (l2b_ctg_t*)calloc(n_ctg + 1, sizeof(l2b_ctg_t));
+	r->off = (uint64_t*)calloc(n_ctg + 1, sizeof(uint64_t));
 	for (k = 0; k < n_ctg; ++k)
-		r->l2b.ctg[k].off = ctg_off[k], r->l2b.ctg[k].len = ctg_len[k], r->l2b.tot_len += ctg_len[k];
+		r->l2b.ctg[k].off = r->off[k] = ctg_off[k], r->l2b.ctg[k].len = ctg_len[k], r->l2b.tot_len += ctg_len[k];
 	r->l2b.pac = (uint64_t*)pac, r->l2b.n_pac = r->l2b.m_pac = n_pac;
 	r->l2b.n_ambi = r->l2b.m_ambi = n_ambi, r->l2b.ambi = (l2b_intv_t*)ambi;
 	*ref = r;
@@ -57,7 +61,7 @@ int ksw2g_ref_create(ksw2g_ctx_t *ctx, int64_t n_ctg, const uint64_t *ctg_off, c
 
 void ksw2g_ref_destroy(ksw2g_ref_t *ref)
 {
-	if (ref) free(ref->l2b.ctg), free(ref);
+	if (ref) free(ref->l2b.ctg), free(ref->off), free(ref);
 }
 
 static void stub_opt(const ksw2g_chain_opt_t *c, mb_opt_t *o)
@@ -185,5 +189,20 @@ int ksw2g_align_pairs(ksw2g_ctx_t *ctx, const ksw2g_align_opt_t *ao, const int8_
 	}
 	free(ez.cigar);
 	if (cigar_used) *cigar_used = used;
+	return 0;
+}
+
+/* mate rescue of candidate windows (pe.c:340-368, 249-300) by the oracle's restatement */
+int ksw2g_rescue_batch(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, const ksw2g_rescue_opt_t *opt, int n_jobs,
+                       const ksw2g_rescue_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, ksw2g_rescue_result_t *res,
+                       uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_used)
+{
+	int64_t r;
+	(void)ctx, (void)qbuf_len;
+	r = orc_rescue_batch((const orc_rescue_opt_t*)opt, n_jobs, (const orc_rescue_job_t*)jobs, qbuf, ref->l2b.pac,
+	                     ref->off, (int64_t)ref->l2b.n_ambi, (const uint64_t*)ref->l2b.ambi, (orc_rescue_res_t*)res,
+	                     cigar, cigar_cap, 8);
+	if (r < 0) return KSW2G_E_CAPACITY;
+	if (cigar_used) *cigar_used = r;
 	return 0;
 }
