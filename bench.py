@@ -663,6 +663,50 @@ def serving_point(frac=0.8, duration=3.0):
     return line
 
 
+def mapper_point(n_pairs=100_000):
+    """The batched minibwa (minibwa_gb300/mapper) against the stock build of the same reference
+    sources on the same simulated pairs, both with all host threads: reads mapped per second of
+    wall time, whether their SAM outputs are byte-identical, and the batched run's stages."""
+    import shutil
+    import tempfile
+    from minibwa_gb300 import mapper, synth
+    from oracle import oracle as O
+    tree = O.ref_tree()
+    if tree is None:
+        return {"unavailable": "the reference's sources are not staged (make -C oracle stage REF=...)"}
+    stock = O.build_minibwa_stock()
+    batch = mapper.build(tree)["batch"]
+    d = tempfile.mkdtemp(prefix="mapper_point_")
+    try:
+        g = synth.mapper_genome(ctg_len=(6_000_000, 4_000_000, 2_000_000), n_repeats=800)
+        synth.write_fasta(os.path.join(d, "g.fa"), g)
+        mapper.index(stock, "g.fa", "g", d)
+        a, b = synth.mapper_pairs(g, n_pairs)
+        synth.write_fasta(os.path.join(d, "p1.fa"), a), synth.write_fasta(os.path.join(d, "p2.fa"), b)
+        threads = os.cpu_count() or 1
+        args = ["g", "p1.fa", "p2.fa"]
+        mapper.map_reads(stock, args, d, threads)  # page in the index and the binaries
+        sa, ts = mapper.map_reads(stock, args, d, threads)
+        env = dict(os.environ, MBG_TIMING="1")
+        t0 = time.perf_counter()
+        out = subprocess.run([batch, "map", "-t", str(threads)] + args, cwd=d, capture_output=True, env=env)
+        tb = time.perf_counter() - t0
+        if out.returncode != 0:
+            return {"unavailable": "batched minibwa failed: " + out.stderr.decode(errors="replace")[-300:]}
+        stages = [ln.split("] ", 1)[1] for ln in out.stderr.decode().splitlines() if ln.startswith("[M::mbg]")]
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    n = 2 * n_pairs
+    return {"metric": "reads mapped/s, whole minibwa run (index loaded, SAM written)", "value": n / tb,
+            "unit": "reads/s", "wall_s": tb, "sam_identical_to_stock": out.stdout == sa,
+            "workload": f"{n_pairs} simulated 150 nt pairs (synth.mapper_pairs) on a 12 Mb simulated genome with "
+                        f"800 near-repeats, minibwa map -t {threads}",
+            "stages": stages,
+            "cpu_baseline": {"value": n / ts, "unit": "reads/s", "cores": threads, "kind": "reference",
+                             "sample": f"the stock minibwa built from the reference's sources, same reads, "
+                                       f"{threads} threads, {ts:.2f} s wall"}}
+
+
 def main():
     args = parse()
     rank, world = dist_init(args)
@@ -697,6 +741,7 @@ def main():
             extra[name] = mx
             del wx
         extra["cfg4"] = serving_point()
+        extra["mapper"] = mapper_point()
     if rank == 0:
         line = {
             "metric": Workload(args.workload, args, rank, sizes_only=True).metric, "value": m["value"],

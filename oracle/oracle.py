@@ -97,6 +97,16 @@ def build_minibwa(gpulib_dir):
     return {k: os.path.join(HERE, "_ref", "minibwa_" + k) for k in ("stock", "gpu", "stock_km", "gpu_km")}
 
 
+def build_minibwa_stock():
+    """Compile the reference's minibwa from its sources, stock (oracle/_ref/minibwa_stock); needs a
+    reference tree."""
+    t = ref_tree()
+    if not t:
+        raise RuntimeError("no reference tree: set KSW2_REF_TREE or stage one (make -C oracle stage REF=...)")
+    subprocess.check_call(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", "_ref/minibwa_stock", f"REF={t}"])
+    return os.path.join(HERE, "_ref", "minibwa_stock")
+
+
 def build_mbgstub():
     """Compile the batched minibwa against _ref/libmbgstub.so (ksw2g_align_chains by the
     reference's own mb_align1 on the CPU) and the stock minibwa; needs a reference tree.
