@@ -310,7 +310,10 @@ int ksw2g_ext_get_family(void);
  *           plus 32 bytes.  All jobs of one call use the same gap mode
  *           (score-only, left-aligned or right-aligned CIGAR).  The host copies
  *           the array on the stream, so it must stay unchanged until the stream
- *           has passed the call.
+ *           has passed the call.  Under stream capture the copy is recorded with
+ *           the pointer and every replay reads the array again, without the
+ *           checks of the captured call: it must then hold the same jobs for as
+ *           long as the graph is replayed.
  *  arena_len bytes of d_arena; a job whose sequence plus its padding ends past
  *           it is rejected (KSW2G_E_ARG) before any device work.
  *  d_res    device array of n_jobs results (as ksw2g_ext_batch fills them).
