@@ -99,9 +99,11 @@ struct ksw2g_ctx {
   PinBuf one_h;         // per-call drop-in staging (pinned)
   DevBuf rs_q, rs_t, rs_meta, rs_res, rs_hist;  // mate-rescue prefilter: reads, windows, records, votes
   PinBuf rs_h;                                  // mate-rescue staging (pinned)
-  PinBuf rs_rq;                                 // mate-rescue reversed read prefixes (pinned)
   int oneshot_launches = 0;                     // kernels the last one-shot extension call launched
-  ksw2g_batch *rs_ll[6] = {};                   // mate-rescue ksw_ll batches, one per (size, methylation)
+  ksw2g_batch *rs_ll[6 * 7] = {};               // mate-rescue ksw_ll batches, one per (size, methylation,
+                                                // query-segment class)
+  ksw2g_batch *rs_ext[3] = {};                  // mate-rescue extz2 batches, one per methylation mode
+  DevBuf rs_rq, rs_rmeta;                       // reversed read prefixes on the device and their records
   int rs_launches = 0;                          // kernels the last rescue call launched
   double rs_ms[3] = {0, 0, 0};                  // its stages' wall time: prefilter, ksw_ll, extz2
   double ch_ms[6] = {};      // the last ksw2g_align_chains call's stages (host wall time)
@@ -168,6 +170,9 @@ struct SeqSeg {
   int64_t qlen;
   const uint8_t *tbuf;
   int64_t tlen;
+  // device copy of qbuf (qlen bytes) already on the context's stream: the queries are packed
+  // from it and qbuf is not read (single-segment batches only)
+  const uint8_t *qdev = nullptr;
 };
 // Targets read from a device-resident reference instead of host buffers: job
 // k's target is the window [toff, toff+tlen) of contig tid[k], decoded with

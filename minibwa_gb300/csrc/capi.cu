@@ -142,11 +142,12 @@ extern "C" void ksw2g_ctx_destroy(ksw2g_ctx_t *c) {
   c->tb_pool.release();
   c->one.release();
   c->one_h.release();
-  for (DevBuf *d : {&c->rs_q, &c->rs_t, &c->rs_meta, &c->rs_res, &c->rs_hist}) d->release();
+  for (DevBuf *d : {&c->rs_q, &c->rs_t, &c->rs_meta, &c->rs_res, &c->rs_hist, &c->rs_rq, &c->rs_rmeta}) d->release();
   for (ksw2g_batch *b : c->rs_ll)
     if (b) ksw2g_batch_free(b);
+  for (ksw2g_batch *b : c->rs_ext)
+    if (b) ksw2g_batch_free(b);
   c->rs_h.release();
-  c->rs_rq.release();
   cudaStreamDestroy(c->st);
   delete c;
 }
@@ -219,6 +220,8 @@ int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, co
                            std::vector<int64_t> &qpad, std::vector<int64_t> &tpad, const RefTargets *rt) {
   int64_t qbuf_len = 0, tbuf_len = 0;
   for (int k = 0; k < nseg; ++k) qbuf_len += segs[k].qlen, tbuf_len += rt ? 0 : segs[k].tlen;
+  const uint8_t *qdev = nseg == 1 ? segs[0].qdev : nullptr;  // queries already on the device
+  const int64_t qraw = qdev ? 0 : qbuf_len;                      // query bytes uploaded into raw
   qpad.resize(n), tpad.resize(n);
   int64_t a = 0;
   for (int i = 0; i < n; ++i) {
@@ -228,7 +231,7 @@ int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, co
   const int64_t arena_bytes = a + 64;
   int rc;
   if ((rc = b->arena.ensure(arena_bytes))) return rc;
-  if ((rc = b->raw.ensure(qbuf_len + tbuf_len + 16))) return rc;
+  if ((rc = b->raw.ensure(qraw + tbuf_len + 16))) return rc;
   // metadata of the packed sequences (queries, then targets unless they come from the
   // device reference): raw offsets (int64), lengths (int32), arena offsets (int64)
   const int npack = rt ? n : 2 * n;
@@ -241,13 +244,13 @@ int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, co
   int64_t *dof = (int64_t *)(hm.data() + o_dof);
   for (int i = 0; i < n; ++i) {
     ro[i] = qoff[i], ln[i] = qlen[i], dof[i] = qpad[i];
-    if (!rt) ro[n + i] = qbuf_len + toff[i], ln[n + i] = tlen[i], dof[n + i] = tpad[i];
+    if (!rt) ro[n + i] = qraw + toff[i], ln[n + i] = tlen[i], dof[n + i] = tpad[i];
   }
   uint8_t *raw = b->raw.as<uint8_t>();
   {
-    int64_t qa = 0, ta = qbuf_len;
+    int64_t qa = 0, ta = qraw;
     for (int k = 0; k < nseg; ++k) {
-      if (segs[k].qlen) CK(cudaMemcpyAsync(raw + qa, segs[k].qbuf, segs[k].qlen, cudaMemcpyHostToDevice, c->st));
+      if (segs[k].qlen && !qdev) CK(cudaMemcpyAsync(raw + qa, segs[k].qbuf, segs[k].qlen, cudaMemcpyHostToDevice, c->st));
       if (!rt && segs[k].tlen) CK(cudaMemcpyAsync(raw + ta, segs[k].tbuf, segs[k].tlen, cudaMemcpyHostToDevice, c->st));
       qa += segs[k].qlen, ta += rt ? 0 : segs[k].tlen;
     }
@@ -256,7 +259,12 @@ int upload_and_pack(ksw2g_ctx *c, ksw2g_batch *b, int n, const int64_t *qoff, co
   const int64_t *dro = b->rawmeta.as<int64_t>();
   const int32_t *dln = (const int32_t *)(b->rawmeta.as<uint8_t>() + o_ln);
   const int64_t *ddof = (const int64_t *)(b->rawmeta.as<uint8_t>() + o_dof);
-  CK(launch_pack(npack, raw, dro, dln, b->arena.as<uint8_t>(), ddof, c->st));
+  if (qdev) {  // queries from their device copy, targets (unless from the reference) from raw
+    CK(launch_pack(n, qdev, dro, dln, b->arena.as<uint8_t>(), ddof, c->st));
+    if (!rt) CK(launch_pack(n, raw, dro + n, dln + n, b->arena.as<uint8_t>(), ddof + n, c->st));
+  } else {
+    CK(launch_pack(npack, raw, dro, dln, b->arena.as<uint8_t>(), ddof, c->st));
+  }
   if (rt) {  // targets: windows of the device reference, decoded into their arena slots
     // layout: start (int64), arena offset (int64), contig (int32), length (int32), flags (int32)
     const size_t rm = (size_t)n * (8 + 8 + 4 + 4 + 4);

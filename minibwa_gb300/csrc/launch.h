@@ -70,6 +70,9 @@ cudaError_t launch_ext_bt(const ksw2g_job *jobs, const int32_t *order, int n_job
                           uint8_t *tb_pool,
                           const int64_t *tb_off, ksw2g_ext_result *res, uint32_t *cigar_out,
                           unsigned long long *cursor, long long cigar_cap, int *err, cudaStream_t st);
+// Index of the smallest segment count instantiated for the DPX ksw_ll kernels that holds `slen`
+// segments (6 classes; 6 = beyond them).  Jobs of one class share a kernel instance.
+int ll_slen_class(int slen);
 cudaError_t launch_pack(int n, const uint8_t *raw, const int64_t *raw_off, const int32_t *len, uint8_t *arena,
                         const int64_t *dst_off, cudaStream_t st);
 

@@ -53,6 +53,12 @@ static size_t wide_smem_bytes(int size, int m, int slen) {
   const int lanes = size == 1 ? 16 : 8;
   return (size_t)(m + 3) * slen * lanes * sizeof(int16_t);
 }
+int ll_slen_class(int slen) {
+  for (int i = 0; i < kNumSlenD; ++i)
+    if (slen <= kSlenD[i]) return i;
+  return kNumSlenD;
+}
+
 int ll_slen_cap(int size, int m) {
   const size_t per = wide_smem_bytes(size, m, 1);  // bytes per segment
   const int s = (int)((size_t)wide_smem_cap() / (per ? per : 1));

@@ -55,16 +55,17 @@ void gen_nt4(int8_t *mat, int8_t a, int8_t b, int8_t b_ts, int8_t b_ambi, int mt
 
 inline int64_t al16(int64_t x) { return (x + 15) & ~(int64_t)15; }
 
-// dst[p] = src[n-1-p], eight bytes at a time
-void reverse_bytes(uint8_t *dst, const uint8_t *src, int n) {
-  int p = 0;
-  for (; p + 8 <= n; p += 8) {
-    uint64_t w;
-    memcpy(&w, src + n - p - 8, 8);
-    w = __builtin_bswap64(w);
-    memcpy(dst + p, &w, 8);
+// mb_seq_rev of the read prefixes ksw_ll ends at (pe.c:283), from the reads the prefilter
+// uploaded: one block per prefix
+__global__ void rev_prefix_kernel(int n, const uint8_t *__restrict__ src, const int64_t *__restrict__ soff,
+                                  const int32_t *__restrict__ len, uint8_t *__restrict__ dst,
+                                  const int64_t *__restrict__ doff) {
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint8_t *s = src + soff[i];
+    uint8_t *d = dst + doff[i];
+    const int L = len[i];
+    for (int p = threadIdx.x; p < L; p += blockDim.x) d[p] = s[L - 1 - p];
   }
-  for (; p < n; ++p) dst[p] = src[n - 1 - p];
 }
 
 double ms_since(std::chrono::steady_clock::time_point t0) {
@@ -173,16 +174,22 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
   }
   // one batch per (size, methylation mode); all are prepared, then run on the context's two
   // streams at once, the largest alone on the first, so the few i16 jobs overlap the u8 ones
+  // Jobs are grouped further by the kernel instance their segment count needs, so that short
+  // reads do not run padded to the longest read of the batch.
   struct LLGroup {
     int slot, size;
     std::vector<int> idx;
   };
   std::vector<LLGroup> groups;
+  std::vector<int> cls(n, 0);
+  for (int i = 0; i < n; ++i)
+    if (ll_size[i]) cls[i] = ll_slen_class((jobs[i].qlen + (ll_size[i] == 1 ? 16 : 8) - 1) / (ll_size[i] == 1 ? 16 : 8));
   for (int size = 1; size <= 2; ++size)
-    for (int mt = 0; mt <= 2; ++mt) {
-      LLGroup g{(size - 1) * 3 + mt, size, {}};
+    for (int mt = 0; mt <= 2; ++mt)
+     for (int sc = 0; sc < 7; ++sc) {
+      LLGroup g{((size - 1) * 3 + mt) * 7 + sc, size, {}};
       for (int i = 0; i < n; ++i)
-        if (ll_size[i] == size && jobs[i].meth == mt) g.idx.push_back(i);
+        if (ll_size[i] == size && jobs[i].meth == mt && cls[i] == sc) g.idx.push_back(i);
       if (g.idx.empty()) continue;
       int8_t mat[25];
       gen_nt4(mat, 1, (int8_t)b_mm, (int8_t)b_ts, (int8_t)b_ambi, mt);
@@ -195,7 +202,8 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
         tids[k] = jobs[i].tid;
       }
       if (!c->rs_ll[g.slot]) c->rs_ll[g.slot] = new ksw2g_batch;
-      const SeqSeg seg{lj.data(), (int)lj.size(), qbuf, qbuf_len, nullptr, 0};
+      // the reads the prefilter uploaded stay on the device
+      const SeqSeg seg{lj.data(), (int)lj.size(), qbuf, qbuf_len, nullptr, 0, c->rs_q.as<uint8_t>()};
       const RefTargets rt{ref, tids.data(), nullptr};
       if ((rc = ll_prepare_segs(c, c->rs_ll[g.slot], size, 5, mat, gapo, gape, 1, &seg, &rt))) return rc;
       groups.push_back(std::move(g));
@@ -236,29 +244,43 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     const int flag = KSW_EZ_EXTZ_ONLY | KSW_EZ_RIGHT | KSW_EZ_REV_CIGAR | (mt ? KSW_EZ_GENERIC_SC : 0);
     std::vector<ksw2g_job_t> ej(idx.size());
     std::vector<int32_t> tids(idx.size()), tfl(idx.size(), KSW2G_REF_REVERSE);
-    int64_t rq_len = 0;
-    for (int i : idx) rq_len += res[i].ll_qe + 1;
-    // the reversed prefixes go to a reused pinned buffer: no zero fill, and the upload is a DMA
-    if ((rc = c->rs_rq.ensure((size_t)std::max<int64_t>(rq_len, 1)))) return rc;
-    uint8_t *rq = (uint8_t *)c->rs_rq.p;
+    // the reversed prefixes are cut from the device copy of the reads (no host byte touched)
+    const int m = (int)idx.size();
+    const size_t o_len = (size_t)8 * m, o_dof = (o_len + (size_t)4 * m + 7) & ~(size_t)7, rm = o_dof + (size_t)8 * m;
+    std::vector<uint8_t> hr(rm);
+    int64_t *hso = (int64_t *)hr.data(), *hdo = (int64_t *)(hr.data() + o_dof);
+    int32_t *hln = (int32_t *)(hr.data() + o_len);
     int64_t qo = 0;
-    for (size_t k = 0; k < idx.size(); ++k) {
+    for (int k = 0; k < m; ++k) {
       const int i = idx[k];
       const int qe = res[i].ll_qe + 1, te = res[i].ll_te + 1;
-      const uint8_t *src = qbuf + jobs[i].qoff;
-      reverse_bytes(rq + qo, src, qe);  // mb_seq_rev(qe, qseq)
+      hso[k] = jobs[i].qoff, hln[k] = qe, hdo[k] = qo;
       ej[k] = ksw2g_job_t{qo, res[i].ts2, qe, te, o.bw, o.zdrop, o.end_bonus, flag};
       tids[k] = jobs[i].tid;
       qo += qe;
     }
+    const int64_t rq_len = qo;
+    if ((rc = c->rs_rq.ensure((size_t)std::max<int64_t>(rq_len, 1) + 16)) || (rc = c->rs_rmeta.ensure(rm))) return rc;
+    uint8_t *drm = c->rs_rmeta.as<uint8_t>();
+    if (cudaMemcpyAsync(drm, hr.data(), rm, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return report_error(KSW2G_E_CUDA, "rescue: prefix records upload failed");
+    rev_prefix_kernel<<<std::min(m, c->nsm * 16), 64, 0, st>>>(m, c->rs_q.as<uint8_t>(), (const int64_t *)drm,
+                                                               (const int32_t *)(drm + o_len), c->rs_rq.as<uint8_t>(),
+                                                               (const int64_t *)(drm + o_dof));
+    if (cudaGetLastError() != cudaSuccess) return report_error(KSW2G_E_CUDA, "rescue: prefix kernel failed");
     std::vector<ksw2g_ext_result_t> er(idx.size());
     int64_t u = 0;
+    if (!c->rs_ext[mt]) c->rs_ext[mt] = new ksw2g_batch;
+    ksw2g_batch *eb = c->rs_ext[mt];
+    const SeqSeg seg{ej.data(), m, qbuf, rq_len, nullptr, 0, c->rs_rq.as<uint8_t>()};
+    const RefTargets rt{ref, tids.data(), tfl.data()};
     // CIGARs go straight into the caller's buffer behind those of earlier groups
-    if ((rc = ksw2g_ext_batch_ref(c, ref, 0, 5, mat, (int8_t)o.q, (int8_t)o.e, (int8_t)o.q, (int8_t)o.e,
-                                  (int)idx.size(), ej.data(), tids.data(), tfl.data(), rq, rq_len, er.data(),
-                                  cigar ? cigar + used : nullptr, cigar ? cigar_cap - used : 0, &u)))
+    if ((rc = ext_prepare_segs(c, eb, 0, 5, mat, (int8_t)o.q, (int8_t)o.e, (int8_t)o.q, (int8_t)o.e, 1, &seg, &rt)) ||
+        (rc = ksw2g_batch_run(c, eb)) ||
+        (rc = ksw2g_ext_fetch(c, eb, er.data(), cigar ? cigar + used : nullptr, cigar ? cigar_cap - used : 0, &u)))
       return rc;
-    c->rs_launches += c->oneshot_launches;
+    c->rs_launches += 2 + eb->launches;  // prefix records and kernel, then packing, gather and the DP
+
     for (size_t k = 0; k < idx.size(); ++k) {
       const int i = idx[k];
       ksw2g_rescue_result_t &R = res[i];
