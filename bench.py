@@ -359,6 +359,7 @@ def run_rescue(args, rank, world):
     barrier(world)
     torch.cuda.synchronize()
     stage_ms = np.zeros(3)
+    dev_ms = np.zeros(2)
     launches = 0
     with ClockSampler(dev) as clk:
         t0 = time.perf_counter()
@@ -367,6 +368,7 @@ def run_rescue(args, rank, world):
             nl, ms3 = dref.rescue_stats()
             launches += nl
             stage_ms += ms3
+            dev_ms += dref.rescue_device_ms()
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / args.steps
     dt_max = allmax(dt, world)
@@ -392,6 +394,7 @@ def run_rescue(args, rank, world):
         h2d = jobs.nbytes + len(qbuf)
         d2h = res.nbytes + 4 * used.value
         stage_ms /= args.steps
+        dev_ms /= args.steps
         line = {
             "metric": "rescue candidates/s", "value": value, "unit": "candidates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt_max * 1e3, "higher_is_better": True,
@@ -403,6 +406,9 @@ def run_rescue(args, rank, world):
                        "rescued_fraction": float(res["rescued"].mean()),
                        "ll_fraction": float(res["ll_done"].mean())},
             "stages_ms": {"gather_prefilter": stage_ms[0], "ksw_ll": stage_ms[1], "extz2": stage_ms[2]},
+            "kernels_ms": {"ksw_ll": dev_ms[0], "extz2": dev_ms[1],
+                           "note": "CUDA events around the stages' DP and backtrack launches; the rest of each "
+                                   "stage is host work and copies"},
             "gpu_launches": launches,
             "roofline": None,
             "e2e": {"value": value, "unit": "candidates/s", "h2d_bytes_per_step": int(h2d),

@@ -262,6 +262,9 @@ int ksw2g_rescue_batch(ksw2g_ctx_t *ctx, const ksw2g_ref_t *ref, const ksw2g_res
 /* The last rescue call of ctx: kernels launched, and the wall time (ms) of its three
  * stages (window gather + prefilter, ksw_ll, extz2), each including its copies. */
 int ksw2g_rescue_last_stats(const ksw2g_ctx_t *ctx, int *launches, double *ms3);
+/* Its ksw_ll and extz2 (DP and backtrack) kernels' device time in ms[0], ms[1], from CUDA events
+ * around the launches; the rest of a stage's wall time is host work and copies. */
+int ksw2g_rescue_last_device_ms(const ksw2g_ctx_t *ctx, double *ms2);
 
 /* ---- CUDA graphs: one launch runs several prepared batches concurrently ----
  * Captures the kernels of n prepared batches (extension or ll) into one CUDA

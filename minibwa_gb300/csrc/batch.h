@@ -106,6 +106,7 @@ struct ksw2g_ctx {
   DevBuf rs_rq, rs_rmeta;                       // reversed read prefixes on the device and their records
   int rs_launches = 0;                          // kernels the last rescue call launched
   double rs_ms[3] = {0, 0, 0};                  // its stages' wall time: prefilter, ksw_ll, extz2
+  double rs_dev_ms[2] = {0, 0};                 // device time of its ksw_ll and extz2 kernels
   double ch_ms[6] = {};      // the last ksw2g_align_chains call's stages (host wall time)
   int64_t ch_n[4] = {};      // its hits, first-pass jobs, second-pass jobs, inversion checks
   ksw2g_batch *scratch = nullptr;  // reused by the one-shot batch calls

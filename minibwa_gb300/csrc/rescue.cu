@@ -82,7 +82,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     return report_error(KSW2G_E_ARG, "rescue: bad arguments");
   if (opt->a <= 0) return report_error(KSW2G_E_ARG, "rescue: the match score must be positive");
   if (cigar_used) *cigar_used = 0;
-  c->rs_launches = 0, c->rs_ms[0] = c->rs_ms[1] = c->rs_ms[2] = 0;
+  c->rs_launches = 0, c->rs_ms[0] = c->rs_ms[1] = c->rs_ms[2] = 0, c->rs_dev_ms[0] = c->rs_dev_ms[1] = 0;
   if (n == 0) return 0;
   if (cudaSetDevice(c->device) != cudaSuccess) return report_error(KSW2G_E_CUDA, "rescue: bad device");
   const ksw2g_rescue_opt_t &o = *opt;
@@ -174,22 +174,16 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
   }
   // one batch per (size, methylation mode); all are prepared, then run on the context's two
   // streams at once, the largest alone on the first, so the few i16 jobs overlap the u8 ones
-  // Jobs are grouped further by the kernel instance their segment count needs, so that short
-  // reads do not run padded to the longest read of the batch.
   struct LLGroup {
     int slot, size;
     std::vector<int> idx;
   };
   std::vector<LLGroup> groups;
-  std::vector<int> cls(n, 0);
-  for (int i = 0; i < n; ++i)
-    if (ll_size[i]) cls[i] = ll_slen_class((jobs[i].qlen + (ll_size[i] == 1 ? 16 : 8) - 1) / (ll_size[i] == 1 ? 16 : 8));
   for (int size = 1; size <= 2; ++size)
-    for (int mt = 0; mt <= 2; ++mt)
-     for (int sc = 0; sc < 7; ++sc) {
-      LLGroup g{((size - 1) * 3 + mt) * 7 + sc, size, {}};
+    for (int mt = 0; mt <= 2; ++mt) {
+      LLGroup g{(size - 1) * 3 + mt, size, {}};
       for (int i = 0; i < n; ++i)
-        if (ll_size[i] == size && jobs[i].meth == mt && cls[i] == sc) g.idx.push_back(i);
+        if (ll_size[i] == size && jobs[i].meth == mt) g.idx.push_back(i);
       if (g.idx.empty()) continue;
       int8_t mat[25];
       gen_nt4(mat, 1, (int8_t)b_mm, (int8_t)b_ts, (int8_t)b_ambi, mt);
@@ -213,6 +207,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
   std::sort(groups.begin(), groups.end(), [](const LLGroup &x, const LLGroup &y) { return x.idx.size() > y.idx.size(); });
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     ksw2g_batch *b = c->rs_ll[groups[gi].slot];
+    ksw2g_batch_set_timing(b, 1);
     if ((rc = ll_run_on(b, gi == 0 ? c->st : c->aux))) return rc;
     c->rs_launches += 2 + b->launches;  // query packing and window gather, then the DP
   }
@@ -221,6 +216,8 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
   for (const LLGroup &g : groups) {
     std::vector<ksw2g_ll_result_t> lr(g.idx.size());
     if ((rc = ksw2g_ll_fetch(c, c->rs_ll[g.slot], lr.data()))) return rc;
+    double dp = 0, bt = 0;
+    if (ksw2g_batch_kernel_ms(c->rs_ll[g.slot], &dp, &bt, nullptr, nullptr) == 0) c->rs_dev_ms[0] += dp + bt;
     for (size_t k = 0; k < g.idx.size(); ++k) {
       ksw2g_rescue_result_t &R = res[g.idx[k]];
       R.ll_done = 1, R.ll_score = lr[k].score, R.ll_te = lr[k].te, R.ll_qe = lr[k].qe;
@@ -276,10 +273,14 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
     const RefTargets rt{ref, tids.data(), tfl.data()};
     // CIGARs go straight into the caller's buffer behind those of earlier groups
     if ((rc = ext_prepare_segs(c, eb, 0, 5, mat, (int8_t)o.q, (int8_t)o.e, (int8_t)o.q, (int8_t)o.e, 1, &seg, &rt)) ||
-        (rc = ksw2g_batch_run(c, eb)) ||
+        (rc = ksw2g_batch_set_timing(eb, 1)) || (rc = ksw2g_batch_run(c, eb)) ||
         (rc = ksw2g_ext_fetch(c, eb, er.data(), cigar ? cigar + used : nullptr, cigar ? cigar_cap - used : 0, &u)))
       return rc;
     c->rs_launches += 2 + eb->launches;  // prefix records and kernel, then packing, gather and the DP
+    {
+      double dp = 0, bt = 0;
+      if (ksw2g_batch_kernel_ms(eb, &dp, &bt, nullptr, nullptr) == 0) c->rs_dev_ms[1] += dp + bt;
+    }
 
     for (size_t k = 0; k < idx.size(); ++k) {
       const int i = idx[k];
@@ -307,6 +308,12 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
   }
   if (cigar_used) *cigar_used = used;
   c->rs_ms[2] = ms_since(t0);
+  return 0;
+}
+
+extern "C" int ksw2g_rescue_last_device_ms(const ksw2g_ctx_t *c, double *ms) {
+  if (!c || !ms) return report_error(KSW2G_E_ARG, "rescue: null argument");
+  ms[0] = c->rs_dev_ms[0], ms[1] = c->rs_dev_ms[1];
   return 0;
 }
 

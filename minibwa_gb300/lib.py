@@ -139,6 +139,7 @@ def load_library():
         "ksw2g_ll_batch_ref": (i32, [vp, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp, u8p, i64, vp]),
         "ksw2g_rescue_batch": (i32, [vp, vp, vp, i32, vp, u8p, i64, vp, vp, i64, vp]),
         "ksw2g_rescue_last_stats": (i32, [vp, vp, vp]),
+        "ksw2g_rescue_last_device_ms": (i32, [vp, vp]),
         "ksw2g_align_chains_last_stats": (i32, [vp, vp, vp]),
         "ksw2g_align_chains": (i32, [vp, vp, i32, vp, i32, vp, vp, i64, u8p, i64, vp, vp, i64, C.POINTER(i64)]),
         "ksw2g_align_pairs": (i32, [vp, vp, vp, i32, vp, u8p, i64, u8p, i64, vp, vp, i64, vp]),
@@ -517,6 +518,12 @@ class Reference:
         n = (C.c_int64 * 4)()
         _check(self.L.ksw2g_align_chains_last_stats(self.ctx.h, ms, n))
         return list(ms), list(n)
+
+    def rescue_device_ms(self):
+        """[ksw_ll, extz2] kernel time (ms) of the context's last rescue call."""
+        ms = (C.c_double * 2)()
+        _check(self.L.ksw2g_rescue_last_device_ms(self.ctx.h, ms))
+        return list(ms)
 
     def rescue_stats(self):
         """(kernel launches, [prefilter, ksw_ll, extz2] stage ms) of the context's last rescue call."""
