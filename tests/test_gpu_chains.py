@@ -103,3 +103,31 @@ def test_chains_edges(dev):
     with pytest.raises(RuntimeError):  # CIGAR buffer too small
         ref.align_chains(opt, z["chains"][:4], z["anchors"].copy(), z["qbuf"], cigar_cap=1)
     ref.close()
+
+
+@pytest.mark.parametrize("threads", ["1", "3"])
+def test_chains_host_thread_count(built, threads):
+    """The host stages of ksw2g_align_chains split hits over threads (KSW2G_HOST_THREADS, read once
+    per process): one and three threads give the fixture's results too."""
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    code = (
+        "import sys; sys.path.insert(0, 'tests')\n"
+        "from test_chains import chain_sets, expected, load_chains_golden\n"
+        "from test_gpu_chains import as_align1\n"
+        "from minibwa_gb300 import Context\n"
+        "from minibwa_gb300.lib import Reference\n"
+        "z = load_chains_golden(); ctx = Context(0)\n"
+        "ref = Reference(ctx, z['pac'], z['ctg_off'], z['ctg_len'], z['ambi'])\n"
+        "bad = 0\n"
+        "for name, opt, idx in chain_sets(z):\n"
+        "    ch = z['chains'][idx.start:idx.stop]\n"
+        "    res, cig = ref.align_chains(opt, ch, z['anchors'].copy(), z['qbuf'])\n"
+        "    bad += sum(as_align1(ch[k], res[k], cig) != expected(z, i) for k, i in enumerate(idx))\n"
+        "print('mismatches', bad)\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                         env=dict(os.environ, KSW2G_HOST_THREADS=threads))
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "mismatches 0" in out.stdout, out.stdout
