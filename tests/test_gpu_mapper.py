@@ -3,8 +3,9 @@ handed to the GPU at once (minibwa_gb300/mapper) maps the same reads as the stoc
 byte for byte.
 
 Stock minibwa is the reference compiled from its own sources (oracle/Makefile); the batched
-build is the same sources with align.o replaced, map-main.c's worker patched to defer each
-read's alignment, and libksw2gpu.so in place of the three ksw2 objects.  Read sets: the
+build is the same sources with three lines of map-main.c and one of pe.c substituted (each
+read's alignment deferred, the mini-batch's hits and mate-rescue windows aligned on the GPU),
+and libksw2gpu.so in place of the three ksw2 objects.  Read sets: the
 reference's own test pairs on chrM; 100,000 simulated pairs on a 4 Mb simulated genome with
 repeats (noisy mates for rescue, junk tails, chimeras); simulated long reads with inversions,
 junk blocks and chimeras (-x lr: z-drop splits, the inversion check, the long-read seed
@@ -105,3 +106,16 @@ def test_bisulfite_pairs(mp):
         a, b = sim_pairs(np.random.default_rng(20261205), g, 800, meth=True)
         write_fa(m1, a), write_fa(os.path.join(mp["dir"], "m2.fa"), b)
     _same(mp, ["--meth", "chrMm", "m1.fa", "m2.fa"], 1600)
+
+
+def test_missing_device_fails_loudly(mp):
+    """A GPU the batched mapper cannot open ends the run with an error and no SAM records,
+    rather than aligning anywhere else (no CPU fallback)."""
+    import subprocess
+    t1 = os.path.join(mp["tree"], "test", "chrM-read_1.fa.gz")
+    env = dict(os.environ, MBG_DEVICE="63")
+    out = subprocess.run([mp["batch"]["batch"], "map", "-t", "4", "chrM", t1], cwd=mp["dir"], capture_output=True,
+                         env=env)
+    assert out.returncode != 0
+    assert b"ksw2g_ctx_create" in out.stderr
+    assert not any(ln and not ln.startswith(b"@") for ln in out.stdout.splitlines())
