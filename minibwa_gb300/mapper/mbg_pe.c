@@ -62,6 +62,8 @@ typedef struct {
 	const uint32_t *cig;
 } mbg_pe_shared_t;
 
+#define MBG_MS(a, b) (((b).tv_sec - (a).tv_sec) * 1e3 + ((b).tv_usec - (a).tv_usec) * 1e-3)
+
 static __thread const mbg_pair_t *tl_pair;
 static __thread const mbg_pe_shared_t *tl_pe;
 
@@ -252,7 +254,6 @@ void mbg_pair_step(const mb_opt_t *opt, const mb_idx_t *idx, int n_thread, mb_tb
 	kt_for(n_thread, mbg_pe_worker, &s, n_frag);
 	gettimeofday(&t3, 0);
 	if (getenv("MBG_TIMING"))
-#define MBG_MS(a, b) ((b.tv_sec - a.tv_sec) * 1e3 + (b.tv_usec - a.tv_usec) * 1e-3)
 		fprintf(stderr, "[M::mbg] pairing: %ld fragments, %ld rescue windows; windows %.1f ms, device rescue %.1f ms, "
 				"mb_pair %.1f ms\n", (long)n_frag, (long)n_job, MBG_MS(t0, t1), MBG_MS(t1, t2), MBG_MS(t2, t3));
 	for (i = 0; i < n_frag; ++i) free(s.pr[i].win), free(s.pr[i].qs);
