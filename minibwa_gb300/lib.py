@@ -24,6 +24,8 @@ KSW_LL_STOP = 0x20000
 KSW_LL_SUBO = 0x40000
 
 # include/ksw2_gb300.h layouts
+KSW2G_E_CAPACITY = -5  # caller's output buffer too small (include/ksw2_gb300.h)
+
 EXT_JOB = np.dtype([("qoff", "<i8"), ("toff", "<i8"), ("qlen", "<i4"), ("tlen", "<i4"),
                     ("w", "<i4"), ("zdrop", "<i4"), ("end_bonus", "<i4"), ("flag", "<i4")])
 EXT_RESULT = np.dtype([("score", "<i4"), ("max", "<i4"), ("max_q", "<i4"), ("max_t", "<i4"),
@@ -502,13 +504,21 @@ class Reference:
             anchors = np.ascontiguousarray(anchors, ANCHOR)
         qbuf = _u8(qbuf)
         res = np.zeros(len(ch), CHAIN_RESULT)
+        grow = cigar_cap is None  # the default bound is a guess: grow it when a hit's CIGAR needs more
         if cigar_cap is None:
             cigar_cap = int(2 * ch["qlen"].astype(np.int64).sum() + 4 * ch["cnt"].astype(np.int64).sum()) + 64
-        cig = np.zeros(max(int(cigar_cap), 1), np.uint32)
         used = C.c_int64()
-        _check(self.L.ksw2g_align_chains(self.ctx.h, self.h, len(o), _ptr(o), len(ch), _ptr(ch), _ptr(anchors),
-                                         len(anchors), _ptr(qbuf), len(qbuf), _ptr(res), _ptr(cig), int(cigar_cap),
-                                         C.byref(used)))
+        while True:
+            cig = np.zeros(max(int(cigar_cap), 1), np.uint32)
+            flags = anchors["flag"].copy()
+            rc = self.L.ksw2g_align_chains(self.ctx.h, self.h, len(o), _ptr(o), len(ch), _ptr(ch), _ptr(anchors),
+                                           len(anchors), _ptr(qbuf), len(qbuf), _ptr(res), _ptr(cig),
+                                           int(cigar_cap), C.byref(used))
+            if rc != KSW2G_E_CAPACITY or not grow:
+                break
+            anchors["flag"] = flags  # the call is repeated on the anchors as they were
+            cigar_cap *= 2
+        _check(rc)
         return res, cig[:used.value]
 
     def chains_stats(self):
