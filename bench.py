@@ -642,13 +642,18 @@ def serving_point(frac=0.8, duration=3.0):
     the reference CPU implementation's rate on a sample of the same mix."""
     from minibwa_gb300 import serving
     from oracle import oracle as O
-    out = serving.sweep(duration=duration, fracs=(frac,), percall_threads=0, check=True, log=open(os.devnull, "w"))
+    # the per-call drop-in's closed-loop rate on the same mix (16 caller threads, about 4 s at most)
+    out = serving.sweep(duration=duration, fracs=(frac,), percall_threads=16, check=True, log=open(os.devnull, "w"),
+                        percall_peak_jobs=6000, percall_deadline=1.0, percall_peak_only=True)
     row = out["rates"][0]
     line = {"metric": "served jobs/s at %d%% of peak, p50/p99 latency" % round(frac * 100),
             "value": row["served_jobs_s"], "unit": "jobs/s", "p50_ms": row["p50_ms"], "p99_ms": row["p99_ms"],
             "max_ms": row["max_ms"], "offered_jobs_s": row["offered_jobs_s"], "peak_jobs_s": out["peak_jobs_s"],
             "requests": row["requests"], "duration_s": duration,
             "mismatches_vs_alone": out["mismatches_vs_alone"],
+            "percall_dropin_jobs_s": out.get("percall_peak_jobs_s"),
+            "engine_peak_over_percall": (out["peak_jobs_s"] / out["percall_peak_jobs_s"]
+                                         if out.get("percall_peak_jobs_s") else None),
             "mix": "70% extz2 150 nt w=25, 20% extd2 log-normal 1-10 kb w=500, 10% ksw_ll i16; request batches "
                    "of 1-4096 jobs, Poisson arrivals; 8 slots, 40 GB traceback budget"}
     # CPU: the reference's functions over a sample of the three pools in the mix's proportions

@@ -195,7 +195,8 @@ def pct(a, q):
 
 
 def sweep(duration=3.0, fracs=(0.1, 0.25, 0.5, 0.8, 1.0), slots=8, budget=40 << 30, percall_threads=16,
-          percall_deadline=4.0, check=True, log=sys.stderr, max_merge=None):
+          percall_deadline=4.0, check=True, log=sys.stderr, max_merge=None, percall_peak_jobs=20000,
+          percall_peak_only=False):
     from .lib import Context, Server
     sets = JobSets()
     srv = Server(0, slots=slots, tb_budget=budget, max_merge=max_merge)
@@ -228,13 +229,13 @@ def sweep(duration=3.0, fracs=(0.1, 0.25, 0.5, 0.8, 1.0), slots=8, budget=40 << 
     srv.close()
     # per-call drop-in: closed-loop peak, then the same open-loop rates under a deadline
     if percall_threads > 0:
-        tr = Trace(sets, 20000, None, seed=5)
+        tr = Trace(sets, percall_peak_jobs, None, seed=5)
         pc = run_percall(sets, tr, percall_threads, percall_deadline * 4)
         out["percall_peak_jobs_s"] = pc["done"] / pc["wall"] if pc["wall"] > 0 else None
         out["percall_threads"] = percall_threads
         print(f"per-call peak: {pc['done']} jobs in {pc['wall']:.3f} s", file=log, flush=True)
         out["percall_rates"] = []
-        for fr in fracs:
+        for fr in (() if percall_peak_only else fracs):
             rate = fr * peak
             tr = Trace(sets, int(rate * min(duration, 1.0)), rate, seed=int(fr * 1000) + 3)
             pc = run_percall(sets, tr, percall_threads, percall_deadline)
