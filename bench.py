@@ -674,10 +674,22 @@ def serving_point(frac=0.8, duration=3.0):
     return line
 
 
-def mapper_point(n_pairs=100_000):
+def _timed_run(cmd, cwd, env=None):
+    """(completed process, wall s, CPU s of the child: user + system)"""
+    import resource
+    r0 = resource.getrusage(resource.RUSAGE_CHILDREN)
+    t0 = time.perf_counter()
+    out = subprocess.run(cmd, cwd=cwd, capture_output=True, env=env)
+    dt = time.perf_counter() - t0
+    r1 = resource.getrusage(resource.RUSAGE_CHILDREN)
+    return out, dt, (r1.ru_utime - r0.ru_utime) + (r1.ru_stime - r0.ru_stime)
+
+
+def mapper_point(n_pairs=100_000, n_long=1000):
     """The batched minibwa (minibwa_gb300/mapper) against the stock build of the same reference
-    sources on the same simulated pairs, both with all host threads: reads mapped per second of
-    wall time, whether their SAM outputs are byte-identical, and the batched run's stages."""
+    sources on the same simulated reads, both with all host threads: reads mapped per second of
+    wall time and the host CPU time each spent, whether their SAM outputs are byte-identical, and
+    the batched run's stages.  Pairs (the short-read preset) and long reads (-x lr)."""
     import shutil
     import tempfile
     from minibwa_gb300 import mapper, synth
@@ -688,34 +700,39 @@ def mapper_point(n_pairs=100_000):
     stock = O.build_minibwa_stock()
     batch = mapper.build(tree)["batch"]
     d = tempfile.mkdtemp(prefix="mapper_point_")
+    threads = os.cpu_count() or 1
+    runs = {}
     try:
         g = synth.mapper_genome(ctg_len=(6_000_000, 4_000_000, 2_000_000), n_repeats=800)
         synth.write_fasta(os.path.join(d, "g.fa"), g)
         mapper.index(stock, "g.fa", "g", d)
         a, b = synth.mapper_pairs(g, n_pairs)
         synth.write_fasta(os.path.join(d, "p1.fa"), a), synth.write_fasta(os.path.join(d, "p2.fa"), b)
-        threads = os.cpu_count() or 1
-        args = ["g", "p1.fa", "p2.fa"]
-        mapper.map_reads(stock, args, d, threads)  # page in the index and the binaries
-        sa, ts = mapper.map_reads(stock, args, d, threads)
+        synth.write_fasta(os.path.join(d, "long.fa"), synth.mapper_long_reads(g, n_long))
         env = dict(os.environ, MBG_TIMING="1")
-        t0 = time.perf_counter()
-        out = subprocess.run([batch, "map", "-t", str(threads)] + args, cwd=d, capture_output=True, env=env)
-        tb = time.perf_counter() - t0
-        if out.returncode != 0:
-            return {"unavailable": "batched minibwa failed: " + out.stderr.decode(errors="replace")[-300:]}
-        stages = [ln.split("] ", 1)[1] for ln in out.stderr.decode().splitlines() if ln.startswith("[M::mbg]")]
+        for name, args, n in (("pairs", ["g", "p1.fa", "p2.fa"], 2 * n_pairs),
+                              ("long_reads", ["-x", "lr", "g", "long.fa"], n_long)):
+            mapper.map_reads(stock, args, d, threads)  # page in the index and the binary
+            so, ts, cs = _timed_run([stock, "map", "-t", str(threads)] + args, d)
+            bo, tb, cb = _timed_run([batch, "map", "-t", str(threads)] + args, d, env)
+            if so.returncode != 0 or bo.returncode != 0:
+                return {"unavailable": "minibwa failed: " + (bo.stderr or so.stderr).decode(errors="replace")[-300:]}
+            runs[name] = {"reads": n, "batched_reads_s": n / tb, "stock_reads_s": n / ts, "batched_wall_s": tb,
+                          "stock_wall_s": ts, "batched_cpu_s": cb, "stock_cpu_s": cs,
+                          "sam_identical_to_stock": bo.stdout == so.stdout,
+                          "stages": [ln.split("] ", 1)[1] for ln in bo.stderr.decode().splitlines()
+                                     if ln.startswith("[M::mbg]")]}
     finally:
         shutil.rmtree(d, ignore_errors=True)
-    n = 2 * n_pairs
-    return {"metric": "reads mapped/s, whole minibwa run (index loaded, SAM written)", "value": n / tb,
-            "unit": "reads/s", "wall_s": tb, "sam_identical_to_stock": out.stdout == sa,
-            "workload": f"{n_pairs} simulated 150 nt pairs (synth.mapper_pairs) on a 12 Mb simulated genome with "
-                        f"800 near-repeats, minibwa map -t {threads}",
-            "stages": stages,
-            "cpu_baseline": {"value": n / ts, "unit": "reads/s", "cores": threads, "kind": "reference",
-                             "sample": f"the stock minibwa built from the reference's sources, same reads, "
-                                       f"{threads} threads, {ts:.2f} s wall"}}
+    p = runs["pairs"]
+    return {"metric": "reads mapped/s, whole minibwa run (index loaded, SAM written)", "value": p["batched_reads_s"],
+            "unit": "reads/s", "sam_identical_to_stock": all(r["sam_identical_to_stock"] for r in runs.values()),
+            "workload": f"{n_pairs} simulated 150 nt pairs and {n_long} long reads (1-8 kb, -x lr) from synth on a "
+                        f"12 Mb simulated genome with 800 near-repeats, minibwa map -t {threads}",
+            "runs": runs,
+            "cpu_baseline": {"value": p["stock_reads_s"], "unit": "reads/s", "cores": threads, "kind": "reference",
+                             "sample": f"the stock minibwa built from the reference's sources, same pairs, "
+                                       f"{threads} threads, {p['stock_wall_s']:.2f} s wall"}}
 
 
 def main():
