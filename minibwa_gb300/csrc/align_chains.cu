@@ -13,6 +13,9 @@
 // the exact second pass (align.c:690-693) in a second batch, and assembles each chain in order,
 // discarding the speculative jobs behind a z-drop.  The hit then holds what mb_align1 leaves
 // in it before mb_update_extra (align.c:753), which the caller runs.
+// The host stages -- deriving the jobs, copying the sequences into the batches, the z-drop
+// scans and the assembly -- run over the host threads (host_parallel.h), one chain per item;
+// results do not depend on the thread count.
 #include <cuda_runtime.h>
 #include <string.h>
 
