@@ -121,7 +121,12 @@ struct Bin {
   int mode, shape;
   int64_t order_off;
   int count;
+  double cost;  // rough device cycles (bin_cost in capi.cu)
+  int sub;      // stream of the wave it runs on: 0 the wave's own, s > 0 side stream s - 1
 };
+// Bins of one wave run at once on the wave's stream and up to kSideStreams side streams,
+// which fork from it at the wave's start and join it before the wave's backtrack.
+constexpr int kSideStreams = 3;
 struct Wave {
   int w0, w1;            // range of the longest-first job order (batch->sorted)
   int64_t tb_bytes;
@@ -150,7 +155,25 @@ struct ksw2g_batch {
   std::vector<int> tkind;        // 0 DP kernel, 1 backtrack kernel, per timed launch
   int n_timed = 0;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // two-stream runs
+  // side streams of multi-bin waves and their fork and join events, one set per stream
+  // parity of a two-stream run; created on first use
+  cudaStream_t side[2][kSideStreams] = {};
+  cudaEvent_t ev_wfork[2] = {}, ev_wjoin[2][kSideStreams] = {};
 };
+
+// Destroy the batch's events and side streams (work already enqueued on them completes).
+inline void batch_release_streams(ksw2g_batch *b) {
+  for (cudaEvent_t e : b->tev) cudaEventDestroy(e);
+  b->tev.clear();
+  b->n_timed = 0;
+  for (cudaEvent_t *e : {&b->ev_fork, &b->ev_join, &b->ev_wfork[0], &b->ev_wfork[1]})
+    if (*e) cudaEventDestroy(*e), *e = nullptr;
+  for (int p = 0; p < 2; ++p)
+    for (int i = 0; i < kSideStreams; ++i) {
+      if (b->ev_wjoin[p][i]) cudaEventDestroy(b->ev_wjoin[p][i]), b->ev_wjoin[p][i] = nullptr;
+      if (b->side[p][i]) cudaStreamDestroy(b->side[p][i]), b->side[p][i] = nullptr;
+    }
+}
 
 
 // Make every device buffer of the batch grow in stream order on st.

@@ -31,6 +31,9 @@ cudaError_t launch_ext_dp_d2(int mode, int shape, const ksw2g_ext_params &P, con
 cudaError_t launch_ext_dp(int dual, int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L,
                           int max_blocks, cudaStream_t st) {
   if (shape == kWideShape) return launch_ext_wide(P, L, st);
+  if (shape >= kSplitBase)
+    return dual ? launch_ext_split_d2(mode, shape - kSplitBase, P, L, max_blocks, st)
+                : launch_ext_split_z2(mode, shape - kSplitBase, P, L, max_blocks, st);
   if (shape >= kExt16Base)
     return dual ? launch_ext16_dp_d2(mode, shape - kExt16Base, P, L, max_blocks, st)
                 : launch_ext16_dp_z2(mode, shape - kExt16Base, P, L, max_blocks, st);
@@ -48,6 +51,23 @@ static int g_pref[2][3][kMaxPrefCol + 1];
 static std::mutex g_pref_mu;
 // lane width forced on every batch: -1 none (preferences decide), 0 bytes, 1 16-bit halves
 static std::atomic<int> g_family{-1};
+// block-split kernel (ksw2g_ext_set_split): -1 the batch decides, 0 never, 1 wherever a split
+// shape holds the band
+static std::atomic<int> g_split{0};
+// A batch runs its jobs of one (mode, shape) on the block-split kernel when they number at most
+// kSplitMaxJobs and their bands are wider than kSplitMinCol 16-cell blocks.  A thread group
+// computes a pair's anti-diagonals one after another (one 10 kb extd2 pair at w=500 takes
+// 1.42 us per anti-diagonal on a GB300, the same with up to 608 such pairs at once), so a
+// batch of few long pairs lasts as long as its longest pair on one group; a block splits
+// each anti-diagonal over its warps.
+static const int kSplitMinCol = 16;
+static const int kSplitMaxJobs = 304;
+
+static bool use_split(int n_col, int count) {
+  const int m = g_split.load(std::memory_order_relaxed);
+  if (m == 0 || ext_split_for(n_col) < 0) return false;
+  return m == 1 || (n_col > kSplitMinCol && count <= kSplitMaxJobs);
+}
 
 static bool shape_holds(int s, int n_col) {
   return s >= 0 && s < kNumExtShapes && kExtShapes[s].G * kExtShapes[s].K >= 4 * n_col;
@@ -168,9 +188,7 @@ extern "C" void ksw2g_batch_free(ksw2g_batch_t *b) {
   for (DevBuf *d : {&b->raw, &b->rawmeta, &b->arena, &b->jobs, &b->order, &b->sorted, &b->tb_off, &b->res, &b->bts, &b->cigar,
                     &b->counters, &b->llmat, &b->blist, &b->blist_off, &b->wide})
     d->release();
-  for (cudaEvent_t e : b->tev) cudaEventDestroy(e);
-  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
-  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  batch_release_streams(b);
   delete b;
 }
 extern "C" int ksw2g_batch_launches(const ksw2g_batch_t *b) { return b ? b->launches : 0; }
@@ -326,6 +344,37 @@ int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   return ext_prepare_segs(c, b, dual, m, mat, q, e, q2, e2, 1, &seg);
 }
 
+// Rough device time of a bin in cycles, to spread the bins of a wave over streams: its
+// longest pair's anti-diagonals at one group's latency plus all its anti-diagonal words
+// at the whole device's rate.  Measured on a GB300: one 10 kb extd2 pair at w=500 alone
+// takes about 2,200 + 140 K cycles per anti-diagonal on a group of K words a thread, and
+// the block-wide kernel about 8,000; 1,000,000 config-1 pairs run at about 0.02 cycles per
+// anti-diagonal word.
+static double bin_cost(int shape, int64_t max_diag, double diag_words) {
+  double lat = 8000.0;
+  if (shape >= kSplitBase) lat = 1000.0;  // to be measured
+  else if (shape != kWideShape) lat = 2200.0 + 140.0 * kExtShapes[shape >= kExt16Base ? shape - kExt16Base : shape].K;
+  return (double)max_diag * lat + 0.02 * diag_words;
+}
+// Assign the bins of a wave to its streams, costliest first, each to the stream with the least
+// cost so far (the longest-processing-time rule), and order them that way for launching.  The
+// block-wide kernel's bins share one stream, because they share the wave's scratch.
+static void spread_bins(std::vector<Bin> &bins) {
+  std::stable_sort(bins.begin(), bins.end(), [](const Bin &a, const Bin &b) { return a.cost > b.cost; });
+  double load[1 + kSideStreams] = {};
+  int wide_sub = -1;
+  for (Bin &bn : bins) {
+    int s = 0;
+    if (bn.shape == kWideShape && wide_sub >= 0) s = wide_sub;
+    else
+      for (int i = 1; i <= kSideStreams; ++i)
+        if (load[i] < load[s]) s = i;
+    if (bn.shape == kWideShape) wide_sub = s;
+    load[s] += bn.cost;
+    bn.sub = s;
+  }
+}
+
 int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int8_t *mat, int8_t q, int8_t e,
                      int8_t q2, int8_t e2, int nseg, const SeqSeg *segs, const RefTargets *rt) {
   if (rt && (nseg != 1 || !rt->ref || (segs[0].n > 0 && !rt->tid)))
@@ -346,7 +395,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   derive_ext_params(dual, m, mat, q, e, q2, e2, b->P);
   std::vector<int64_t> qo(n), to(n);
   std::vector<int32_t> ql(n), tl(n);
-  std::vector<int> shape(n), mode(n);
+  std::vector<int> shape(n), mode(n), ncol(n);
   std::vector<int64_t> foot(n);
   int64_t cig = 0, wide_max = 0;
   double band_cells = 0;  // sum of (qlen + tlen) x band width: the batch's size class
@@ -364,7 +413,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     const bool live = J.qlen > 0 && J.tlen > 0 && !b->P.skip_all;
     const int nc = live ? ext_ncol(J.qlen, J.tlen, J.w) : 1;
     shape[i] = ext_shape_id(dual, mode[i], nc, b->P);
-    if (shape[i] == kWideShape) ++n_wide, wide_max = std::max(wide_max, ext_wide_scratch(J.qlen, J.tlen));
+    ncol[i] = nc;
     foot[i] = (live && mode[i] != 0) ? (((int64_t)(J.qlen + J.tlen - 1) * nc * 16 + 15) & ~(int64_t)15) : 0;
     if (foot[i] > c->tb_budget)
       return set_err(KSW2G_E_CAPACITY, "job %d: traceback needs %lld bytes, budget %lld", i, (long long)foot[i],
@@ -372,6 +421,15 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     if (mode[i] != 0) cig += J.qlen + J.tlen + 1;
     band_cells += (double)(J.qlen + J.tlen) * (nc > 1 ? 16.0 * (nc - 1) : 0.0);
   }
+  {  // jobs of the (mode, shape) classes that hold few of them move to the block-split kernel
+    std::vector<int> cnt(3 * kNumShapeIds, 0);
+    for (int i = 0; i < n; ++i) ++cnt[mode[i] * kNumShapeIds + shape[i]];
+    for (int i = 0; i < n; ++i)
+      if (jobs[i].qlen > 0 && jobs[i].tlen > 0 && use_split(ncol[i], cnt[mode[i] * kNumShapeIds + shape[i]]))
+        shape[i] = kSplitBase + ext_split_for(ncol[i]);
+  }
+  for (int i = 0; i < n; ++i)
+    if (shape[i] == kWideShape) ++n_wide, wide_max = std::max(wide_max, ext_wide_scratch(jobs[i].qlen, jobs[i].tlen));
   std::vector<int64_t> qpad, tpad;
   int rc = upload_and_pack(c, b, n, qo.data(), ql.data(), to.data(), tl.data(), nseg, segs, qpad, tpad, rt);
   if (rc) return rc;
@@ -410,6 +468,8 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   const int nshp = kNumShapeIds;  // both lane widths' shapes and the block-wide kernel
   const int nbins = 3 * nshp;
   std::vector<int32_t> bcount(nbins), bpos(nbins);
+  std::vector<int64_t> bmaxd(nbins);
+  std::vector<double> bwords(nbins);
   for (int i = 0; i < n;) {
     Wave wv;
     wv.w0 = i;
@@ -420,15 +480,24 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     wv.tb_bytes = acc;
     std::fill(bcount.begin(), bcount.end(), 0);
     for (int k = wv.w0; k < wv.w1; ++k) ++bcount[mode[srt[k]] * nshp + shape[srt[k]]];
+    std::fill(bmaxd.begin(), bmaxd.end(), 0);
+    std::fill(bwords.begin(), bwords.end(), 0.0);
+    for (int k = wv.w0; k < wv.w1; ++k) {
+      const int j = srt[k], bi = mode[j] * nshp + shape[j];
+      const int64_t nd = std::max<int64_t>((int64_t)ql[j] + tl[j] - 1, 0);
+      bmaxd[bi] = std::max(bmaxd[bi], nd);
+      bwords[bi] += (double)nd * 4.0 * ncol[j];
+    }
     for (int bi = 0; bi < nbins; ++bi) {
       bpos[bi] = (int32_t)ordp;
       if (bcount[bi]) {
-        wv.bins.push_back(Bin{bi / nshp, bi % nshp, ordp, bcount[bi]});
+        wv.bins.push_back(Bin{bi / nshp, bi % nshp, ordp, bcount[bi], bin_cost(bi % nshp, bmaxd[bi], bwords[bi]), 0});
         wv.any_cig |= bi / nshp != 0;
       }
       ordp += bcount[bi];
     }
     for (int k = wv.w0; k < wv.w1; ++k) ord[bpos[mode[srt[k]] * nshp + shape[srt[k]]]++] = srt[k];
+    spread_bins(wv.bins);
     b->waves.push_back(wv);
   }
   b->n_counters = 0;
@@ -536,18 +605,35 @@ int ext_run_on2(ksw2g_batch *b, cudaStream_t s0, cudaStream_t s1, uint8_t *tb0, 
   int ci = 0;
   for (size_t w = 0; w < b->waves.size(); ++w) {
     const Wave &wv = b->waves[w];
-    st = two && (w & 1) ? s1 : s0;
-    tb = two && (w & 1) ? tb1 : tb0;
+    const int par = two && (w & 1) ? 1 : 0;
+    st = par ? s1 : s0;
+    tb = par ? tb1 : tb0;
+    int nside = 0;
+    for (auto &bn : wv.bins) nside = std::max(nside, bn.sub);
+    if (nside) {  // fork the side streams from the wave's stream (after its previous wave's backtrack)
+      if (!b->ev_wfork[par]) CK(cudaEventCreateWithFlags(&b->ev_wfork[par], cudaEventDisableTiming));
+      for (int i = 0; i < nside; ++i) {
+        if (!b->side[par][i]) CK(cudaStreamCreateWithFlags(&b->side[par][i], cudaStreamNonBlocking));
+        if (!b->ev_wjoin[par][i]) CK(cudaEventCreateWithFlags(&b->ev_wjoin[par][i], cudaEventDisableTiming));
+      }
+      CK(cudaEventRecord(b->ev_wfork[par], st));
+      for (int i = 0; i < nside; ++i) CK(cudaStreamWaitEvent(b->side[par][i], b->ev_wfork[par], 0));
+    }
     for (auto &bn : wv.bins) {
+      const cudaStream_t bs = bn.sub ? b->side[par][bn.sub - 1] : st;
       ExtLaunch L{dj, dord + bn.order_off, bn.count, b->arena.as<uint8_t>(), dr, db, tb, dto,
                   jc + ci++};
       if (bn.shape == kWideShape)  // each stream of a two-stream run has its own half of the scratch
-        L.wide_scratch = b->wide.as<uint8_t>() + (size_t)(st == s0 ? 0 : 1) * b->wide_blocks * b->wide_stride,
+        L.wide_scratch = b->wide.as<uint8_t>() + (size_t)par * b->wide_blocks * b->wide_stride,
         L.wide_stride = b->wide_stride, L.wide_blocks = b->wide_blocks;
-      CK(timed_begin(b, 0, st));
-      CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, st));
-      CK(timed_end(b, st));
+      CK(timed_begin(b, 0, bs));
+      CK(launch_ext_dp(b->kind, bn.mode, bn.shape, b->P, L, 0, bs));
+      CK(timed_end(b, bs));
       ++b->launches;
+    }
+    for (int i = 0; i < nside; ++i) {
+      CK(cudaEventRecord(b->ev_wjoin[par][i], b->side[par][i]));
+      CK(cudaStreamWaitEvent(st, b->ev_wjoin[par][i], 0));
     }
     if (wv.any_cig) {
       CK(timed_begin(b, 1, st));
@@ -828,6 +914,12 @@ extern "C" int ksw2g_ext_set_family(int family) {
   return 0;
 }
 extern "C" int ksw2g_ext_get_family(void) { return g_family.load(); }
+extern "C" int ksw2g_ext_set_split(int mode) {
+  if (mode < -1 || mode > 1) return set_err(KSW2G_E_ARG, "split mode must be -1 (batch decides), 0 (never) or 1 (always)");
+  g_split.store(mode);
+  return 0;
+}
+extern "C" int ksw2g_ext_get_split(void) { return g_split.load(); }
 
 // ---------------------------------------------------------------- per-call drop-in
 // Allocation of ez->cigar and of the ksw_ll_qinit block follows the caller's
@@ -896,7 +988,8 @@ static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen
   ksw2g_ctx *c = thread_ctx();
   const int mode = ext_mode(flag);
   const int nc = ext_ncol(qlen, tlen, w);
-  const int shape = ext_shape_id(dual, mode, nc, P);
+  int shape = ext_shape_id(dual, mode, nc, P);
+  if (use_split(nc, 1)) shape = kSplitBase + ext_split_for(nc);
   const int64_t ncig = mode ? (int64_t)qlen + tlen + 1 : 0;
   const int64_t foot = mode ? (int64_t)(qlen + tlen - 1) * nc * 16 : 0;
   const size_t o_job = 32, o_tbo = o_job + 48, o_bt = o_tbo + 16, o_res = o_bt + 16;

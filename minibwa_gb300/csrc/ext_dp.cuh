@@ -85,6 +85,187 @@ __device__ __forceinline__ uint32_t ld_qw(const uint8_t *qp, int hi, int qlen) {
   return w;
 }
 
+// Batch constants of the cell recurrence and the score lookup, in byte lanes.
+struct ExtConsts {
+  uint32_t q4, q24, qe4, qe24, mch4, mis4, N4, m14, maxsc4, mchraw4, sc_lo, sc_hi;
+  uint32_t initb, init2b, init4, init24, s_init4;
+  bool nt4;
+};
+template <int VAR>
+__device__ __forceinline__ ExtConsts ext_consts(const ksw2g_ext_params &P) {
+  constexpr bool D2 = VAR == 1;
+  ExtConsts c;
+  c.q4 = splat8(P.c_q), c.q24 = splat8(P.c_q2), c.qe4 = splat8(P.c_qe), c.qe24 = splat8(P.c_qe2);
+  c.mch4 = splat8(D2 ? P.c_mch : P.c_mch + P.c_qe2);  // extz2 stores s + 2(q+e)
+  c.mis4 = splat8(D2 ? P.c_mis : P.c_mis + P.c_qe2);
+  c.N4 = splat8(D2 ? P.c_N : P.c_N + P.c_qe2);
+  c.m14 = splat8(P.c_m1), c.maxsc4 = splat8(P.c_maxsc), c.mchraw4 = splat8(P.c_mch);
+  // score table of the byte-permute lookup: lane index 0 = match, 1-3 = mismatch, 4-7 = N
+  c.nt4 = P.c_m1 == 4;
+  c.sc_lo = (c.mch4 & 0xffu) | (c.mis4 & 0xffffff00u), c.sc_hi = c.N4;
+  c.initb = D2 ? (uint32_t)(uint8_t)(-P.q - P.e) : 0u;
+  c.init2b = D2 ? (uint32_t)(uint8_t)(-P.q2 - P.e2) : 0u;
+  c.init4 = splat8(c.initb), c.init24 = splat8(c.init2b);
+  c.s_init4 = D2 ? 0u : splat8(P.c_qe2);
+  return c;
+}
+// H increment of one byte of u or v: extd2 stores it signed, extz2 biased by q+e
+template <int VAR>
+__device__ __forceinline__ int32_t ext_vv(uint32_t byte, int qe) {
+  return VAR ? (int32_t)(int8_t)(uint8_t)byte : (int32_t)(byte & 0xffu) - qe;
+}
+
+// The four query bytes of a word whose lowest query index is idx0 (lane j = query[idx0 + 3 - j]
+// after the permute qsel of the anti-diagonal).
+__device__ __forceinline__ uint32_t ld_qword(const uint8_t *qp, int idx0, uint32_t qsel) {
+  const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
+  return __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
+}
+// Scores of four lanes by one byte-permute lookup, exact for m = 5 (N = 4) where every lane has
+// t | q <= 4: the lane index (t ^ q) & 3 | (t | q) & 4 is 0 for a match, 1-3 for a mismatch and 4
+// for N.  A lane with t | q >= 5 sets bits 3-7 of its byte in bad.
+__device__ __forceinline__ uint32_t score_lookup(uint32_t Tw, uint32_t Qw, const ExtConsts &c, uint32_t &bad) {
+  const uint32_t tq = Tw | Qw;
+  const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | (tq & 0x04040404u);
+  bad |= tq | (tq + 0x03030303u);
+  return __byte_perm(c.sc_lo, c.sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
+}
+// Scores of four lanes by the general comparisons (ksw2_extz2_sse.c:117-136), or from the
+// matrix under KSW_EZ_GENERIC_SC.
+template <int VAR>
+__device__ __forceinline__ uint32_t score_exact(uint32_t Tw, uint32_t Qw, bool generic, const ksw2g_ext_params &P,
+                                                const ExtConsts &c) {
+  uint32_t sn;
+  if (!generic) {
+    const uint32_t eq = eqz8(Tw ^ Qw);
+    const uint32_t nn = eqz8(Tw ^ c.m14) | eqz8(Qw ^ c.m14);
+    sn = sel(bmask(eq), c.mch4, c.mis4);
+    sn = sel(bmask(nn), c.N4, sn);
+  } else {
+    sn = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int tc = (Tw >> (8 * b)) & 0xff, qc = (Qw >> (8 * b)) & 0xff;
+      uint32_t v = (uint32_t)(uint8_t)P.mat[(tc * P.m + qc) & 255];
+      if (!VAR) v = (v + P.c_qe2) & 0xffu;
+      sn |= v << (8 * b);
+    }
+  }
+  return sn;
+}
+
+// One word (four cells) of an anti-diagonal (ksw2_extz2_sse.c:142-215, ksw2_extd2_sse.c:183-314):
+// xt1, vt1, x2t1 are x, v, x2 of the cells t-1 .. t+2 on the anti-diagonal before, s the scores;
+// u, v, x, y (x2, y2) are updated in place and the traceback byte lanes returned.
+template <int VAR, int MODE>
+__device__ __forceinline__ uint32_t ext_cell(uint32_t xt1, uint32_t vt1, uint32_t x2t1, uint32_t s, uint32_t &U,
+                                             uint32_t &V, uint32_t &X, uint32_t &Y, uint32_t &X2, uint32_t &Y2,
+                                             const ExtConsts &c) {
+  const uint32_t ut = U;
+  uint32_t z = s, a = add8(xt1, vt1), b = add8(Y, ut), d = 0;
+  uint32_t nu, nv, nx, ny, nx2 = 0, ny2 = 0;
+  if (!VAR) {
+    if (MODE == 0) {
+      z = maxs8(z, a);
+    } else if (MODE == 1) {
+      const uint32_t M = bmask(gts8(a, z));
+      d = M & 0x01010101u;
+      z = sel(M, a, z);
+      d = sel(bmask(gts8(b, z)), 0x02020202u, d);
+    } else {
+      const uint32_t M = bmask(gts8(z, a));
+      d = ~M & 0x01010101u;
+      z = sel(M, z, a);
+      d = sel(bmask(gts8(z, b)), d, 0x02020202u);
+    }
+    z = maxu8(z, b);
+    z = minu8(z, c.maxsc4);
+    nu = sub8(z, vt1);
+    nv = sub8(z, ut);
+    z = sub8(z, c.q4);
+    a = sub8(a, z);
+    b = sub8(b, z);
+    if (MODE == 1) {
+      const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi;
+      nx = a & bmask(ga);
+      ny = b & bmask(gb);
+      d |= (ga >> 4) | (gb >> 3);
+    } else {
+      nx = relu8(a);
+      ny = relu8(b);
+      if (MODE == 2) d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3);
+    }
+  } else {
+    uint32_t a2 = add8(x2t1, vt1), b2 = add8(Y2, ut);
+    if (MODE == 0) {
+      z = maxs8(z, a);
+      z = maxs8(z, b);
+      z = maxs8(z, a2);
+      z = maxs8(z, b2);
+    } else if (MODE == 1) {
+      uint32_t M = bmask(gts8(a, z));
+      d = M & 0x01010101u;
+      z = sel(M, a, z);
+      M = bmask(gts8(b, z));
+      d = sel(M, 0x02020202u, d);
+      z = sel(M, b, z);
+      M = bmask(gts8(a2, z));
+      d = sel(M, 0x03030303u, d);
+      z = sel(M, a2, z);
+      M = bmask(gts8(b2, z));
+      d = sel(M, 0x04040404u, d);
+      z = sel(M, b2, z);
+    } else {
+      uint32_t M = bmask(gts8(z, a));
+      d = ~M & 0x01010101u;
+      z = sel(M, z, a);
+      M = bmask(gts8(z, b));
+      d = sel(M, d, 0x02020202u);
+      z = sel(M, z, b);
+      M = bmask(gts8(z, a2));
+      d = sel(M, d, 0x03030303u);
+      z = sel(M, z, a2);
+      M = bmask(gts8(z, b2));
+      d = sel(M, d, 0x04040404u);
+      z = sel(M, z, b2);
+    }
+    z = mins8(z, c.mchraw4);
+    nu = sub8(z, vt1);
+    nv = sub8(z, ut);
+    uint32_t tq = sub8(z, c.q4);
+    a = sub8(a, tq);
+    b = sub8(b, tq);
+    tq = sub8(z, c.q24);
+    a2 = sub8(a2, tq);
+    b2 = sub8(b2, tq);
+    if (MODE == 1) {
+      const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi, ga2 = gt0s8(a2) & kHi, gb2 = gt0s8(b2) & kHi;
+      nx = sub8_nn((a & bmask(ga)) | kHi, c.qe4);
+      ny = sub8_nn((b & bmask(gb)) | kHi, c.qe4);
+      nx2 = sub8_nn((a2 & bmask(ga2)) | kHi, c.qe24);
+      ny2 = sub8_nn((b2 & bmask(gb2)) | kHi, c.qe24);
+      d |= (ga >> 4) | (gb >> 3) | (ga2 >> 2) | (gb2 >> 1);
+    } else {
+      nx = sub8_nn(relu8(a) | kHi, c.qe4);
+      ny = sub8_nn(relu8(b) | kHi, c.qe4);
+      nx2 = sub8_nn(relu8(a2) | kHi, c.qe24);
+      ny2 = sub8_nn(relu8(b2) | kHi, c.qe24);
+      if (MODE == 2) d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3) | ((~a2 & kHi) >> 2) | ((~b2 & kHi) >> 1);
+    }
+  }
+  U = nu, V = nv, X = nx, Y = ny;
+  if (VAR) X2 = nx2, Y2 = ny2;
+  return d;
+}
+
+// Tie-break key of the reference's exact max (ksw2_extz2_sse.c:216-261) for the cell at offset
+// o = t - st0 of an anti-diagonal whose band is [st0, st0 + E]: en0 first (key 0), then the four
+// int32 lanes over [st0, en1) -- lowest lane, then lowest t --, then the scalar tail [en1, en0).
+__device__ __forceinline__ uint32_t max_key(int o, int E) {
+  const int L4 = E & ~3;
+  return o == E ? 0u : o < L4 ? ((uint32_t)(1 + (o & 3)) << 24) | (uint32_t)o : (5u << 24) | (uint32_t)o;
+}
+
 // VAR: 0 = extz2 (affine), 1 = extd2 (dual affine)
 // MODE: 0 = score only, 1 = left-aligned gaps with traceback, 2 = right-aligned gaps with traceback
 #ifndef KSW2G_EXT_MINB4
@@ -109,18 +290,8 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
   const unsigned gm = group_mask<G>();
 
   // batch constants (byte lanes)
-  const uint32_t q4 = splat8(P.c_q), q24 = splat8(P.c_q2), qe4 = splat8(P.c_qe), qe24 = splat8(P.c_qe2);
-  const uint32_t mch4 = splat8(D2 ? P.c_mch : P.c_mch + P.c_qe2);  // extz2 stores s + 2(q+e)
-  const uint32_t mis4 = splat8(D2 ? P.c_mis : P.c_mis + P.c_qe2);
-  const uint32_t N4 = splat8(D2 ? P.c_N : P.c_N + P.c_qe2);
-  const uint32_t m14 = splat8(P.c_m1), maxsc4 = splat8(P.c_maxsc), mchraw4 = splat8(P.c_mch);
-  // score table of the byte-permute lookup: lane index 0 = match, 1-3 = mismatch, 4-7 = N
-  const bool nt4 = P.c_m1 == 4;
-  const uint32_t sc_lo = (mch4 & 0xffu) | (mis4 & 0xffffff00u), sc_hi = N4;
-  const uint32_t initb = D2 ? (uint32_t)(uint8_t)(-P.q - P.e) : 0u;
-  const uint32_t init2b = D2 ? (uint32_t)(uint8_t)(-P.q2 - P.e2) : 0u;
-  const uint32_t init4 = splat8(initb), init24 = splat8(init2b);
-  const uint32_t s_init4 = D2 ? 0u : splat8(P.c_qe2);
+  const ExtConsts C = ext_consts<VAR>(P);
+  const uint32_t initb = C.initb, init2b = C.init2b, init4 = C.init4, init24 = C.init24, s_init4 = C.s_init4;
   // extz2: q+e; extd2: q+e as declared before the swap (ksw2_extd2_sse.c:60,70), used only at r == 0
   const int qe = P.qe_scalar;
   const int ez_e = D2 ? P.e2 : P.e;
@@ -140,7 +311,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
   int32_t hA = 0, hB = 0, last_en0 = 0;  // H[en0] and H[en0 - 1] after the last anti-diagonal
   bool active = false, need = true;
 
-  auto vv = [&](uint32_t byte) -> int32_t { return D2 ? (int32_t)(int8_t)(uint8_t)byte : (int32_t)(byte & 0xffu) - qe; };
+  auto vv = [&](uint32_t byte) -> int32_t { return ext_vv<VAR>(byte, qe); };
 
   for (;;) {
     // ---------------- take the next job ----------------
@@ -275,7 +446,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           // store them).  The scores are first taken by a byte-permute lookup, exact for m = 5
           // (N = 4) when in every lane t | q <= 4; otherwise the thread runs the loop again with
           // the general comparisons (or the matrix), over the same byte masks.
-          uint32_t bad = generic || !nt4 ? 0xffffffffu : 0u;
+          uint32_t bad = generic || !C.nt4 ? 0xffffffffu : 0u;
 #pragma unroll
           for (int i = 0; i <= K; ++i) {
             const int p0 = base + 4 * (k + G * i);
@@ -285,16 +456,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             if (i < K || (p0 + 3 >= st0 && p0 <= fend)) {
               // words of slots 1.. start above st0 (the window starts at st0's 16-cell block)
               const int idx0 = i == 0 ? min(max(r - p0 - 3, r - fend - 3), r - st0) : max(r - p0 - 3, r - fend - 3);
-              const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
-              const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
-              const uint32_t Tw = TW[i];
-              // lanes with t | q <= 4 (codes 0-3, or N = 4 against 0 or N): the lane index
-              // (t ^ q) & 3 | (t | q) & 4 is 0 for a match, 1-3 for a mismatch and 4 for N, and
-              // one byte permute looks it up; any other lane (t | q >= 5) marks the word bad
-              const uint32_t tq = Tw | Qw;
-              const uint32_t ix = ((Tw ^ Qw) & 0x03030303u) | (tq & 0x04040404u);
-              const uint32_t sn = __byte_perm(sc_lo, sc_hi, __byte_perm(ix | (ix >> 4), 0u, 0x4420));
-              bad |= tq | (tq + 0x03030303u);  // bits 3-7 of a lane set iff t | q >= 5
+              const uint32_t sn = score_lookup(TW[i], ld_qword(qp, idx0, qsel), C, bad);
               const uint32_t wm = i == 0 ? lanes_from(st0 - p0) & lanes_upto(fend - p0) : lanes_upto(fend - p0);
               S[i] = (S[i] & ~wm) | (sn & wm);
             }
@@ -304,26 +466,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             for (int i = 0; i <= K; ++i) {
               const int p0 = base + 4 * (k + G * i);
               if (p0 + 3 >= st0 && p0 <= fend) {
-                const int idx0 = r - p0 - 3;
-                const uint32_t *qa = (const uint32_t *)(qp + (idx0 & ~3));
-                const uint32_t Qw = __byte_perm(__ldg(qa), __ldg(qa + 1), qsel);
-                const uint32_t Tw = TW[i];
-                uint32_t sn;
-                if (!generic) {
-                  const uint32_t eq = eqz8(Tw ^ Qw);
-                  const uint32_t nn = eqz8(Tw ^ m14) | eqz8(Qw ^ m14);
-                  sn = sel(bmask(eq), mch4, mis4);
-                  sn = sel(bmask(nn), N4, sn);
-                } else {
-                  sn = 0;
-#pragma unroll
-                  for (int b = 0; b < 4; ++b) {
-                    const int tc = (Tw >> (8 * b)) & 0xff, qc = (Qw >> (8 * b)) & 0xff;
-                    uint32_t v = (uint32_t)(uint8_t)P.mat[(tc * P.m + qc) & 255];
-                    if (!D2) v = (v + P.c_qe2) & 0xffu;
-                    sn |= v << (8 * b);
-                  }
-                }
+                const uint32_t sn = score_exact<VAR>(TW[i], ld_qword(qp, r - p0 - 3, qsel), generic, P, C);
                 const uint32_t wm = lanes_from(st0 - p0) & lanes_upto(fend - p0);
                 S[i] = (S[i] & ~wm) | (sn & wm);
               }
@@ -361,102 +504,8 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           uint32_t xt1 = __byte_perm(rv[i], X[i], 0x6540);  // x[r-1][t-1 .. t+2]
           uint32_t vt1 = __byte_perm(rv[i], V[i], 0x6541);
           if (!D2 && i == 0 && k == 0) xt1 |= extx, vt1 |= extv;
-          const uint32_t ut = U[i];
-          uint32_t z = S[i], a = add8(xt1, vt1), b = add8(Y[i], ut), d = 0;
-          uint32_t nu, nv, nx, ny, nx2 = 0, ny2 = 0;
-          if (!D2) {
-            if (MODE == 0) {
-              z = maxs8(z, a);
-            } else if (MODE == 1) {
-              const uint32_t M = bmask(gts8(a, z));
-              d = M & 0x01010101u;
-              z = sel(M, a, z);
-              d = sel(bmask(gts8(b, z)), 0x02020202u, d);
-            } else {
-              const uint32_t M = bmask(gts8(z, a));
-              d = ~M & 0x01010101u;
-              z = sel(M, z, a);
-              d = sel(bmask(gts8(z, b)), d, 0x02020202u);
-            }
-            z = maxu8(z, b);
-            z = minu8(z, maxsc4);
-            nu = sub8(z, vt1);
-            nv = sub8(z, ut);
-            z = sub8(z, q4);
-            a = sub8(a, z);
-            b = sub8(b, z);
-            if (MODE == 1) {
-              const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi;
-              nx = a & bmask(ga);
-              ny = b & bmask(gb);
-              d |= (ga >> 4) | (gb >> 3);
-            } else {
-              nx = relu8(a);
-              ny = relu8(b);
-              if (MODE == 2) d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3);
-            }
-          } else {
-            const uint32_t x2t1 = __byte_perm(rv[i], X2[i], 0x6542);
-            uint32_t a2 = add8(x2t1, vt1), b2 = add8(Y2[i], ut);
-            if (MODE == 0) {
-              z = maxs8(z, a);
-              z = maxs8(z, b);
-              z = maxs8(z, a2);
-              z = maxs8(z, b2);
-            } else if (MODE == 1) {
-              uint32_t M = bmask(gts8(a, z));
-              d = M & 0x01010101u;
-              z = sel(M, a, z);
-              M = bmask(gts8(b, z));
-              d = sel(M, 0x02020202u, d);
-              z = sel(M, b, z);
-              M = bmask(gts8(a2, z));
-              d = sel(M, 0x03030303u, d);
-              z = sel(M, a2, z);
-              M = bmask(gts8(b2, z));
-              d = sel(M, 0x04040404u, d);
-              z = sel(M, b2, z);
-            } else {
-              uint32_t M = bmask(gts8(z, a));
-              d = ~M & 0x01010101u;
-              z = sel(M, z, a);
-              M = bmask(gts8(z, b));
-              d = sel(M, d, 0x02020202u);
-              z = sel(M, z, b);
-              M = bmask(gts8(z, a2));
-              d = sel(M, d, 0x03030303u);
-              z = sel(M, z, a2);
-              M = bmask(gts8(z, b2));
-              d = sel(M, d, 0x04040404u);
-              z = sel(M, z, b2);
-            }
-            z = mins8(z, mchraw4);
-            nu = sub8(z, vt1);
-            nv = sub8(z, ut);
-            uint32_t tq = sub8(z, q4);
-            a = sub8(a, tq);
-            b = sub8(b, tq);
-            tq = sub8(z, q24);
-            a2 = sub8(a2, tq);
-            b2 = sub8(b2, tq);
-            if (MODE == 1) {
-              const uint32_t ga = gt0s8(a) & kHi, gb = gt0s8(b) & kHi, ga2 = gt0s8(a2) & kHi, gb2 = gt0s8(b2) & kHi;
-              nx = sub8_nn((a & bmask(ga)) | kHi, qe4);
-              ny = sub8_nn((b & bmask(gb)) | kHi, qe4);
-              nx2 = sub8_nn((a2 & bmask(ga2)) | kHi, qe24);
-              ny2 = sub8_nn((b2 & bmask(gb2)) | kHi, qe24);
-              d |= (ga >> 4) | (gb >> 3) | (ga2 >> 2) | (gb2 >> 1);
-            } else {
-              nx = sub8_nn(relu8(a) | kHi, qe4);
-              ny = sub8_nn(relu8(b) | kHi, qe4);
-              nx2 = sub8_nn(relu8(a2) | kHi, qe24);
-              ny2 = sub8_nn(relu8(b2) | kHi, qe24);
-              if (MODE == 2)
-                d |= ((~a & kHi) >> 4) | ((~b & kHi) >> 3) | ((~a2 & kHi) >> 2) | ((~b2 & kHi) >> 1);
-            }
-          }
-          U[i] = nu, V[i] = nv, X[i] = nx, Y[i] = ny;
-          if (D2) X2[i] = nx2, Y2[i] = ny2;
+          const uint32_t x2t1 = D2 ? __byte_perm(rv[i], X2[i], 0x6542) : 0u;
+          const uint32_t d = ext_cell<VAR, MODE>(xt1, vt1, x2t1, S[i], U[i], V[i], X[i], Y[i], X2[i], Y2[i], C);
           if (CIG) row[wi] = d;
         }
         ++n_diag;
@@ -528,7 +577,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
           if (need_mt && lmax == gmax) {
             // cells holding the maximum: one bit per cell of the thread's words (cells past en0
             // never hold it; cells below st0 are masked), then the key of each, usually one
-            const int E = en0 - st0, L4 = E & ~3;
+            const int E = en0 - st0;
             uint32_t mm = 0;
 #pragma unroll
             for (int i = 0; i < K; ++i) {
@@ -541,11 +590,7 @@ ext_dp_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__ or
             while (mm) {
               const int j = __ffs(mm) - 1;
               mm &= mm - 1;
-              const int o = base + 4 * (k + G * (j >> 2)) + (j & 3) - st0;
-              const uint32_t kk = o == E  ? 0u
-                                  : o < L4 ? ((uint32_t)(1 + (o & 3)) << 24) | (uint32_t)o
-                                           : (5u << 24) | (uint32_t)o;
-              key = min(key, kk);
+              key = min(key, max_key(base + 4 * (k + G * (j >> 2)) + (j & 3) - st0, E));
             }
           }
           if (need_mt) key = __reduce_min_sync(gm, key);

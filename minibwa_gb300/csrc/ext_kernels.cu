@@ -1,7 +1,10 @@
 // ext_kernels.cu -- instantiations and launchers of the extension kernels.
 // Compiled once per (VAR) via -DKSW2G_EXT_VAR=0/1 so the two halves build in parallel.
 #include <cuda_runtime.h>
+#include <atomic>
+
 #include "ext_dp.cuh"
+#include "ext_split.cuh"
 #include "launch.h"
 #include "shapes.h"
 
@@ -27,7 +30,14 @@ static const ext_fn kTable[kNumExtShapes][3] = {KSW2G_SHAPES(KSW2G_ROW)};
 #if KSW2G_EXT_VAR == 0
 #define KSW2G_SHAPE(i, G, K) {G, K},
 const ExtShape kExtShapes[kNumExtShapes] = {KSW2G_SHAPES(KSW2G_SHAPE)};
+const SplitShape kSplitShapes[kNumSplitShapes] = {KSW2G_SPLIT_SHAPES(KSW2G_SHAPE)};
 #undef KSW2G_SHAPE
+
+int ext_split_for(int n_col) {
+  for (int i = 0; i < kNumSplitShapes; ++i)
+    if (32 * kSplitShapes[i].NW * kSplitShapes[i].K >= 4 * n_col) return i;
+  return -1;
+}
 
 int ext_shape_for(int n_col) {
   for (int i = 0; i < kNumExtShapes; ++i)
@@ -104,6 +114,51 @@ cudaError_t launch_ext_dp_d2(int mode, int shape, const ksw2g_ext_params &P, con
   if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
   fn<<<blocks, 128, 0, st>>>(L.jobs, L.order, L.n_jobs, L.arena, P, L.res, L.bts, L.tb_pool, L.tb_off,
                              L.job_counter);
+  return cudaGetLastError();
+}
+
+// block-split kernel, one instance per words a thread; the block's warps come from the launch
+static const ext_fn kSplitTable[3][3] = {
+    {ext_split_kernel<KSW2G_EXT_VAR, 0, 1>, ext_split_kernel<KSW2G_EXT_VAR, 1, 1>, ext_split_kernel<KSW2G_EXT_VAR, 2, 1>},
+    {ext_split_kernel<KSW2G_EXT_VAR, 0, 2>, ext_split_kernel<KSW2G_EXT_VAR, 1, 2>, ext_split_kernel<KSW2G_EXT_VAR, 2, 2>},
+    {ext_split_kernel<KSW2G_EXT_VAR, 0, 4>, ext_split_kernel<KSW2G_EXT_VAR, 1, 4>, ext_split_kernel<KSW2G_EXT_VAR, 2, 4>}};
+
+#if KSW2G_EXT_VAR == 0
+cudaError_t launch_ext_split_z2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                                cudaStream_t st)
+#else
+cudaError_t launch_ext_split_d2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                                cudaStream_t st)
+#endif
+{
+  if (L.n_jobs <= 0) return cudaSuccess;
+  if (shape < 0 || shape >= kNumSplitShapes || mode < 0 || mode > 2) return cudaErrorInvalidValue;
+  const int NW = kSplitShapes[shape].NW, K = kSplitShapes[shape].K;
+  const int ki = K == 1 ? 0 : K == 2 ? 1 : 2;
+  if (NW < 1 || NW > kSplitMaxWarps || (K != 1 && K != 2 && K != 4)) return cudaErrorInvalidValue;
+  const ext_fn fn = kSplitTable[ki][mode];
+  // resident blocks per SM of every (shape, mode), and the device's SMs, found once (callers
+  // on several host threads may race here; they store the same values)
+  static std::atomic<int> occ[kNumSplitShapes][3];
+  static std::atomic<int> dev_sms{0};
+  int o = occ[shape][mode].load(std::memory_order_relaxed);
+  if (!o) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, 32 * NW, 0);
+    o = o > 0 ? o : 1;
+    occ[shape][mode].store(o, std::memory_order_relaxed);
+  }
+  int sms = dev_sms.load(std::memory_order_relaxed);
+  if (!sms) {
+    int d = 0;
+    cudaGetDevice(&d);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+    dev_sms.store(sms, std::memory_order_relaxed);
+  }
+  int blocks = L.n_jobs;
+  if (blocks > sms * o) blocks = sms * o;
+  if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
+  fn<<<blocks, 32 * NW, 0, st>>>(L.jobs, L.order, L.n_jobs, L.arena, P, L.res, L.bts, L.tb_pool, L.tb_off,
+                                 L.job_counter);
   return cudaGetLastError();
 }
 

@@ -52,7 +52,20 @@ int64_t ext_wide_scratch(int qlen, int tlen);
 
 // The 16-bit-lane (DPX) kernels of the same (G, K) shapes have the shape ids kExt16Base + s.
 constexpr int kExt16Base = KSW2G_NUM_SHAPES + 1;
-constexpr int kNumShapeIds = 2 * KSW2G_NUM_SHAPES + 1;
+// The block-split kernel's shapes (ext_split.cuh) have the shape ids kSplitBase + s.
+struct SplitShape {
+  int NW, K;
+};
+constexpr int kNumSplitShapes = KSW2G_NUM_SPLIT_SHAPES;
+extern const SplitShape kSplitShapes[kNumSplitShapes];
+constexpr int kSplitBase = 2 * KSW2G_NUM_SHAPES + 1;
+constexpr int kNumShapeIds = kSplitBase + KSW2G_NUM_SPLIT_SHAPES;
+// Smallest split shape able to hold n_col_ blocks, or -1.
+int ext_split_for(int n_col);
+cudaError_t launch_ext_split_z2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                                cudaStream_t st);
+cudaError_t launch_ext_split_d2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
+                                cudaStream_t st);
 cudaError_t launch_ext16_dp_z2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,
                                cudaStream_t st);
 cudaError_t launch_ext16_dp_d2(int mode, int shape, const ksw2g_ext_params &P, const ExtLaunch &L, int max_blocks,

@@ -412,6 +412,7 @@ extern "C" void ksw2g_server_destroy(ksw2g_server_t *S) {
                       &s->batch.counters, &s->batch.llmat, &s->batch.blist, &s->batch.blist_off, &s->batch.wide})
       d->release();
     cudaStreamSynchronize(s->ctx.st);
+    batch_release_streams(&s->batch);
     s->res_pin.release(), s->cig_pin.release(), s->hdr_pin.release();
     cudaStreamDestroy(s->ctx.st);
     delete s;

@@ -11,3 +11,10 @@
   X(0, 4, 3) X(1, 4, 4) X(2, 8, 3) X(3, 8, 4) X(4, 16, 2) X(5, 4, 8) X(6, 16, 3) X(7, 16, 4) X(8, 32, 4) \
   X(9, 32, 5) X(10, 32, 8)
 #define KSW2G_NUM_SHAPES 11
+
+// Block shapes (NW warps x K words a thread) of the block-split kernel (ext_split.cuh), ordered
+// by window words 32*NW*K; the kernel is instantiated once per K and takes NW from the launch.
+#define KSW2G_SPLIT_SHAPES(X)                                                                      \
+  X(0, 2, 1) X(1, 3, 1) X(2, 4, 1) X(3, 5, 1) X(4, 6, 1) X(5, 8, 1) X(6, 10, 1) X(7, 12, 1) X(8, 16, 1) \
+  X(9, 12, 2) X(10, 16, 2) X(11, 12, 4) X(12, 16, 4)
+#define KSW2G_NUM_SPLIT_SHAPES 13

@@ -126,6 +126,8 @@ def load_library():
         "ksw2g_ext_set_shape": (i32, [i32, i32, i32, i32, i32]),
         "ksw2g_ext_set_family": (i32, [i32]),
         "ksw2g_ext_get_family": (i32, []),
+        "ksw2g_ext_set_split": (i32, [i32]),
+        "ksw2g_ext_get_split": (i32, []),
         "ksw2g_debug_fail_device_alloc": (None, [i32]),
         "ksw2g_probe_int32_peak": (i32, [i32, C.POINTER(C.c_double)]),
         "ksw2g_batch_set_timing": (i32, [vp, i32]),
@@ -342,6 +344,15 @@ def set_ext_family(family):
     L = load_library()
     prev = L.ksw2g_ext_get_family()
     _check(L.ksw2g_ext_set_family(int(family)))
+    return prev
+
+
+def set_ext_split(mode):
+    """Block-split kernel use for extension batches prepared from now on: -1 the batch decides,
+    0 never, 1 wherever a block holds the band.  Returns the previous setting."""
+    L = load_library()
+    prev = L.ksw2g_ext_get_split()
+    _check(L.ksw2g_ext_set_split(int(mode)))
     return prev
 
 

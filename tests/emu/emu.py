@@ -43,6 +43,8 @@ def lib():
         vp, i = C.c_void_p, C.c_int
         _L.emu_ext.restype = i
         _L.emu_ext.argtypes = [i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, C.c_longlong, i, i]
+        _L.emu_ext_split.restype = i
+        _L.emu_ext_split.argtypes = [i, i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, C.c_longlong]
         _L.emu_ll.restype = i
         _L.emu_ll.argtypes = [i, i, i, vp, vp, vp, i, i, i, vp, vp, vp, i, i]
         _L.emu_derive_params.restype = None
@@ -93,9 +95,11 @@ def shape_for(nc):
     return -1
 
 
-def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=None, shape=None, family=0):
+def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=None, shape=None, family=0,
+        split=None):
     """Run one batch (one flag/mode for all jobs) through the emulated kernels (family 0: byte
-    lanes, ext_dp_kernel; 1: 16-bit lanes, ext16_dp_kernel).
+    lanes, ext_dp_kernel; 1: 16-bit lanes, ext16_dp_kernel; split=(warps, words a thread): the
+    block-split kernel, ext_split_kernel).
     Returns (EXT_RESULT array, list of CIGAR lists)."""
     L = lib()
     n = len(qs)
@@ -109,6 +113,13 @@ def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=N
     mat = np.ascontiguousarray(mat, np.int8)
     L.emu_derive_params(int(dual), m, mat.ctypes.data, q, e, q2, e2, P.ctypes.data)
     mode = 0 if flag & 1 else (2 if flag & 2 else 1)
+    if split is not None:
+        nw, k = split
+        if any(32 * nw * k < 4 * ncol(len(a), len(b), w) for a, b in zip(qs, ts)):
+            raise ValueError("block too small for the band")
+        run = lambda *a: L.emu_ext_split(int(dual), mode, nw, k, *a)  # noqa: E731
+    else:
+        run = None
     wide = L.emu_num_shapes()  # index of the block-wide kernel
     need = max(shape_for(ncol(len(a), len(b), w)) for a, b in zip(qs, ts))
     if need < 0:
@@ -126,8 +137,13 @@ def ext(dual, m, mat, q, e, q2, e2, qs, ts, w, zdrop, end_bonus, flag, threads=N
     bts = np.zeros(n * 16, np.uint8)
     cap = sum(len(a) + len(b) + 1 for a, b in zip(qs, ts)) + 16
     cig = np.zeros(cap, np.uint32)
-    rc = L.emu_ext(int(dual), mode, shape, P.ctypes.data, n, jobs.ctypes.data, arena.ctypes.data, res.ctypes.data,
-                   bts.ctypes.data, tb.ctypes.data, tb_off.ctypes.data, cig.ctypes.data, cap, threads, family)
+    if run is not None:
+        rc = run(P.ctypes.data, n, jobs.ctypes.data, arena.ctypes.data, res.ctypes.data, bts.ctypes.data,
+                 tb.ctypes.data, tb_off.ctypes.data, cig.ctypes.data, cap)
+    else:
+        rc = L.emu_ext(int(dual), mode, shape, P.ctypes.data, n, jobs.ctypes.data, arena.ctypes.data,
+                       res.ctypes.data, bts.ctypes.data, tb.ctypes.data, tb_off.ctypes.data, cig.ctypes.data, cap,
+                       threads, family)
     if rc != 0:
         raise RuntimeError(f"emu_ext rc={rc}")
     cigars = [cig[r["cigar_off"]:r["cigar_off"] + r["n_cigar"]].tolist() if r["n_cigar"] > 0 else [] for r in res]

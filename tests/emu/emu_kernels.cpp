@@ -19,6 +19,7 @@ LaneState g_lane_state[1024];
 #include "../../minibwa_gb300/csrc/ext_bt.cuh"
 #include "../../minibwa_gb300/csrc/ext_dp.cuh"
 #include "../../minibwa_gb300/csrc/ext16_dp.cuh"
+#include "../../minibwa_gb300/csrc/ext_split.cuh"
 #include "../../minibwa_gb300/csrc/ext_wide.cuh"
 #include "../../minibwa_gb300/csrc/host_common.h"
 #include "../../minibwa_gb300/csrc/ll.cuh"
@@ -112,6 +113,37 @@ int emu_ext(int dual, int mode, int shape, const ksw2g_ext_params *P, int n, con
     const ext_fn f = family ? kTab16[shape][dual][mode] : kTab[shape][dual][mode];
     run_block(threads, [&] { f(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter); });
   }
+  if (mode != 0) {
+    unsigned long long cursor = 0;
+    int err = 0;
+    blockDim.x = 1;
+    for (int j = 0; j < n; ++j) {
+      threadIdx.x = 0;
+      blockIdx.x = j;
+      ext_bt_kernel(jobs, nullptr, n, bts, tb_pool, tb_off, res, cigar, &cursor, cap, &err);
+    }
+    if (err) return -2;
+  }
+  return 0;
+}
+
+// The block-split kernel (ext_split.cuh) with one emulated block of 32*nw threads, k words a
+// thread, then the backtrack kernel.
+int emu_ext_split(int dual, int mode, int nw, int k, const ksw2g_ext_params *P, int n, const ksw2g_job *jobs,
+                  const uint8_t *arena, ksw2g_ext_result *res, ksw2g_bt *bts, uint8_t *tb_pool,
+                  const int64_t *tb_off, uint32_t *cigar, long long cap) {
+  if (nw < 1 || nw > kSplitMaxWarps || (k != 1 && k != 2 && k != 4) || mode < 0 || mode > 2) return -1;
+  static const ext_fn tab[2][3][3] = {
+      {{ext_split_kernel<0, 0, 1>, ext_split_kernel<0, 1, 1>, ext_split_kernel<0, 2, 1>},
+       {ext_split_kernel<0, 0, 2>, ext_split_kernel<0, 1, 2>, ext_split_kernel<0, 2, 2>},
+       {ext_split_kernel<0, 0, 4>, ext_split_kernel<0, 1, 4>, ext_split_kernel<0, 2, 4>}},
+      {{ext_split_kernel<1, 0, 1>, ext_split_kernel<1, 1, 1>, ext_split_kernel<1, 2, 1>},
+       {ext_split_kernel<1, 0, 2>, ext_split_kernel<1, 1, 2>, ext_split_kernel<1, 2, 2>},
+       {ext_split_kernel<1, 0, 4>, ext_split_kernel<1, 1, 4>, ext_split_kernel<1, 2, 4>}}};
+  const ext_fn f = tab[dual ? 1 : 0][k == 1 ? 0 : k == 2 ? 1 : 2][mode];
+  int counter = 0;
+  const ksw2g_ext_params Pc = *P;
+  run_block(32 * nw, [&] { f(jobs, nullptr, n, arena, Pc, res, bts, tb_pool, tb_off, &counter); });
   if (mode != 0) {
     unsigned long long cursor = 0;
     int err = 0;

@@ -224,3 +224,76 @@ def test_emulated_ungap_kernel(emu, global_hist):
     got = emu.ungap(pairs, meth, global_hist)
     for i, ((q, t), mt) in enumerate(zip(pairs, meth)):
         assert got[i] == O.ungap(q, t, 7, mt), i
+
+
+SPLIT_SHAPES = ((1, 1), (2, 1), (3, 1), (1, 2), (2, 2), (1, 4))
+
+
+def test_emulated_split_kernel_matches_golden(emu, golden):
+    """The block-split kernel (ext_split.cuh) on the golden cases, every sixth one, in every block
+    shape of up to three warps that holds the band."""
+    cases = list(golden_ext_cases(golden))
+    for i, c in enumerate(cases[2::6]):
+        nc = emu.ncol(len(c["query"]), len(c["target"]), c["w"])
+        for nw, k in SPLIT_SHAPES:
+            if 32 * nw * k < 4 * nc:
+                continue
+            res, cig = emu.ext(c["dual"], c["m"], c["mat"], c["q"], c["e"], c["q2"], c["e2"], [c["query"]],
+                               [c["target"]], c["w"], c["zdrop"], c["end_bonus"], c["flag"], split=(nw, k))
+            got = {f: int(res[0][f]) for f in EXT_FIELDS}
+            assert got == c["out"], (i, nw, k, got, c["out"])
+            assert cig[0] == c["cigar"], (i, nw, k)
+
+
+def test_emulated_split_kernel_long_pairs(emu):
+    """Pairs long enough for the window to slide many times across warp boundaries, with junk
+    tails that z-drop, in both variants, every traceback mode and the approximate max, against
+    the oracle; several pairs per block take jobs one after another."""
+    from minibwa_gb300 import synth
+    from oracle import oracle as O
+    p = synth.config1(6, seed=41)
+    qs = [p.query(i) for i in range(len(p))]
+    ts = [p.target(i) for i in range(len(p))]
+    for dual, flag, w, split in ((1, 0x40, 100, (2, 1)), (1, 0x42, 60, (1, 2)), (0, 0x00, 90, (3, 1)),
+                                 (0, 0x41, 120, (2, 2)), (1, 0x18, 80, (2, 1)), (0, 0x58, 100, (1, 4)),
+                                 (1, 0xc0, 200, (4, 1)), (0, 0x44, 100, (2, 1))):
+        q2, e2 = (24, 1) if dual else (12, 2)
+        res, cig = emu.ext(dual, 5, p.mat, 12, 2, q2, e2, qs, ts, w, 100, 10, flag, split=split)
+        for i in range(len(qs)):
+            exp, _ = O.extz(dual, qs[i], ts[i], 5, p.mat, 12, 2, q2, e2, w, 100, 10, flag)
+            assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, w, i)
+            assert cig[i] == exp["cigar"], (dual, flag, w, i)
+
+
+def test_emulated_split_kernel_edges(emu):
+    """One-cell bands, codes above N (the general score path) and empty sequences on the
+    block-split kernel."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(31)
+    mat = np.array([3 if i // 5 == i % 5 else -4 for i in range(25)], np.int8)
+    mat[20:25] = -1
+    mat[4::5] = -1
+    qs = [rng.integers(0, 4, 46).astype(np.uint8) for _ in range(4)]
+    ts = [q[:tl].copy() for q, tl in zip(qs, (1, 2, 3, 5))]
+    for dual in (0, 1):
+        for flag in (0x00, 0x01, 0x40, 0x42):
+            for w in (2, 6):
+                res, cig = emu.ext(dual, 5, mat, 3, 1, 20, 1, qs, ts, w, -1, 5, flag, split=(2, 1))
+                for i in range(len(qs)):
+                    exp, _ = O.extz(dual, qs[i], ts[i], 5, mat, 3, 1, 20 if dual else 3, 1, w, -1, 5, flag)
+                    assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, w)
+                    assert cig[i] == exp["cigar"], (dual, flag, w, i)
+    qs, ts = [], []
+    for _ in range(6):
+        base = rng.integers(0, 4, 160).astype(np.uint8)
+        q, t = base[: int(rng.integers(60, 160))].copy(), base[: int(rng.integers(60, 160))].copy()
+        q[rng.random(len(q)) < 0.1] = rng.integers(4, 8)
+        t[rng.random(len(t)) < 0.05] = rng.integers(4, 8)
+        qs.append(q), ts.append(t)
+    qs.append(np.zeros(0, np.uint8)), ts.append(rng.integers(0, 4, 30).astype(np.uint8))
+    for dual, flag in ((0, 0x42), (1, 0x40), (1, 0x01)):
+        res, cig = emu.ext(dual, 5, mat, 6, 1, 20, 1, qs, ts, 40, 100, 5, flag, split=(2, 1))
+        for i in range(len(qs)):
+            exp, _ = O.extz(dual, qs[i], ts[i], 5, mat, 6, 1, 20 if dual else 6, 1, 40, 100, 5, flag)
+            assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, i)
+            assert cig[i] == exp["cigar"], (dual, flag, i)
