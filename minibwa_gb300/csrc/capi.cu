@@ -53,20 +53,23 @@ static std::mutex g_pref_mu;
 static std::atomic<int> g_family{-1};
 // block-split kernel (ksw2g_ext_set_split): -1 the batch decides, 0 never, 1 wherever a split
 // shape holds the band
-static std::atomic<int> g_split{0};
-// A batch runs its jobs of one (mode, shape) on the block-split kernel when they number at most
-// kSplitMaxJobs and their bands are wider than kSplitMinCol 16-cell blocks.  A thread group
-// computes a pair's anti-diagonals one after another (one 10 kb extd2 pair at w=500 takes
-// 1.42 us per anti-diagonal on a GB300, the same with up to 608 such pairs at once), so a
-// batch of few long pairs lasts as long as its longest pair on one group; a block splits
-// each anti-diagonal over its warps.
-static const int kSplitMinCol = 16;
+static std::atomic<int> g_split{-1};
+// Which jobs a batch runs on the block-split kernel.  Bands wider than every thread-group shape
+// always do: one 10 kb extd2 pair at w=1100 takes 1.46 us per anti-diagonal there against 3.75
+// on the block-wide kernel (ext_wide.cuh), and 608 such pairs 6.0 against 8.9 us.  The jobs of
+// a thread-group (mode, shape) class do when they number at most kSplitMaxJobs and their
+// bands span at least kSplitMinCol 16-cell blocks: a group computes a pair's anti-diagonals
+// one after another (1.41 us each at w=100 and at w=500, the same with up to 608 such pairs at
+// once), so a batch of few long pairs lasts as long as its longest pair on one group, while a
+// block takes 1.01 us at w=100 and 1.22 us at w=500.  With more pairs the groups' throughput
+// wins (608 pairs at w=500: 1.42 us on groups, 2.67 on blocks).
+static const int kSplitMinCol = 8;
 static const int kSplitMaxJobs = 304;
 
-static bool use_split(int n_col, int count) {
+static bool use_split(int n_col, int count, bool wide) {
   const int m = g_split.load(std::memory_order_relaxed);
   if (m == 0 || ext_split_for(n_col) < 0) return false;
-  return m == 1 || (n_col > kSplitMinCol && count <= kSplitMaxJobs);
+  return m == 1 || wide || (n_col >= kSplitMinCol && count <= kSplitMaxJobs);
 }
 
 static bool shape_holds(int s, int n_col) {
@@ -345,16 +348,21 @@ int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
 }
 
 // Rough device time of a bin in cycles, to spread the bins of a wave over streams: its
-// longest pair's anti-diagonals at one group's latency plus all its anti-diagonal words
-// at the whole device's rate.  Measured on a GB300: one 10 kb extd2 pair at w=500 alone
-// takes about 2,200 + 140 K cycles per anti-diagonal on a group of K words a thread, and
-// the block-wide kernel about 8,000; 1,000,000 config-1 pairs run at about 0.02 cycles per
-// anti-diagonal word.
+// longest pair's anti-diagonals at one pair's latency plus all its anti-diagonal words at the
+// whole device's rate.  Measured on a GB300 with one 10 kb extd2 pair: about 2,200 + 140 K
+// cycles per anti-diagonal on a group of K words a thread, 1,900 + 110 NW K on a block of NW
+// warps, 8,000 on the block-wide kernel; 1,000,000 config-1 pairs run at about 0.02 cycles per
+// anti-diagonal word on groups, and blocks take about three times the groups' device time per
+// word.
 static double bin_cost(int shape, int64_t max_diag, double diag_words) {
-  double lat = 8000.0;
-  if (shape >= kSplitBase) lat = 1000.0;  // to be measured
-  else if (shape != kWideShape) lat = 2200.0 + 140.0 * kExtShapes[shape >= kExt16Base ? shape - kExt16Base : shape].K;
-  return (double)max_diag * lat + 0.02 * diag_words;
+  double lat = 8000.0, per_word = 0.06;
+  if (shape >= kSplitBase) {
+    const SplitShape &b = kSplitShapes[shape - kSplitBase];
+    lat = 1900.0 + 110.0 * b.NW * b.K;
+  } else if (shape != kWideShape) {
+    lat = 2200.0 + 140.0 * kExtShapes[shape >= kExt16Base ? shape - kExt16Base : shape].K, per_word = 0.02;
+  }
+  return (double)max_diag * lat + per_word * diag_words;
 }
 // Assign the bins of a wave to its streams, costliest first, each to the stream with the least
 // cost so far (the longest-processing-time rule), and order them that way for launching.  The
@@ -425,7 +433,8 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     std::vector<int> cnt(3 * kNumShapeIds, 0);
     for (int i = 0; i < n; ++i) ++cnt[mode[i] * kNumShapeIds + shape[i]];
     for (int i = 0; i < n; ++i)
-      if (jobs[i].qlen > 0 && jobs[i].tlen > 0 && use_split(ncol[i], cnt[mode[i] * kNumShapeIds + shape[i]]))
+      if (jobs[i].qlen > 0 && jobs[i].tlen > 0 &&
+          use_split(ncol[i], cnt[mode[i] * kNumShapeIds + shape[i]], shape[i] == kWideShape))
         shape[i] = kSplitBase + ext_split_for(ncol[i]);
   }
   for (int i = 0; i < n; ++i)
@@ -989,7 +998,7 @@ static void ext_one(void *km, int dual, int qlen, const uint8_t *query, int tlen
   const int mode = ext_mode(flag);
   const int nc = ext_ncol(qlen, tlen, w);
   int shape = ext_shape_id(dual, mode, nc, P);
-  if (use_split(nc, 1)) shape = kSplitBase + ext_split_for(nc);
+  if (use_split(nc, 1, shape == kWideShape)) shape = kSplitBase + ext_split_for(nc);
   const int64_t ncig = mode ? (int64_t)qlen + tlen + 1 : 0;
   const int64_t foot = mode ? (int64_t)(qlen + tlen - 1) * nc * 16 : 0;
   const size_t o_job = 32, o_tbo = o_job + 48, o_bt = o_tbo + 16, o_res = o_bt + 16;
