@@ -685,7 +685,7 @@ def _timed_run(cmd, cwd, env=None):
     return out, dt, (r1.ru_utime - r0.ru_utime) + (r1.ru_stime - r0.ru_stime)
 
 
-def mapper_point(n_pairs=100_000, n_long=1000):
+def mapper_point(n_pairs=100_000, n_long=16_000):
     """The batched minibwa (minibwa_gb300/mapper) against the stock build of the same reference
     sources on the same simulated reads, both with all host threads: reads mapped per second of
     wall time and the host CPU time each spent, whether their SAM outputs are byte-identical, and

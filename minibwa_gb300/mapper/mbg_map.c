@@ -89,6 +89,37 @@ static void mbg_gpu_init(const mb_idx_t *idx);
 static pthread_t g_init_tid;
 static int g_init_running;
 
+// Bringing up the CUDA context takes about 0.1 s.  A map run starts it when the program starts,
+// on a thread of its own, so that it overlaps the loading of the index and of the first reads;
+// mbg_gpu_init waits for it and reports its failure.
+static pthread_t g_ctx_tid;
+static int g_ctx_running, g_ctx_rc;
+static char g_ctx_err[512];
+static double g_t_start, g_t_ctx;  // program start; the context's creation time
+
+static void *mbg_ctx_thread(void *unused)
+{
+	const char *dev = getenv("MBG_DEVICE");
+	double t0 = mbg_ms();
+	(void)unused;
+	if ((g_ctx_rc = ksw2g_ctx_create(dev? atoi(dev) : 0, &g_ctx)) != 0)
+		snprintf(g_ctx_err, sizeof(g_ctx_err), "%s", ksw2g_last_error());
+	g_t_ctx = mbg_ms() - t0;
+	return 0;
+}
+
+__attribute__((constructor)) static void mbg_ctx_early(int argc, char **argv)
+{ // glibc passes the program's arguments to constructors
+	g_t_start = mbg_ms();
+	if (argc > 1 && argv && argv[1] && strcmp(argv[1], "map") == 0)
+		g_ctx_running = pthread_create(&g_ctx_tid, 0, mbg_ctx_thread, 0) == 0;
+}
+
+static void mbg_exit_timing(void)
+{ // registered after the CUDA runtime's own exit handler, so it runs before the runtime's teardown
+	fprintf(stderr, "[M::mbg] exit begins %.1f ms after the program started\n", mbg_ms() - g_t_start);
+}
+
 static void *mbg_gpu_init_thread(void *idx)
 {
 	mbg_gpu_init((const mb_idx_t*)idx);
@@ -174,6 +205,11 @@ static void mbg_gpu_init(const mb_idx_t *idx)
 	const l2b_t *l = idx->l2b;
 	uint64_t *off, *len, k;
 	const char *dev = getenv("MBG_DEVICE");
+	if (g_ctx_running) pthread_join(g_ctx_tid, 0), g_ctx_running = 0;
+	if (g_ctx_rc) {
+		fprintf(stderr, "[E::%s] ksw2g_ctx_create: %s\n", __func__, g_ctx_err);
+		exit(1);
+	}
 	if (g_ctx && g_l2b == l) return;
 	if (!g_ctx && ksw2g_ctx_create(dev? atoi(dev) : 0, &g_ctx)) mbg_fail("ksw2g_ctx_create");
 	if (g_ref) ksw2g_ref_destroy(g_ref);
@@ -182,6 +218,11 @@ static void mbg_gpu_init(const mb_idx_t *idx)
 	if (ksw2g_ref_create(g_ctx, l->n_ctg, off, len, l->pac, l->n_pac, l->n_ambi, (const uint64_t*)l->ambi, &g_ref))
 		mbg_fail("ksw2g_ref_create");
 	free(off), free(len);
+	if (!g_l2b && getenv("MBG_TIMING")) {
+		fprintf(stderr, "[M::mbg] CUDA context created in %.1f ms; reference resident %.1f ms after the program started\n",
+				g_t_ctx, mbg_ms() - g_t_start);
+		atexit(mbg_exit_timing);
+	}
 	g_l2b = l;
 }
 
