@@ -55,13 +55,13 @@ static std::atomic<int> g_family{-1};
 // shape holds the band
 static std::atomic<int> g_split{-1};
 // Which jobs a batch runs on the block-split kernel.  Bands wider than every thread-group shape
-// always do: one 10 kb extd2 pair at w=1100 takes 1.46 us per anti-diagonal there against 3.75
+// always do: one 10 kb extd2 pair at w=1100 takes 1.25 us per anti-diagonal there against 3.75
 // on the block-wide kernel (ext_wide.cuh), and 608 such pairs 6.0 against 8.9 us.  The jobs of
 // a thread-group (mode, shape) class do when they number at most kSplitMaxJobs and their
 // bands span at least kSplitMinCol 16-cell blocks: a group computes a pair's anti-diagonals
 // one after another (1.41 us each at w=100 and at w=500, the same with up to 608 such pairs at
 // once), so a batch of few long pairs lasts as long as its longest pair on one group, while a
-// block takes 1.01 us at w=100 and 1.22 us at w=500.  With more pairs the groups' throughput
+// block takes 0.95 us at w=100 and 1.00 us at w=500.  With more pairs the groups' throughput
 // wins (608 pairs at w=500: 1.42 us on groups, 2.67 on blocks).
 static const int kSplitMinCol = 8;
 static const int kSplitMaxJobs = 304;
@@ -350,7 +350,7 @@ int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
 // Rough device time of a bin in cycles, to spread the bins of a wave over streams: its
 // longest pair's anti-diagonals at one pair's latency plus all its anti-diagonal words at the
 // whole device's rate.  Measured on a GB300 with one 10 kb extd2 pair: about 2,200 + 140 K
-// cycles per anti-diagonal on a group of K words a thread, 1,900 + 110 NW K on a block of NW
+// cycles per anti-diagonal on a group of K words a thread, 1,750 + 85 NW K on a block of NW
 // warps, 8,000 on the block-wide kernel; 1,000,000 config-1 pairs run at about 0.02 cycles per
 // anti-diagonal word on groups, and blocks take about three times the groups' device time per
 // word.
@@ -358,7 +358,7 @@ static double bin_cost(int shape, int64_t max_diag, double diag_words) {
   double lat = 8000.0, per_word = 0.06;
   if (shape >= kSplitBase) {
     const SplitShape &b = kSplitShapes[shape - kSplitBase];
-    lat = 1900.0 + 110.0 * b.NW * b.K;
+    lat = 1750.0 + 85.0 * b.NW * b.K;
   } else if (shape != kWideShape) {
     lat = 2200.0 + 140.0 * kExtShapes[shape >= kExt16Base ? shape - kExt16Base : shape].K, per_word = 0.02;
   }

@@ -146,17 +146,49 @@ ext_split_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__
     }
 #pragma unroll
     for (int i = 0; i <= K; ++i) S[i] = s_init4, TW[i] = ld_tw(tp, 4 * (k + NT * i), tlen);
+    // band [s0, e0] of anti-diagonal rr (ksw2_extz2_sse.c:99-102)
+    auto band = [&](int rr, int &s0, int &e0) {
+      s0 = rr - qlen + 1 > 0 ? rr - qlen + 1 : 0;
+      e0 = rr < tlen - 1 ? rr : tlen - 1;
+      const int a = (rr - w + 1) >> 1, b = (rr + w) >> 1;
+      if (s0 < a) s0 = a;
+      if (e0 > b) e0 = b;
+    };
+    // substitution scores of anti-diagonal rr written by the reference's 16-byte stores from s0
+    // (ksw2_extz2_sse.c:117-136), into the window with base bs
+    auto scores = [&](int rr, int s0, int e0, int bs) {
+      const bool generic = flag & KSW2G_GENERIC_SC;
+      const int fend = generic ? e0 : s0 + (((e0 - s0) >> 4) << 4) + 15;
+      const int o = (rr + 1) & 3;
+      const uint32_t qsel = (uint32_t)((o + 3) | ((o + 2) << 4) | ((o + 1) << 8) | (o << 12));
+      uint32_t bad = generic || !C.nt4 ? 0xffffffffu : 0u;
+#pragma unroll
+      for (int i = 0; i <= K; ++i) {
+        const int p0 = bs + 4 * (k + NT * i);
+        if (p0 + 3 >= s0 && p0 <= fend) {
+          const uint32_t sn = score_lookup(TW[i], ld_qword(qp, rr - p0 - 3, qsel), C, bad);
+          const uint32_t wm = lanes_from(s0 - p0) & lanes_upto(fend - p0);
+          S[i] = (S[i] & ~wm) | (sn & wm);
+        }
+      }
+      if (bad & 0xf8f8f8f8u) {
+#pragma unroll
+        for (int i = 0; i <= K; ++i) {
+          const int p0 = bs + 4 * (k + NT * i);
+          if (p0 + 3 >= s0 && p0 <= fend) {
+            const uint32_t sn = score_exact<VAR>(TW[i], ld_qword(qp, rr - p0 - 3, qsel), generic, P, C);
+            const uint32_t wm = lanes_from(s0 - p0) & lanes_upto(fend - p0);
+            S[i] = (S[i] & ~wm) | (sn & wm);
+          }
+        }
+      }
+    };
 
     // ---------------- anti-diagonals ----------------
     for (bool done = false; !done;) {
       const int p = r & 1;
-      int st0 = r - qlen + 1 > 0 ? r - qlen + 1 : 0;
-      int en0 = r < tlen - 1 ? r : tlen - 1;
-      {
-        const int a = (r - w + 1) >> 1, b = (r + w) >> 1;
-        if (st0 < a) st0 = a;
-        if (en0 > b) en0 = b;
-      }
+      int st0, en0;
+      band(r, st0, en0);
       if (st0 > en0) {  // ksw2_extz2_sse.c:103-106
         zdropped = 1;
         break;
@@ -233,34 +265,7 @@ ext_split_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__
           if (D2) Y2[i] = e ? (Y2[i] & keep) | (init2b << sh) : Y2[i];
         }
       }
-      // ---- substitution scores written by the 16-byte stores from st0 (ksw2_extz2_sse.c:117-136) ----
-      {
-        const bool generic = flag & KSW2G_GENERIC_SC;
-        const int fend = generic ? en0 : st0 + (((en0 - st0) >> 4) << 4) + 15;
-        const int o = (r + 1) & 3;
-        const uint32_t qsel = (uint32_t)((o + 3) | ((o + 2) << 4) | ((o + 1) << 8) | (o << 12));
-        uint32_t bad = generic || !C.nt4 ? 0xffffffffu : 0u;
-#pragma unroll
-        for (int i = 0; i <= K; ++i) {
-          const int p0 = base + 4 * (k + NT * i);
-          if (p0 + 3 >= st0 && p0 <= fend) {
-            const uint32_t sn = score_lookup(TW[i], ld_qword(qp, r - p0 - 3, qsel), C, bad);
-            const uint32_t wm = lanes_from(st0 - p0) & lanes_upto(fend - p0);
-            S[i] = (S[i] & ~wm) | (sn & wm);
-          }
-        }
-        if (bad & 0xf8f8f8f8u) {
-#pragma unroll
-          for (int i = 0; i <= K; ++i) {
-            const int p0 = base + 4 * (k + NT * i);
-            if (p0 + 3 >= st0 && p0 <= fend) {
-              const uint32_t sn = score_exact<VAR>(TW[i], ld_qword(qp, r - p0 - 3, qsel), generic, P, C);
-              const uint32_t wm = lanes_from(st0 - p0) & lanes_upto(fend - p0);
-              S[i] = (S[i] & ~wm) | (sn & wm);
-            }
-          }
-        }
-      }
+      scores(r, st0, en0, base);
       // ---- cells st..en of the anti-diagonal (ksw2_extz2_sse.c:142-215, ksw2_extd2_sse.c:183-314) ----
       const int nlive = (enb - wb + 1) << 2;
       const uint32_t extx = (!D2 && (x1 & 0x80)) ? 0xffffff00u : 0u;  // sign-extended _mm_cvtsi32_si128
@@ -347,6 +352,24 @@ ext_split_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__
           const int ps = st0 - base, bsel = ps & 3;
           if (k == (ps >> 2)) xs.pub[p][2] = bsel == 0 ? H0[0] : bsel == 1 ? H1[0] : bsel == 2 ? H2[0] : H3[0];
         }
+        if (K == 1) {
+          // One word a thread: every thread finds the key of its own maximum without a branch,
+          // and two warp reductions of the packed (H, key) give the warp's; the cells holding
+          // the warp's maximum are those at their thread's maximum where it equals the warp's.
+          const int E = en0 - st0, L4 = E & ~3, o0 = base + 4 * k - st0;
+          uint32_t lkey = 0xffffffffu;
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int32_t h = b == 0 ? H0[0] : b == 1 ? H1[0] : b == 2 ? H2[0] : H3[0];
+            const int o = o0 + b;
+            const uint32_t kk = o == E ? 0u : o < L4 ? ((uint32_t)(1 + (o & 3)) << 24) | (uint32_t)o : (5u << 24) | (uint32_t)o;
+            lkey = h == lmax && b >= lo ? min(lkey, kk) : lkey;
+          }
+          const uint32_t hi = (uint32_t)lmax ^ 0x80000000u, lw = 0xffffffffu - lkey;
+          const uint32_t mh = __reduce_max_sync(full, hi);
+          const uint32_t ml = __reduce_max_sync(full, hi == mh ? lw : 0u);
+          if (lane == 0) xs.wmk[p][wp] = ((uint64_t)mh << 32) | ml;
+        } else {
         const int32_t wmax = __reduce_max_sync(full, lmax);
         // The key is wanted only where the block's maximum may set a new maximum or z-drop
         // (ksw_apply_zdrop, ksw2.h:181-197); a warp whose own maximum rules both out cannot
@@ -374,6 +397,7 @@ ext_split_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__
           key = __reduce_min_sync(full, key);
         }
         if (lane == 0) xs.wmk[p][wp] = split_pack(wmax, key);
+        }
       } else {
         // ---- approximate max: the followed cell's v and u (ksw2_extz2_sse.c:262-278) ----
         const int ta = r == 0 ? 0 : last_H0_t, tbb = last_H0_t + 1;
@@ -389,8 +413,13 @@ ext_split_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__
       __syncthreads();
       // ---- the same decisions in every thread (ksw2_extz2_sse.c:216-278, ksw2_extd2_sse.c:315-385) ----
       if (!approx) {
-        uint64_t best = xs.wmk[p][0];
-        for (int u = 1; u < NW; ++u) best = max(best, xs.wmk[p][u]);
+        uint64_t best;
+        {  // the warps' packed maxima, reduced across the lanes of every warp at once
+          const uint64_t e = lane < NW ? xs.wmk[p][lane] : 0ull;
+          const uint32_t hi = (uint32_t)(e >> 32), lw = (uint32_t)e;
+          const uint32_t mh = __reduce_max_sync(full, hi);
+          best = ((uint64_t)mh << 32) | __reduce_max_sync(full, hi == mh ? lw : 0u);
+        }
         const int32_t max_H = (int32_t)((uint32_t)(best >> 32) ^ 0x80000000u);
         const uint32_t key = 0xffffffffu - (uint32_t)best;
         const int32_t Hen0 = xs.pub[p][0];
