@@ -62,7 +62,7 @@ static std::atomic<int> g_split{-1};
 // one after another (1.41 us each at w=100 and at w=500, the same with up to 608 such pairs at
 // once), so a batch of few long pairs lasts as long as its longest pair on one group, while a
 // block takes 0.95 us at w=100 and 1.00 us at w=500.  With more pairs the groups' throughput
-// wins (608 pairs at w=500: 1.42 us on groups, 2.67 on blocks).
+// wins (608 pairs at w=500: 1.42 us on groups, 2.25 on blocks).
 static const int kSplitMinCol = 8;
 static const int kSplitMaxJobs = 304;
 
