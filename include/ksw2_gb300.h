@@ -297,8 +297,8 @@ int ksw2g_ext_set_family(int family);
 int ksw2g_ext_get_family(void);
 /* Use of the block-split kernel for extension batches prepared after the call: -1 (default)
  * the batch decides (a block per pair for the jobs of a band class that are few and wide),
- * 0 never, 1 for every job whose band a block holds.  Process-wide.  Returns 0 or
- * KSW2G_E_ARG. */
+ * 0 never, 1 for every job whose band a block holds.  Process-wide; the environment variable
+ * KSW2G_SPLIT (-1, 0 or 1) sets the value a process starts with.  Returns 0 or KSW2G_E_ARG. */
 int ksw2g_ext_set_split(int mode);
 int ksw2g_ext_get_split(void);
 

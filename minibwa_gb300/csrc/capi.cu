@@ -52,18 +52,23 @@ static std::mutex g_pref_mu;
 // lane width forced on every batch: -1 none (preferences decide), 0 bytes, 1 16-bit halves
 static std::atomic<int> g_family{-1};
 // block-split kernel (ksw2g_ext_set_split): -1 the batch decides, 0 never, 1 wherever a split
-// shape holds the band
-static std::atomic<int> g_split{-1};
+// shape holds the band; the environment variable KSW2G_SPLIT sets the initial value
+static int split_from_env() {
+  const char *v = getenv("KSW2G_SPLIT");
+  const int m = v && *v ? atoi(v) : -1;
+  return m >= -1 && m <= 1 ? m : -1;
+}
+static std::atomic<int> g_split{split_from_env()};
 // Which jobs a batch runs on the block-split kernel.  Bands wider than every thread-group shape
 // always do: one 10 kb extd2 pair at w=1100 takes 1.25 us per anti-diagonal there against 3.75
 // on the block-wide kernel (ext_wide.cuh), and 608 such pairs 6.0 against 8.9 us.  The jobs of
 // a thread-group (mode, shape) class do when they number at most kSplitMaxJobs and their
-// bands span at least kSplitMinCol 16-cell blocks: a group computes a pair's anti-diagonals
+// bands span at least kSplitMinCol 16-cell blocks (w above about 250): a group computes a pair's anti-diagonals
 // one after another (1.41 us each at w=100 and at w=500, the same with up to 608 such pairs at
 // once), so a batch of few long pairs lasts as long as its longest pair on one group, while a
 // block takes 0.95 us at w=100 and 1.00 us at w=500.  With more pairs the groups' throughput
 // wins (608 pairs at w=500: 1.42 us on groups, 2.25 on blocks).
-static const int kSplitMinCol = 8;
+static const int kSplitMinCol = 17;
 static const int kSplitMaxJobs = 304;
 
 static bool use_split(int n_col, int count, bool wide) {
