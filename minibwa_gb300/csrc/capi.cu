@@ -17,6 +17,7 @@
 #include "launch.h"
 #include "host_common.h"
 #include "batch.h"
+#include "host_parallel.h"
 
 static_assert(sizeof(ksw2g_job_t) == sizeof(ksw2g_job), "job layout");
 static_assert(sizeof(ksw2g_ext_result_t) == sizeof(ksw2g_ext_result), "result layout");
@@ -411,28 +412,54 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   std::vector<int> shape(n), mode(n), ncol(n);
   std::vector<int64_t> foot(n);
   int64_t cig = 0, wide_max = 0;
-  double band_cells = 0;  // sum of (qlen + tlen) x band width: the batch's size class
+  int64_t band_cells = 0;  // sum of (qlen + tlen) x band width: the batch's size class
   int n_wide = 0;
-  for (int i = 0; i < n; ++i) {
-    const ksw2g_job_t &J = jobs[i];
-    if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
-        (!rt && J.toff + J.tlen > tbuf_len))
-      return set_err(KSW2G_E_ARG, "job %d: sequence out of buffer bounds", i);
-    if (rt && ref_check_window(rt->ref, rt->tid[i], J.toff, J.tlen)) return KSW2G_E_ARG;
-    if ((J.flag & KSW_EZ_GENERIC_SC) && m > 16)
-      return set_err(KSW2G_E_UNSUPPORTED, "job %d: GENERIC_SC needs m <= 16 on the device (m=%d)", i, m);
-    qo[i] = J.qoff, to[i] = J.toff, ql[i] = J.qlen, tl[i] = J.tlen;
-    mode[i] = ext_mode(J.flag);
-    const bool live = J.qlen > 0 && J.tlen > 0 && !b->P.skip_all;
-    const int nc = live ? ext_ncol(J.qlen, J.tlen, J.w) : 1;
-    shape[i] = ext_shape_id(dual, mode[i], nc, b->P);
-    ncol[i] = nc;
-    foot[i] = (live && mode[i] != 0) ? (((int64_t)(J.qlen + J.tlen - 1) * nc * 16 + 15) & ~(int64_t)15) : 0;
-    if (foot[i] > c->tb_budget)
-      return set_err(KSW2G_E_CAPACITY, "job %d: traceback needs %lld bytes, budget %lld", i, (long long)foot[i],
-                     (long long)c->tb_budget);
-    if (mode[i] != 0) cig += J.qlen + J.tlen + 1;
-    band_cells += (double)(J.qlen + J.tlen) * (nc > 1 ? 16.0 * (nc - 1) : 0.0);
+  {
+    // One job's checks and plan; returns nonzero at the first failing check, with the error
+    // set on the calling thread.
+    auto plan = [&](int i, int64_t &cg, int64_t &bc) -> int {
+      const ksw2g_job_t &J = jobs[i];
+      if (J.qlen < 0 || J.tlen < 0 || J.qoff < 0 || J.toff < 0 || J.qoff + J.qlen > qbuf_len ||
+          (!rt && J.toff + J.tlen > tbuf_len))
+        return set_err(KSW2G_E_ARG, "job %d: sequence out of buffer bounds", i);
+      if (rt && ref_check_window(rt->ref, rt->tid[i], J.toff, J.tlen)) return KSW2G_E_ARG;
+      if ((J.flag & KSW_EZ_GENERIC_SC) && m > 16)
+        return set_err(KSW2G_E_UNSUPPORTED, "job %d: GENERIC_SC needs m <= 16 on the device (m=%d)", i, m);
+      qo[i] = J.qoff, to[i] = J.toff, ql[i] = J.qlen, tl[i] = J.tlen;
+      mode[i] = ext_mode(J.flag);
+      const bool live = J.qlen > 0 && J.tlen > 0 && !b->P.skip_all;
+      const int nc = live ? ext_ncol(J.qlen, J.tlen, J.w) : 1;
+      shape[i] = ext_shape_id(dual, mode[i], nc, b->P);
+      ncol[i] = nc;
+      foot[i] = (live && mode[i] != 0) ? (((int64_t)(J.qlen + J.tlen - 1) * nc * 16 + 15) & ~(int64_t)15) : 0;
+      if (foot[i] > c->tb_budget)
+        return set_err(KSW2G_E_CAPACITY, "job %d: traceback needs %lld bytes, budget %lld", i, (long long)foot[i],
+                       (long long)c->tb_budget);
+      if (mode[i] != 0) cg += J.qlen + J.tlen + 1;
+      bc += (int64_t)(J.qlen + J.tlen) * (nc > 1 ? 16 * (nc - 1) : 0);
+      return 0;
+    };
+    // over threads in ranges; a range stops at its first failing job, and the first failing job
+    // of the batch is planned again on this thread, which reports it
+    const int64_t grain = 16384;
+    const int nr = (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), (n + grain - 1) / grain));
+    std::vector<int64_t> rcg(nr, 0), rbc(nr, 0);
+    std::vector<int> rfail(nr, -1);
+    parallel_for(nr, 1, [&](int64_t lo, int64_t hi) {
+      for (int64_t t = lo; t < hi; ++t)
+        for (int i = (int)(n * t / nr), e = (int)(n * (t + 1) / nr); i < e; ++i)
+          if (plan(i, rcg[t], rbc[t])) {
+            rfail[t] = i;
+            break;
+          }
+    });
+    for (int t = 0; t < nr; ++t) {
+      if (rfail[t] >= 0) {
+        int64_t a = 0, bb = 0;
+        return plan(rfail[t], a, bb);
+      }
+      cig += rcg[t], band_cells += rbc[t];
+    }
   }
   {  // jobs of the (mode, shape) classes that hold few of them move to the block-split kernel
     std::vector<int> cnt(3 * kNumShapeIds, 0);
@@ -475,7 +502,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   // waves, because every wave ends with the tail of its longest pair (config 2's long
   // pairs ran 3.6x slower in 1 GiB waves).
   int64_t wave_cap = std::max<int64_t>(c->tb_budget / std::max(c->wave_div, 1), 16);
-  if (c->wave_div >= 2 && n > 0 && band_cells / n < kLongCells) wave_cap = std::min<int64_t>(wave_cap, kWaveTarget);
+  if (c->wave_div >= 2 && n > 0 && (double)band_cells / n < kLongCells) wave_cap = std::min<int64_t>(wave_cap, kWaveTarget);
   std::vector<int64_t> tbo(n);
   std::vector<int32_t> ord(n);
   int64_t ordp = 0;

@@ -26,6 +26,7 @@
 #include "../../include/ksw2.h"
 #include "../../include/ksw2_gb300.h"
 #include "batch.h"
+#include "host_parallel.h"
 #include "host_common.h"
 #include "launch.h"
 #include "ungap.cuh"
@@ -228,13 +229,15 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
   t0 = std::chrono::steady_clock::now();
   // ---- stage 3: extz2 on the reversed prefixes ending at ksw_ll's end (pe.c:283-300)
   int64_t used = 0;
+  std::vector<int> by_mt[3];  // the candidates that go on to extz2, per methylation mode
+  for (int i = 0; i < n; ++i) {
+    const ksw2g_rescue_result_t &R = res[i];
+    if (R.ll_done && jobs[i].meth >= 0 && jobs[i].meth <= 2 && R.ll_score >= o.min_dp_max &&
+        R.ll_score >= jobs[i].min_sc)
+      by_mt[jobs[i].meth].push_back(i);
+  }
   for (int mt = 0; mt <= 2; ++mt) {
-    std::vector<int> idx;
-    for (int i = 0; i < n; ++i) {
-      const ksw2g_rescue_result_t &R = res[i];
-      if (R.ll_done && jobs[i].meth == mt && R.ll_score >= o.min_dp_max && R.ll_score >= jobs[i].min_sc)
-        idx.push_back(i);
-    }
+    const std::vector<int> &idx = by_mt[mt];
     if (idx.empty()) continue;
     int8_t mat[25];
     gen_nt4(mat, (int8_t)o.a, (int8_t)o.b, (int8_t)o.b_ts, (int8_t)o.b_ambi, mt);
@@ -282,7 +285,8 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
       if (ksw2g_batch_kernel_ms(eb, &dp, &bt, nullptr, nullptr) == 0) c->rs_dev_ms[1] += dp + bt;
     }
 
-    for (size_t k = 0; k < idx.size(); ++k) {
+    parallel_for((int64_t)idx.size(), 16384, [&](int64_t lo, int64_t hi) {
+    for (int64_t k = lo; k < hi; ++k) {
       const int i = idx[k];
       ksw2g_rescue_result_t &R = res[i];
       const ksw2g_ext_result_t &E = er[k];
@@ -304,6 +308,7 @@ extern "C" int ksw2g_rescue_batch(ksw2g_ctx_t *c, const ksw2g_ref_t *ref, const 
         R.qs = qs, R.qe = qe2;
       }
     }
+    });
     if (cigar) used += u;
   }
   if (cigar_used) *cigar_used = used;
