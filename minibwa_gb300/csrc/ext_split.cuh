@@ -356,47 +356,45 @@ ext_split_kernel(const ksw2g_job *__restrict__ jobs, const int32_t *__restrict__
           // One word a thread: every thread finds the key of its own maximum without a branch,
           // and two warp reductions of the packed (H, key) give the warp's; the cells holding
           // the warp's maximum are those at their thread's maximum where it equals the warp's.
-          const int E = en0 - st0, L4 = E & ~3, o0 = base + 4 * k - st0;
+          const int E = en0 - st0, o0 = base + 4 * k - st0;
           uint32_t lkey = 0xffffffffu;
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             const int32_t h = b == 0 ? H0[0] : b == 1 ? H1[0] : b == 2 ? H2[0] : H3[0];
-            const int o = o0 + b;
-            const uint32_t kk = o == E ? 0u : o < L4 ? ((uint32_t)(1 + (o & 3)) << 24) | (uint32_t)o : (5u << 24) | (uint32_t)o;
-            lkey = h == lmax && b >= lo ? min(lkey, kk) : lkey;
+            lkey = h == lmax && b >= lo ? min(lkey, max_key(o0 + b, E)) : lkey;
           }
           const uint32_t hi = (uint32_t)lmax ^ 0x80000000u, lw = 0xffffffffu - lkey;
           const uint32_t mh = __reduce_max_sync(full, hi);
           const uint32_t ml = __reduce_max_sync(full, hi == mh ? lw : 0u);
           if (lane == 0) xs.wmk[p][wp] = ((uint64_t)mh << 32) | ml;
         } else {
-        const int32_t wmax = __reduce_max_sync(full, lmax);
-        // The key is wanted only where the block's maximum may set a new maximum or z-drop
-        // (ksw_apply_zdrop, ksw2.h:181-197); a warp whose own maximum rules both out cannot
-        // hold the block's maximum on an anti-diagonal that does.
-        const bool need_w = ez_e < 0 || wmax > ez_max || (zdrop >= 0 && ez_max - wmax > zdrop);
-        uint32_t key = 0xffffffffu;
-        if (need_w) {
-          if (lmax == wmax) {
-            const int E = en0 - st0;
-            uint32_t mm = 0;
+          const int32_t wmax = __reduce_max_sync(full, lmax);
+          // The key is wanted only where the block's maximum may set a new maximum or z-drop
+          // (ksw_apply_zdrop, ksw2.h:181-197); a warp whose own maximum rules both out cannot
+          // hold the block's maximum on an anti-diagonal that does.
+          const bool need_w = ez_e < 0 || wmax > ez_max || (zdrop >= 0 && ez_max - wmax > zdrop);
+          uint32_t key = 0xffffffffu;
+          if (need_w) {
+            if (lmax == wmax) {
+              const int E = en0 - st0;
+              uint32_t mm = 0;
 #pragma unroll
-            for (int i = 0; i < K; ++i) {
-              mm |= (H0[i] == wmax ? 1u : 0u) << (4 * i);
-              mm |= (H1[i] == wmax ? 2u : 0u) << (4 * i);
-              mm |= (H2[i] == wmax ? 4u : 0u) << (4 * i);
-              mm |= (H3[i] == wmax ? 8u : 0u) << (4 * i);
+              for (int i = 0; i < K; ++i) {
+                mm |= (H0[i] == wmax ? 1u : 0u) << (4 * i);
+                mm |= (H1[i] == wmax ? 2u : 0u) << (4 * i);
+                mm |= (H2[i] == wmax ? 4u : 0u) << (4 * i);
+                mm |= (H3[i] == wmax ? 8u : 0u) << (4 * i);
+              }
+              if (lo > 0) mm &= lo >= 4 ? ~0xfu : ~((1u << lo) - 1u);
+              while (mm) {
+                const int b = __ffs(mm) - 1;
+                mm &= mm - 1;
+                key = min(key, max_key(base + 4 * (k + NT * (b >> 2)) + (b & 3) - st0, E));
+              }
             }
-            if (lo > 0) mm &= lo >= 4 ? ~0xfu : ~((1u << lo) - 1u);
-            while (mm) {
-              const int b = __ffs(mm) - 1;
-              mm &= mm - 1;
-              key = min(key, max_key(base + 4 * (k + NT * (b >> 2)) + (b & 3) - st0, E));
-            }
+            key = __reduce_min_sync(full, key);
           }
-          key = __reduce_min_sync(full, key);
-        }
-        if (lane == 0) xs.wmk[p][wp] = split_pack(wmax, key);
+          if (lane == 0) xs.wmk[p][wp] = split_pack(wmax, key);
         }
       } else {
         // ---- approximate max: the followed cell's v and u (ksw2_extz2_sse.c:262-278) ----
