@@ -687,9 +687,13 @@ def _timed_run(cmd, cwd, env=None):
 
 def mapper_point(n_pairs=100_000, n_long=16_000):
     """The batched minibwa (minibwa_gb300/mapper) against the stock build of the same reference
-    sources on the same simulated reads, both with all host threads: reads mapped per second of
+    sources on the same simulated reads, all with all host threads: reads mapped per second of
     wall time and the host CPU time each spent, whether their SAM outputs are byte-identical, and
-    the batched run's stages.  Pairs (the short-read preset) and long reads (-x lr)."""
+    the batched run's stages.  Pairs (the short-read preset) and long reads (-x lr).  The
+    relinked build (the stock sources with libksw2gpu.so in place of the ksw2 objects, every DP
+    call one per-call drop-in call) is timed beside them on the first 2,000 pairs and 200 long
+    reads, with the stock build on the same subsets: one pair's DP on the device takes about as
+    long as hundreds of them on a host core, so the full sets would take minutes."""
     import shutil
     import tempfile
     from minibwa_gb300 import mapper, synth
@@ -697,7 +701,8 @@ def mapper_point(n_pairs=100_000, n_long=16_000):
     tree = O.ref_tree()
     if tree is None:
         return {"unavailable": "the reference's sources are not staged (make -C oracle stage REF=...)"}
-    stock = O.build_minibwa_stock()
+    builds = O.build_minibwa(os.path.join(ROOT, "minibwa_gb300"))
+    stock, relinked = builds["stock"], builds["gpu"]
     batch = mapper.build(tree)["batch"]
     d = tempfile.mkdtemp(prefix="mapper_point_")
     threads = os.cpu_count() or 1
@@ -708,18 +713,28 @@ def mapper_point(n_pairs=100_000, n_long=16_000):
         mapper.index(stock, "g.fa", "g", d)
         a, b = synth.mapper_pairs(g, n_pairs)
         synth.write_fasta(os.path.join(d, "p1.fa"), a), synth.write_fasta(os.path.join(d, "p2.fa"), b)
-        synth.write_fasta(os.path.join(d, "long.fa"), synth.mapper_long_reads(g, n_long))
+        long_reads = synth.mapper_long_reads(g, n_long)
+        synth.write_fasta(os.path.join(d, "long.fa"), long_reads)
+        synth.write_fasta(os.path.join(d, "p1s.fa"), a[:2000]), synth.write_fasta(os.path.join(d, "p2s.fa"), b[:2000])
+        synth.write_fasta(os.path.join(d, "longs.fa"), long_reads[:200])
         env = dict(os.environ, MBG_TIMING="1")
-        for name, args, n in (("pairs", ["g", "p1.fa", "p2.fa"], 2 * n_pairs),
-                              ("long_reads", ["-x", "lr", "g", "long.fa"], n_long)):
+        for name, args, n, small, n_small in (
+                ("pairs", ["g", "p1.fa", "p2.fa"], 2 * n_pairs, ["g", "p1s.fa", "p2s.fa"], 4000),
+                ("long_reads", ["-x", "lr", "g", "long.fa"], n_long, ["-x", "lr", "g", "longs.fa"], 200)):
             mapper.map_reads(stock, args, d, threads)  # page in the index and the binary
             so, ts, cs = _timed_run([stock, "map", "-t", str(threads)] + args, d)
             bo, tb, cb = _timed_run([batch, "map", "-t", str(threads)] + args, d, env)
-            if so.returncode != 0 or bo.returncode != 0:
-                return {"unavailable": "minibwa failed: " + (bo.stderr or so.stderr).decode(errors="replace")[-300:]}
+            ro, tr, cr = _timed_run([relinked, "map", "-t", str(threads)] + small, d)
+            so2, ts2, cs2 = _timed_run([stock, "map", "-t", str(threads)] + small, d)
+            if so.returncode != 0 or bo.returncode != 0 or ro.returncode != 0 or so2.returncode != 0:
+                return {"unavailable": "minibwa failed: " +
+                        (bo.stderr or ro.stderr or so.stderr).decode(errors="replace")[-300:]}
             runs[name] = {"reads": n, "batched_reads_s": n / tb, "stock_reads_s": n / ts, "batched_wall_s": tb,
                           "stock_wall_s": ts, "batched_cpu_s": cb, "stock_cpu_s": cs,
-                          "sam_identical_to_stock": bo.stdout == so.stdout,
+                          "relinked": {"reads": n_small, "relinked_reads_s": n_small / tr, "relinked_wall_s": tr,
+                                       "relinked_cpu_s": cr, "stock_reads_s": n_small / ts2, "stock_wall_s": ts2,
+                                       "sam_identical_to_stock": ro.stdout == so2.stdout},
+                          "sam_identical_to_stock": bo.stdout == so.stdout and ro.stdout == so2.stdout,
                           "stages": [ln.split("] ", 1)[1] for ln in bo.stderr.decode().splitlines()
                                      if ln.startswith("[M::mbg]")]}
     finally:
@@ -728,7 +743,8 @@ def mapper_point(n_pairs=100_000, n_long=16_000):
     return {"metric": "reads mapped/s, whole minibwa run (index loaded, SAM written)", "value": p["batched_reads_s"],
             "unit": "reads/s", "sam_identical_to_stock": all(r["sam_identical_to_stock"] for r in runs.values()),
             "workload": f"{n_pairs} simulated 150 nt pairs and {n_long} long reads (1-8 kb, -x lr) from synth on a "
-                        f"12 Mb simulated genome with 800 near-repeats, minibwa map -t {threads}",
+                        f"12 Mb simulated genome with 800 near-repeats, minibwa map -t {threads}; the relinked "
+                        f"per-call build on the first 2,000 pairs and 200 long reads",
             "runs": runs,
             "cpu_baseline": {"value": p["stock_reads_s"], "unit": "reads/s", "cores": threads, "kind": "reference",
                              "sample": f"the stock minibwa built from the reference's sources, same pairs, "
