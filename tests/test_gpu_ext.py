@@ -303,23 +303,42 @@ def _wide_pairs(n, lo, hi, w, flag, dual, seed):
 
 def test_wide_bands_block_kernel(ctx):
     """Bands wider than the widest thread group (long reads' end extension with w up to
-    bw_long): batched alone, mixed with narrow pairs in one batch, and over many waves."""
+    bw_long) on the block-wide kernel (the block-split kernel, which takes such bands by
+    default, is off here): batched alone, mixed with narrow pairs in one batch, with several
+    traceback modes in one batch (their block-wide bins share the wave's scratch, so they run
+    on one stream), and over many waves."""
+    import minibwa_gb300.lib as K
     from minibwa_gb300 import Context
-    for flag in (0x40, 0x00, 0xc2, 0x08, 0x41):
-        for dual in (0, 1):
-            _batch_vs_oracle(ctx, _wide_pairs(6, 1500, 4000, -1, flag, dual, seed=flag + dual))
-    mixed = _wide_pairs(40, 300, 3000, 1200, 0x40, 1, seed=3)   # narrow and wide jobs in one batch
-    _batch_vs_oracle(ctx, mixed)
-    c = Context(0, tb_budget=64 << 20)                           # many waves, two streams
+    prev = K.set_ext_split(0)
     try:
-        _batch_vs_oracle(c, _wide_pairs(12, 1500, 3000, 2500, 0x40, 1, seed=9))
+        for flag in (0x40, 0x00, 0xc2, 0x08, 0x41):
+            for dual in (0, 1):
+                _batch_vs_oracle(ctx, _wide_pairs(6, 1500, 4000, -1, flag, dual, seed=flag + dual))
+        mixed = _wide_pairs(40, 300, 3000, 1200, 0x40, 1, seed=3)   # narrow and wide jobs in one batch
+        _batch_vs_oracle(ctx, mixed)
+        modes = _wide_pairs(12, 1500, 3000, -1, 0x40, 1, seed=5)    # score-only, left and right gaps
+        modes.jobs["flag"] = np.array([0x40, 0x41, 0xc2] * 4, np.int32)
+        _batch_vs_oracle(ctx, modes)
+        c = Context(0, tb_budget=64 << 20)                           # many waves, two streams
+        try:
+            _batch_vs_oracle(c, _wide_pairs(12, 1500, 3000, 2500, 0x40, 1, seed=9))
+        finally:
+            c.close()
     finally:
-        c.close()
+        K.set_ext_split(prev)
 
 
 def test_wide_band_per_call(built):
     import minibwa_gb300.lib as K
     p = _wide_pairs(3, 2000, 3000, 3000, 0x40, 1, seed=21)
+    prev = K.set_ext_split(0)  # the block-wide kernel, not the block-split one
+    try:
+        _per_call_wide(K, p)
+    finally:
+        K.set_ext_split(prev)
+
+
+def _per_call_wide(K, p):
     for i in range(len(p)):
         q, t = p.query(i), p.target(i)
         ez = K.ksw_extd2_sse(q, t, 5, p.mat, p.q, p.e, p.q2, p.e2, 3000, 400, 10, 0x40)
