@@ -74,8 +74,8 @@ static const int kSplitMaxJobs = 304;
 
 static bool use_split(int n_col, int count, bool wide) {
   const int m = g_split.load(std::memory_order_relaxed);
-  if (m == 0 || ext_split_for(n_col) < 0) return false;
-  return m == 1 || wide || (n_col >= kSplitMinCol && count <= kSplitMaxJobs);
+  if (m == 0 || (m < 0 && !wide && (n_col < kSplitMinCol || count > kSplitMaxJobs))) return false;
+  return ext_split_for(n_col) >= 0;
 }
 
 static bool shape_holds(int s, int n_col) {
@@ -354,8 +354,8 @@ int ext_prepare_into(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
 }
 
 // Rough device time of a bin in cycles, to spread the bins of a wave over streams: its
-// longest pair's anti-diagonals at one pair's latency plus all its anti-diagonal words at the
-// whole device's rate.  Measured on a GB300 with one 10 kb extd2 pair: about 2,200 + 140 K
+// longest pair's anti-diagonals at one pair's latency plus its anti-diagonal words (diag_words)
+// at the whole device's rate.  Measured on a GB300 with one 10 kb extd2 pair: about 2,200 + 140 K
 // cycles per anti-diagonal on a group of K words a thread, 1,750 + 85 NW K on a block of NW
 // warps, 8,000 on the block-wide kernel; 1,000,000 config-1 pairs run at about 0.02 cycles per
 // anti-diagonal word on groups, and blocks take about three times the groups' device time per
@@ -373,15 +373,25 @@ static double bin_cost(int shape, int64_t max_diag, double diag_words) {
 // Assign the bins of a wave to its streams, costliest first, each to the stream with the least
 // cost so far (the longest-processing-time rule), and order them that way for launching.  The
 // block-wide kernel's bins share one stream, because they share the wave's scratch.
+// KSW2G_SIDE_STREAMS (0 to kSideStreams) sets how many side streams a wave may use.
+static int side_streams() {
+  static const int n = [] {
+    const char *v = getenv("KSW2G_SIDE_STREAMS");
+    const int k = v && *v ? atoi(v) : kSideStreams;
+    return k < 0 ? 0 : k > kSideStreams ? kSideStreams : k;
+  }();
+  return n;
+}
 static void spread_bins(std::vector<Bin> &bins) {
   std::stable_sort(bins.begin(), bins.end(), [](const Bin &a, const Bin &b) { return a.cost > b.cost; });
   double load[1 + kSideStreams] = {};
   int wide_sub = -1;
+  const int ns = side_streams();
   for (Bin &bn : bins) {
     int s = 0;
     if (bn.shape == kWideShape && wide_sub >= 0) s = wide_sub;
     else
-      for (int i = 1; i <= kSideStreams; ++i)
+      for (int i = 1; i <= ns; ++i)
         if (load[i] < load[s]) s = i;
     if (bn.shape == kWideShape) wide_sub = s;
     load[s] += bn.cost;
@@ -509,8 +519,6 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   const int nshp = kNumShapeIds;  // both lane widths' shapes and the block-wide kernel
   const int nbins = 3 * nshp;
   std::vector<int32_t> bcount(nbins), bpos(nbins);
-  std::vector<int64_t> bmaxd(nbins);
-  std::vector<double> bwords(nbins);
   for (int i = 0; i < n;) {
     Wave wv;
     wv.w0 = i;
@@ -521,24 +529,25 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     wv.tb_bytes = acc;
     std::fill(bcount.begin(), bcount.end(), 0);
     for (int k = wv.w0; k < wv.w1; ++k) ++bcount[mode[srt[k]] * nshp + shape[srt[k]]];
-    std::fill(bmaxd.begin(), bmaxd.end(), 0);
-    std::fill(bwords.begin(), bwords.end(), 0.0);
-    for (int k = wv.w0; k < wv.w1; ++k) {
-      const int j = srt[k], bi = mode[j] * nshp + shape[j];
-      const int64_t nd = std::max<int64_t>((int64_t)ql[j] + tl[j] - 1, 0);
-      bmaxd[bi] = std::max(bmaxd[bi], nd);
-      bwords[bi] += (double)nd * 4.0 * ncol[j];
-    }
     for (int bi = 0; bi < nbins; ++bi) {
       bpos[bi] = (int32_t)ordp;
       if (bcount[bi]) {
-        wv.bins.push_back(Bin{bi / nshp, bi % nshp, ordp, bcount[bi], bin_cost(bi % nshp, bmaxd[bi], bwords[bi]), 0});
+        wv.bins.push_back(Bin{bi / nshp, bi % nshp, ordp, bcount[bi], 0.0, 0});
         wv.any_cig |= bi / nshp != 0;
       }
       ordp += bcount[bi];
     }
     for (int k = wv.w0; k < wv.w1; ++k) ord[bpos[mode[srt[k]] * nshp + shape[srt[k]]]++] = srt[k];
-    spread_bins(wv.bins);
+    if (wv.bins.size() > 1) {
+      // a bin's first job is its longest (the order is longest first); its other jobs are
+      // counted at half that length
+      for (Bin &bn : wv.bins) {
+        const int j = ord[bn.order_off];
+        const int64_t nd = std::max<int64_t>((int64_t)ql[j] + tl[j] - 1, 0);
+        bn.cost = bin_cost(bn.shape, nd, 0.5 * (double)nd * 4.0 * ncol[j] * bn.count);
+      }
+      spread_bins(wv.bins);
+    }
     b->waves.push_back(wv);
   }
   b->n_counters = 0;
