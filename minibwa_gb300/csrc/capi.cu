@@ -420,6 +420,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   std::vector<int64_t> qo(n), to(n);
   std::vector<int32_t> ql(n), tl(n);
   std::vector<int> shape(n), mode(n), ncol(n);
+  std::vector<double> dwords(n);  // anti-diagonals x window words of every job (bin costs)
   std::vector<int64_t> foot(n);
   int64_t cig = 0, wide_max = 0;
   int64_t band_cells = 0;  // sum of (qlen + tlen) x band width: the batch's size class
@@ -441,6 +442,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
       const int nc = live ? ext_ncol(J.qlen, J.tlen, J.w) : 1;
       shape[i] = ext_shape_id(dual, mode[i], nc, b->P);
       ncol[i] = nc;
+      dwords[i] = (double)std::max(J.qlen + J.tlen - 1, 0) * 4.0 * nc;
       foot[i] = (live && mode[i] != 0) ? (((int64_t)(J.qlen + J.tlen - 1) * nc * 16 + 15) & ~(int64_t)15) : 0;
       if (foot[i] > c->tb_budget)
         return set_err(KSW2G_E_CAPACITY, "job %d: traceback needs %lld bytes, budget %lld", i, (long long)foot[i],
@@ -519,6 +521,7 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
   const int nshp = kNumShapeIds;  // both lane widths' shapes and the block-wide kernel
   const int nbins = 3 * nshp;
   std::vector<int32_t> bcount(nbins), bpos(nbins);
+  std::vector<double> bwords(nbins);
   for (int i = 0; i < n;) {
     Wave wv;
     wv.w0 = i;
@@ -528,7 +531,11 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     wv.w1 = i;
     wv.tb_bytes = acc;
     std::fill(bcount.begin(), bcount.end(), 0);
-    for (int k = wv.w0; k < wv.w1; ++k) ++bcount[mode[srt[k]] * nshp + shape[srt[k]]];
+    std::fill(bwords.begin(), bwords.end(), 0.0);
+    for (int k = wv.w0; k < wv.w1; ++k) {
+      const int j = srt[k], bi = mode[j] * nshp + shape[j];
+      ++bcount[bi], bwords[bi] += dwords[j];
+    }
     for (int bi = 0; bi < nbins; ++bi) {
       bpos[bi] = (int32_t)ordp;
       if (bcount[bi]) {
@@ -539,12 +546,9 @@ int ext_prepare_segs(ksw2g_ctx *c, ksw2g_batch *b, int dual, int8_t m, const int
     }
     for (int k = wv.w0; k < wv.w1; ++k) ord[bpos[mode[srt[k]] * nshp + shape[srt[k]]]++] = srt[k];
     if (wv.bins.size() > 1) {
-      // a bin's first job is its longest (the order is longest first); its other jobs are
-      // counted at half that length
-      for (Bin &bn : wv.bins) {
+      for (Bin &bn : wv.bins) {  // a bin's first job is its longest (the order is longest first)
         const int j = ord[bn.order_off];
-        const int64_t nd = std::max<int64_t>((int64_t)ql[j] + tl[j] - 1, 0);
-        bn.cost = bin_cost(bn.shape, nd, 0.5 * (double)nd * 4.0 * ncol[j] * bn.count);
+        bn.cost = bin_cost(bn.shape, std::max<int64_t>((int64_t)ql[j] + tl[j] - 1, 0), bwords[bn.mode * nshp + bn.shape]);
       }
       spread_bins(wv.bins);
     }
