@@ -119,3 +119,14 @@ def test_missing_device_fails_loudly(mp):
     assert out.returncode != 0
     assert b"ksw2g_ctx_create" in out.stderr
     assert not any(ln and not ln.startswith(b"@") for ln in out.stdout.splitlines())
+
+
+@pytest.mark.parametrize("split", ["0", "1"])
+def test_long_reads_either_kernel_choice(mp, split):
+    """The extension kernels a batch picks (KSW2G_SPLIT: 0 thread groups and the block-wide kernel
+    only, 1 the block-split kernel for every band it holds) do not change the SAM."""
+    from minibwa_gb300 import mapper
+    args = ["-x", "lr", "g", "long.fa"]
+    sa, _ = mapper.map_reads(mp["stock"]["stock"], args, mp["dir"], 16)
+    sb, _ = mapper.map_reads(mp["batch"]["batch"], args, mp["dir"], 16, env=dict(os.environ, KSW2G_SPLIT=split))
+    assert sa == sb
