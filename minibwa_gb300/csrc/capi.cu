@@ -775,6 +775,17 @@ static int chunk_jobs(int n, const ksw2g_job_t *jobs) {
   return n > 0 && cells / n > kLongCells ? kChunkJobsLong : kChunkJobs;
 }
 
+// Chunk boundaries of a one-shot call of n jobs in chunks of about `per` jobs.  The first chunk
+// is an eighth of that (at least 1,024 jobs), so that the device starts on it while the host
+// still prepares the second.
+static std::vector<int> chunk_starts(int n, int per) {
+  std::vector<int> st{0};
+  const int first = std::min(per, std::max(1024, per / 8));
+  for (int64_t j = first; j < n; j += per) st.push_back((int)j);
+  st.push_back(n);
+  return st;
+}
+
 static int sub_ctx(ksw2g_ctx *c, int i, ksw2g_ctx **out) {
   if (!c->sub[i]) {
     int rc = ksw2g_ctx_create(c->device, &c->sub[i]);
@@ -794,8 +805,8 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
                              const uint8_t *tbuf, int64_t tbuf_len, ksw2g_ext_result_t *res, uint32_t *cigar,
                              int64_t cigar_cap, int64_t *cigar_used, const RefTargets *rt = nullptr) {
   const int cj_jobs = chunk_jobs(n, jobs);
-  const int nch = (n + cj_jobs - 1) / cj_jobs;
-  const int per = (n + nch - 1) / nch;
+  const std::vector<int> cst = chunk_starts(n, cj_jobs);
+  const int nch = (int)cst.size() - 1;
   ksw2g_ctx *sc[kOneShotDepth];
   int rc;
   for (int i = 0; i < kOneShotDepth; ++i)
@@ -810,7 +821,7 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
     pending[s] = -1;
     ksw2g_ctx *x = sc[s];
     ksw2g_batch *b = x->scratch;
-    const int j0 = ch * per;
+    const int j0 = cst[ch];
     struct {
       unsigned long long cursor;
       int err, pad;
@@ -832,7 +843,7 @@ static int ext_batch_chunked(ksw2g_ctx *c, int dual, int8_t m, const int8_t *mat
   for (int ch = 0; ch < nch && !rc; ++ch) {
     const int s = ch % kOneShotDepth;
     if ((rc = finish(s))) break;
-    const int j0 = ch * per, nj = std::min(per, n - j0);
+    const int j0 = cst[ch], nj = cst[ch + 1] - j0;
     ksw2g_ctx *x = sc[s];
     ksw2g_batch *b = x->scratch;
     // upload only the part of the sequence buffers this chunk's jobs read
@@ -1245,8 +1256,8 @@ static const int kLLChunkJobs = 262144;
 static int ll_batch_chunked(ksw2g_ctx *c, int size, int m, const int8_t *mat, int gapo, int gape, int n,
                             const ksw2g_ll_job_t *jobs, const uint8_t *qbuf, int64_t qbuf_len, const uint8_t *tbuf,
                             int64_t tbuf_len, ksw2g_ll_result_t *res) {
-  const int nch = (n + kLLChunkJobs - 1) / kLLChunkJobs;
-  const int per = (n + nch - 1) / nch;
+  const std::vector<int> cst = chunk_starts(n, kLLChunkJobs);
+  const int nch = (int)cst.size() - 1;
   ksw2g_ctx *sc[kOneShotDepth];
   int rc;
   for (int i = 0; i < kOneShotDepth; ++i)
@@ -1257,12 +1268,12 @@ static int ll_batch_chunked(ksw2g_ctx *c, int size, int m, const int8_t *mat, in
     const int ch = pending[s];
     if (ch < 0) return 0;
     pending[s] = -1;
-    return ksw2g_ll_fetch(sc[s], sc[s]->scratch, res ? res + (size_t)ch * per : nullptr);
+    return ksw2g_ll_fetch(sc[s], sc[s]->scratch, res ? res + cst[ch] : nullptr);
   };
   for (int ch = 0; ch < nch && !rc; ++ch) {
     const int s = ch % kOneShotDepth;
     if ((rc = finish(s))) break;
-    const int j0 = ch * per, nj = std::min(per, n - j0);
+    const int j0 = cst[ch], nj = cst[ch + 1] - j0;
     int64_t qlo = qbuf_len, qhi = 0, tlo = tbuf_len, thi = 0;
     for (int i = j0; i < j0 + nj; ++i) {
       const ksw2g_ll_job_t &J = jobs[i];
