@@ -482,6 +482,14 @@ def measure(args, w, ctx, dev, rank, world, steps, warmup, int_peak, with_cpu, s
     L = K.load_library()
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
 
+    # config 2 runs with an autotuned thread-group shape and lane width per band class: the tuner
+    # times every eligible choice on a sample of each class first (not timed here)
+    tuned = {}
+    if w.name == "cfg2":
+        from minibwa_gb300 import autotune
+        for s in w.sets:
+            tuned.update(autotune.tune_ext(ctx, s, sample=16384, reps=2))
+
     # ---------------- value: resident inputs, device timing
     batches = [prepare(ctx, s) for s in w.sets]
     graph = Graph(ctx, batches) if len(batches) > 1 else None
@@ -633,6 +641,11 @@ def measure(args, w, ctx, dev, rank, world, steps, warmup, int_peak, with_cpu, s
         cb, _, outs = cpu_baseline(w, sample)
         out["cpu_baseline"] = cb
         out["parity_vs_cpu"] = parity_vs_cpu(w, results, outs, cb["kind"])
+    if tuned:
+        from minibwa_gb300 import autotune
+        out["autotuned"] = {f"{'extd2' if d else 'extz2'} mode {md} n_col {c}":
+                            f"{g}x{k} {'16-bit' if w16 else 'byte'} lanes" for (d, md, c), (g, k, w16, _) in tuned.items()}
+        autotune.reset(tuned)  # later workloads of the run start from the default shapes
     return out
 
 
@@ -797,7 +810,7 @@ def main():
                                                                   sizes_only=True).set_sizes), world),
         }
         for k in ("bytes_per_step", "gcups", "cells_per_step", "gpu_launches", "roofline", "roofline_hbm", "e2e",
-                  "clocks", "cpu_baseline", "parity_vs_cpu"):
+                  "clocks", "cpu_baseline", "parity_vs_cpu", "autotuned"):
             if k in m:
                 line[k] = m[k]
         if extra:
