@@ -297,3 +297,24 @@ def test_emulated_split_kernel_edges(emu):
             exp, _ = O.extz(dual, qs[i], ts[i], 5, mat, 6, 1, 20 if dual else 6, 1, 40, 100, 5, flag)
             assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, i)
             assert cig[i] == exp["cigar"], (dual, flag, i)
+
+
+def test_emulated_split_kernel_wide_words(emu):
+    """Two and four words a thread (the shapes of bands wider than the widest group), where
+    each warp reduces its maximum first and only the warps that may hold the block's maximum
+    look for its key; full-band extension (w < 0) of pairs of 100-300 bases."""
+    from minibwa_gb300 import synth
+    from oracle import oracle as O
+    p = synth.config1(3, seed=43)
+    qs = [p.query(i) for i in range(len(p))]
+    ts = [p.target(i) for i in range(len(p))]
+    for dual, flag, split in ((1, 0x40, (2, 4)), (0, 0x02, (3, 2)), (1, 0x01, (2, 2))):
+        q2, e2 = (24, 1) if dual else (12, 2)
+        nc = max(emu.ncol(len(a), len(b), -1) for a, b in zip(qs, ts))
+        if 32 * split[0] * split[1] < 4 * nc:
+            continue
+        res, cig = emu.ext(dual, 5, p.mat, 12, 2, q2, e2, qs, ts, -1, 100, 10, flag, split=split)
+        for i in range(len(qs)):
+            exp, _ = O.extz(dual, qs[i], ts[i], 5, p.mat, 12, 2, q2, e2, -1, 100, 10, flag)
+            assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, split, i)
+            assert cig[i] == exp["cigar"], (dual, flag, split, i)
