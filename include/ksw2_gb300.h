@@ -332,7 +332,8 @@ int ksw2g_ext_get_split(void);
  *
  * Rejects (KSW2G_E_CAPACITY, message in ksw2g_last_error()) any call whose
  * scratch (traceback rows, plus 64 bytes per job and at most 1 KiB) exceeds
- * KSW2G_NOALLOC_SCRATCH_BYTES.  The first call on each device looks up the
+ * KSW2G_NOALLOC_SCRATCH_BYTES, and (KSW2G_E_BAND) bands wider than 512 blocks of
+ * 16 cells; bands wider than 64 blocks run one pair per block.  The first call on each device looks up the
  * array's device address; make that first call before any stream capture.
  * The address is kept for the life of the process, so calls after a
  * cudaDeviceReset of that device are not supported.

@@ -116,8 +116,12 @@ extern "C" int ksw2g_ext_noalloc(int dual, int8_t m, const int8_t *mat, int8_t q
     }
     if (mode) cig += (int64_t)J.qlen + J.tlen + 1;
   }
-  const int shape = ext_shape_for(max_nc);
-  if (shape < 0) return fail(KSW2G_E_BAND, "ksw2g_ext_noalloc: band of %d blocks exceeds the widest kernel", max_nc);
+  int shape = ext_shape_for(max_nc);
+  if (shape < 0) {  // wider than every thread group: one pair per block, which needs no scratch of its own
+    const int sp = ext_split_for(max_nc);
+    if (sp < 0) return fail(KSW2G_E_BAND, "ksw2g_ext_noalloc: band of %d blocks exceeds the widest kernel", max_nc);
+    shape = kSplitBase + sp;
+  }
   const size_t o_tbo = kCounters, o_bt = up256(o_tbo + (size_t)n_jobs * 8);
   const size_t o_jobs = up256(o_bt + (size_t)n_jobs * sizeof(ksw2g_bt));
   const size_t o_tb = up256(o_jobs + (size_t)n_jobs * sizeof(ksw2g_job));

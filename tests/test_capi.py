@@ -82,7 +82,13 @@ def test_synthetic_workloads_are_seeded(built):
 
 def test_noalloc_checks_job_descriptors_before_device_work(built):
     """ksw2g_ext_noalloc refuses descriptors that would read past the caller's arena, or that
-    break the padded layout, with KSW2G_E_ARG before it touches a device (so this runs here)."""
+    break the padded layout, with KSW2G_E_ARG before it touches a device (so this runs here).
+    The device buffers passed are placeholders, and the calls with valid descriptors go on to
+    the device: the test runs only where no GPU is visible, where those calls end with no
+    device instead of launching on the placeholders."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: the valid descriptors would launch on placeholder pointers")
     from minibwa_gb300.lib import EXT_JOB, gen_nt4_mat, load_library
     L = load_library()
     f = L.ksw2g_ext_noalloc
@@ -102,3 +108,12 @@ def test_noalloc_checks_job_descriptors_before_device_work(built):
         else:
             assert rc == -2, (arena_len, qoff, qlen, rc)
     assert f(1, 5, mat.ctypes.data, 12, 2, 24, 1, -1, jobs.ctypes.data, 16, 4096, 16, 16, 1 << 20, None) == -2
+    # bands: up to 512 blocks of 16 cells pass (wider than 64 run one pair per block), wider ones
+    # are refused with KSW2G_E_BAND, also before any device work
+    for qlen, band_ok in ((2500, True), (9000, False)):
+        j = jobs.copy()
+        toff = 32 + ((qlen + 15) & ~15) + 64
+        j["qoff"], j["qlen"], j["toff"], j["tlen"], j["w"], j["flag"] = 32, qlen, toff, qlen, -1, 0x41
+        rc = f(1, 5, mat.ctypes.data, 12, 2, 24, 1, 1, j.ctypes.data, 16, 4 * qlen, 16, 16, 1 << 20, None)
+        assert rc != -2, (qlen, rc)  # the descriptor is valid
+        assert (rc != -3) if band_ok else (rc == -3), (qlen, rc)

@@ -88,6 +88,20 @@ def test_noalloc_matches_batch_on_consecutive_calls(L):
         ctx.close()
 
 
+def test_noalloc_wide_bands(L):
+    """Bands wider than the widest thread group run one pair per block, with no scratch beyond
+    the traceback rows."""
+    from minibwa_gb300 import Context, synth
+    p = synth.ext_pairs(2, dict(synth.SPEC_LONG, clip_lo=1500, clip_hi=2500), -1, 400, 10, 0x40, True, seed=80)
+    ctx = Context(0)
+    try:
+        res, cig = _run_noalloc(L, p)
+        ref, rcig = ctx.ext_batch(p.dual, 5, p.mat, p.q, p.e, p.q2, p.e2, p.jobs, p.qbuf, p.tbuf)
+        _check_equal(res, cig, ref, rcig)
+    finally:
+        ctx.close()
+
+
 def test_noalloc_rejects_oversized_batches(L):
     from minibwa_gb300 import synth
     p = synth.config1(3000, seed=79)  # about 170 MB of traceback rows: beyond the fixed scratch
