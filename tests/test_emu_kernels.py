@@ -299,6 +299,36 @@ def test_emulated_split_kernel_edges(emu):
             assert cig[i] == exp["cigar"], (dual, flag, i)
 
 
+def test_emulated_split_kernel_stops(emu):
+    """Pairs stopped early -- z-drop under the exact and the approximate max, the extd2 early
+    stop, bands that empty -- at every point of a pair, from the first anti-diagonals to just
+    before the last, on one and two warps and one and two words a thread."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(47)
+    mat = np.array([2 if i // 5 == i % 5 else -4 for i in range(25)], np.int8)
+    mat[20:25] = -1
+    mat[4::5] = -1
+    qs, ts = [], []
+    for i in range(36):
+        base = rng.integers(0, 4, 170).astype(np.uint8)
+        q, t = base[: int(rng.integers(8, 150))].copy(), base[: int(rng.integers(8, 150))].copy()
+        cut = int(rng.integers(0, max(len(q), 1)))
+        q[cut:] = rng.integers(0, 4, len(q) - cut)  # a junk tail from a random point
+        if i % 3 == 0:
+            t = t[: max(1, len(q) // 3)]  # bands that empty early
+        qs.append(q), ts.append(t)
+    for dual, flag, w, zdrop, split in ((1, 0x40, 12, 8, (1, 1)), (0, 0x40, 30, 15, (2, 1)),
+                                        (1, 0x00, 20, 5, (1, 2)), (0, 0x01, 6, 10, (2, 1)),
+                                        (1, 0x18, 25, 12, (1, 1)), (0, 0x18, 40, 6, (2, 1)),
+                                        (1, 0x41, 60, 30, (1, 2)), (0, 0x42, 3, 4, (1, 1))):
+        q2, e2 = (24, 1) if dual else (4, 2)
+        res, cig = emu.ext(dual, 5, mat, 4, 2, q2, e2, qs, ts, w, zdrop, 3, flag, split=split)
+        for i in range(len(qs)):
+            exp, _ = O.extz(dual, qs[i], ts[i], 5, mat, 4, 2, q2, e2, w, zdrop, 3, flag)
+            assert {f: int(res[i][f]) for f in EXT_FIELDS} == {f: exp[f] for f in EXT_FIELDS}, (dual, flag, w, i)
+            assert cig[i] == exp["cigar"], (dual, flag, w, i)
+
+
 def test_emulated_split_kernel_wide_words(emu):
     """Two and four words a thread (the shapes of bands wider than the widest group), where
     each warp reduces its maximum first and only the warps that may hold the block's maximum
