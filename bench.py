@@ -483,12 +483,14 @@ def measure(args, w, ctx, dev, rank, world, steps, warmup, int_peak, with_cpu, s
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
 
     # config 2 runs with an autotuned thread-group shape and lane width per band class: the tuner
-    # times every eligible choice on a sample of each class first (not timed here)
+    # times every eligible choice on a sample of each class first (not timed here); --lanes 0 or 1
+    # keeps the tuner to that lane width
     tuned = {}
     if w.name == "cfg2":
         from minibwa_gb300 import autotune
         for s in w.sets:
-            tuned.update(autotune.tune_ext(ctx, s, sample=16384, reps=2))
+            lanes = True if args.lanes < 0 else args.lanes
+            tuned.update(autotune.tune_ext(ctx, s, sample=16384, reps=2, lanes=lanes))
 
     # ---------------- value: resident inputs, device timing
     batches = [prepare(ctx, s) for s in w.sets]

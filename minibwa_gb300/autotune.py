@@ -51,8 +51,9 @@ def _time_batch(ctx, b, reps):
 
 
 def tune_ext(ctx, pairs, sample=32768, reps=3, min_class=64, seed=1, lanes=True):
-    """Tune the shape (and with `lanes` the lane width) of every n_col_ class of `pairs` (a
-    synth.Pairs or anything with the same fields).  Installs the winners and returns
+    """Tune the shape (and with `lanes` True the lane width; 0 or 1 keeps byte or 16-bit lanes) of
+    every n_col_ class of `pairs` (a synth.Pairs or anything with the same fields).  Installs the
+    winners and returns
     {(dual, mode, ncol): (G, K, w16, ms_per_pair_by_choice)}, choices keyed (G, K, w16); a
     scoring the 16-bit lanes cannot hold runs those choices on byte lanes, so they tie.
 
@@ -66,6 +67,7 @@ def tune_ext(ctx, pairs, sample=32768, reps=3, min_class=64, seed=1, lanes=True)
     nc = ncol(jobs["qlen"].astype(np.int64), jobs["tlen"].astype(np.int64), jobs["w"].astype(np.int64))
     modes = np.array([mode_of(int(f)) for f in jobs["flag"]])
     rng = np.random.default_rng(seed)
+    widths = (0, 1) if lanes is True else (int(lanes),)
     table = {}
     for md in np.unique(modes):
         for c in np.unique(nc[modes == md]):
@@ -78,7 +80,7 @@ def tune_ext(ctx, pairs, sample=32768, reps=3, min_class=64, seed=1, lanes=True)
             for s, (g, k) in enumerate(shp):
                 if g * k < 4 * int(c):
                     continue
-                for w16 in ((0, 1) if lanes else (0,)):
+                for w16 in widths:
                     L.ksw2g_ext_set_shape(int(pairs.dual), int(md), int(c), int(c), s + w16 * len(shp))
                     b = ExtBatch(ctx, sub.dual, 5, sub.mat, sub.q, sub.e, sub.q2, sub.e2, sub.jobs, sub.qbuf,
                                  sub.tbuf)
